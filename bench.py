@@ -1,0 +1,297 @@
+"""Benchmark of the batched MD-DPD step: atom-steps/s on one GB300 (or N GPUs, one replica set each).
+
+Workload: 256 independent brush channels drawn from the seed (grafting density U[0.05,0.3],
+chain length U{10..100}, channel width U[10,40], box U[15,40], solvent to 0.8, WCA + FENE + DPD
+gamma=5, kT=1, dt=0.005), ~4.7M particles, batched in one context, mixed precision (FP32 pair and
+bond arithmetic on fixed-point positions, FP64 integration), graph-captured 10-step chunks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision mixed|fp64]
+
+A step is one full MD step of all replicas.  `value` times K steps with the state resident on the
+device (CUDA events on the library's stream).  `e2e` times the same steps through the C ABI with
+the state owned by pinned host buffers: every 10-step chunk uploads r, v, a from the host
+(mfa_set_state, which also re-sorts), runs the chunk and reads r, v, a and the energies back.
+The working set (~1.5 GB) is far larger than the 129 MB L2, so no flush is needed between steps.
+`--impl reference` times the restated reference CPU path (the C/OpenMP oracle: linked cells,
+schedule(static,10), per-thread force arrays) on the host cores on a bounded sample of replicas.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s on 1 GB300: batched FP32-force vs plain FP64 (force rel err<=1e-5)"
+UNIT = "atom-steps/s"
+CHUNK = 10
+# algorithmic bytes per particle of the pair kernel (mixed): int4 position + float4 velocity in,
+# three FP64 force components out
+PAIR_BYTES = {"mixed": 16 + 16 + 24, "fp64": 32 + 32 + 24}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if "Active" in v and "Not" not in v})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_workload(seed, n_rep):
+    from mfa_brush_gb300 import configs
+    reps = configs.replicas(n_rep, seed)
+    return configs.wca_params(gamma=5.0, kT=1.0, dt=0.005), reps
+
+
+def cpu_sample(reps, p, steps, warmup, threads):
+    """Restated reference CPU path on the given replicas: (atom-steps/s, atom-steps, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    tot_n, tot_t = 0, 0.0
+    for (s, a_type, r0, v) in reps:
+        o = oracle.Oracle(p, s, a_type, r0, v)
+        if warmup:
+            o.step(warmup, threads, 0)
+        t0 = time.perf_counter()
+        o.step(steps, threads, 0)
+        tot_t += time.perf_counter() - t0
+        tot_n += s.n_part * steps
+        o.close()
+    return tot_n / tot_t, tot_n, tot_t
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    p, reps = make_workload(args.seed, args.replicas)
+    # bounded sample: the first replicas up to ~80k particles, so K steps finish in a few minutes
+    sample, n = [], 0
+    for r in reps:
+        if n > 80000:
+            break
+        sample.append(r)
+        n += r[0].n_part
+    v, an, t = cpu_sample(sample, p, args.steps, args.warmup, threads)
+    desc = "%d of %d replicas (%d particles), %d timed steps after %d warm-up" % (
+        len(sample), len(reps), n, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded brush channels)",
+            "config": {"workload": "256 uneven brush-channel replicas (sample)", "replicas": len(sample),
+                       "particles": n, "precision": "fp64", "l2_flush": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=60)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--replicas", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel-steps", type=int, default=20)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        r = run_reference(args, rank, world)
+        if dist is not None:
+            dist.destroy_process_group()
+        return r
+
+    from mfa_brush_gb300 import build, md
+    build.build()
+    p, reps = make_workload(args.seed + 7919 * rank, args.replicas)
+    from mfa_brush_gb300 import configs
+    systems, a_type, r0, v = configs.concat(reps)
+    n_atoms = int(sum(s.n_part for s in systems))
+    g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=0.3)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up (also captures the 10-step graph)
+    done = 0
+    while done < args.warmup:
+        g.step(CHUNK)
+        done += CHUNK
+    g.synchronize()
+    barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    l0 = g.launch_count()
+    g.synchronize()
+    g.event_record(0)
+    for _ in range(args.steps // CHUNK):
+        g.step(CHUNK)
+    g.event_record(1)
+    ms = g.event_elapsed(0, 1)
+    g.synchronize()
+    clocks = clk.stop()
+    launches = g.launch_count() - l0
+    t = ms / 1000.0
+    if dist is not None:
+        import torch
+        tt = torch.tensor([t], dtype=torch.float64, device="cuda:%d" % local if torch.cuda.is_available() else "cpu")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = n_atoms * world * args.steps / t
+
+    # per-kernel device times (un-graphed, events around each kernel family)
+    kt = g.kernel_times(args.kernel_steps)
+    hbm, peak_kind = peaks()
+    t_pair = kt["pair"][0] / 1000.0
+    achieved = PAIR_BYTES[args.precision] * n_atoms / t_pair / 1e9 if t_pair > 0 else 0.0
+
+    # end-to-end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(g, n_atoms, args, world, dist)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded brush channels)",
+            "config": {"workload": "256 uneven brush-channel replicas, WCA+FENE+DPD, batched",
+                       "replicas": len(systems) * world, "particles_per_gpu": n_atoms,
+                       "precision": args.precision, "chunk_steps": CHUNK, "skin": 0.3,
+                       "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
+                       "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
+            "gpu_launches": int(launches),
+            "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "kernel": "k_pair (mixed)",
+                         "peak_kind": peak_kind},
+            "clocks": clocks}
+    if e2e is not None:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample, n = [], 0
+        for r in reps:
+            if n > 60000:
+                break
+            sample.append(r)
+            n += r[0].n_part
+        cv, an, ct = cpu_sample(sample, p, 40, 5, threads)
+        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d replicas, %d particles, 40 steps (restated reference "
+                                          "OpenMP path)" % (len(sample), n)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(g, n_atoms, args, world, dist):
+    import torch
+    from mfa_brush_gb300 import abi
+    shape = (n_atoms, 3)
+    hr = torch.empty(shape, dtype=torch.float64, pin_memory=torch.cuda.is_available()).numpy()
+    hv = torch.empty(shape, dtype=torch.float64, pin_memory=torch.cuda.is_available()).numpy()
+    ha = torch.empty(shape, dtype=torch.float64, pin_memory=torch.cuda.is_available()).numpy()
+    lib = abi.load_library()
+    dp = abi.dptr
+    abi.check(lib.mfa_sync_to_host(g.ctx, dp(hr), dp(hv), dp(ha), None), g.ctx)
+    e = (abi.Energies * g.nrep)()
+    chunks = max(1, min(args.steps, 100) // CHUNK)
+    # one untimed round trip
+    abi.check(lib.mfa_set_state(g.ctx, dp(hr), dp(hv), dp(ha)), g.ctx)
+    g.step(CHUNK)
+    abi.check(lib.mfa_sync_to_host(g.ctx, dp(hr), dp(hv), dp(ha), None), g.ctx)
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(chunks):
+        abi.check(lib.mfa_set_state(g.ctx, dp(hr), dp(hv), dp(ha)), g.ctx)  # H2D
+        g.step(CHUNK)
+        abi.check(lib.mfa_sync_to_host(g.ctx, dp(hr), dp(hv), dp(ha), None), g.ctx)  # D2H
+        abi.check(lib.mfa_get_energies(g.ctx, e), g.ctx)
+    t = time.perf_counter() - t0
+    if dist is not None:
+        tt = torch.tensor([t], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    steps = chunks * CHUNK
+    bytes_state = 3 * 3 * 8 * n_atoms
+    return {"value": n_atoms * world * steps / t, "unit": UNIT,
+            "h2d_bytes_per_step": bytes_state // CHUNK,
+            "d2h_bytes_per_step": (bytes_state + g.nrep * 104) // CHUNK,
+            "steps": steps, "pattern": "per 10-step chunk: r,v,a H2D (mfa_set_state) + mfa_step(10) + "
+                                       "r,v,a D2H (mfa_sync_to_host) + energies"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,269 @@
+"""Seeded synthetic brush-channel configurations (the reference generates its own with gen_brush.f90;
+none of its published inputs match these workloads).
+
+Particles are laid on a simple-cubic lattice filling the channel interior (z in [0.9, D-0.9]), with
+spacing chosen from the target density, so that no two beads start closer than ~0.95 sigma and
+the first steps need no force switch-on.  Brush chains are lattice self-avoiding walks grown from
+anchor sites drawn uniformly at random on the first and last z layer (first half of the chains on
+the bottom wall, second half on the top wall, heads = bead 1 of each chain), biased away from the
+wall; free (melt) chains are grown the same way from random free sites; solvent beads take
+uniformly random free sites until the total density is reached.  Velocities are Maxwell-Boltzmann
+at kT (heads at rest).  Order of particles follows the reference: brush chains, then melt /
+solvent chains, then particle-4 chains (init_system.f90:172-187).
+
+Workloads (sizes from the project's benchmark definitions):
+  * replicas(256, seed)  -- 256 uneven WCA+FENE+DPD channels, grafting density U[0.05,0.3],
+    N U{10..100}, D U[10,40], L U[15,40], solvent to 0.8 (a replica whose brush alone would
+    exceed 70 % of its beads is redrawn from the same stream);
+  * small_channel()      -- a 20x20x20 channel with 40 chains of 30 beads per wall and solvent
+    to 0.8, the plain-FP64 reference-scale case.
+"""
+import numpy as np
+
+from . import abi, md
+
+# lattice moves: 6 face neighbours (bond a), then 12 edge neighbours (bond sqrt(2) a < R0), the
+# latter with a small weight so a walk only uses them to escape a dead end
+_NEIGH = np.array([[0, 0, 1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, -1]] +
+                  [[dx, dy, dz] for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)
+                   if abs(dx) + abs(dy) + abs(dz) == 2], np.int64)
+_NW = len(_NEIGH)
+_EDGE_W = 1e-3
+
+
+Z_LO = 0.9  # first/last lattice layer: the repulsive 9-3 wall force there is ~100 eps/sigma
+
+
+def _lattice(L, D, n_sites_min, z_lo=Z_LO):
+    """Lattice dims (nx, nz) and spacings covering [0,L)^2 x [z_lo, D-z_lo] with at least
+    n_sites_min sites strictly between the two anchor layers (z index 0 and nz-1)."""
+    a = (L * L * max(D - 2 * z_lo, 0.5) / max(n_sites_min, 1)) ** (1.0 / 3.0)
+    for _ in range(400):
+        nx = max(3, int(L / a))
+        nz = max(3, int((D - 2 * z_lo) / a) + 1)
+        if nx * nx * (nz - 2) >= n_sites_min:
+            break
+        a *= 0.99
+    ax = L / nx
+    az = (D - 2 * z_lo) / (nz - 1)
+    return nx, nz, ax, az
+
+
+def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=None, kT=1.0,
+                  solvent_type=3, melt_type=3, max_fill=0.97):
+    """One replica: returns (abi.System, a_type[n], r0[n,3], v[n,3]).  Types are the reference's:
+    1 head, 2 brush bead, 3 melt/solvent."""
+    rng = np.random.default_rng(seed)
+    n_chain = 2 * int(round(sigma_g * L * L))
+    n_brush = n_chain * n_mon
+    n_total = int(round(rho * L * L * D))
+    if n_chain_d is None:
+        n_chain_d = max(0, (n_total - n_brush) // n_mon_d)
+    n_melt = n_chain_d * n_mon_d
+    n = n_brush + n_melt
+    nx, nz, ax, az = _lattice(L, D, int(np.ceil((n - n_chain) / max_fill)))
+    occ = np.zeros((nx, nx, nz), bool)
+    # the first and last layer hold the brush heads only; no other bead may enter them
+    occ[:, :, 0] = True
+    occ[:, :, nz - 1] = True
+    sites = np.zeros((n, 3), np.int64)
+
+    def regrow(pos, ci, k, w0):
+        """Serial self-avoiding regrowth of beads 1..k of chain ci (its old sites are freed)."""
+        old = pos[ci, 1:k]
+        occ[old[:, 0], old[:, 1], old[:, 2]] = False
+        for _ in range(200):
+            placed = []
+            cur = pos[ci, 0]
+            ok = True
+            for kk in range(1, k + 1):
+                cand = cur[None, :] + _NEIGH
+                cand[:, 0] %= nx
+                cand[:, 1] %= nx
+                inz = (cand[:, 2] >= 0) & (cand[:, 2] < nz)
+                cz = np.clip(cand[:, 2], 0, nz - 1)
+                w = np.where(inz & ~occ[cand[:, 0], cand[:, 1], cz], w0, 0.0)
+                if w.sum() <= 0:
+                    ok = False
+                    break
+                j = rng.choice(_NW, p=w / w.sum())
+                cur = cand[j]
+                occ[tuple(cur)] = True
+                placed.append(cur)
+                pos[ci, kk] = cur
+            if ok:
+                return
+            for p_ in placed:
+                occ[tuple(p_)] = False
+        raise RuntimeError("lattice walk stuck; lower the density or grafting density")
+
+    def grow(starts, length, zdir):
+        """Grows len(starts) lattice SAWs of `length` beads in parallel; returns [c, length, 3]."""
+        c = len(starts)
+        pos = np.zeros((c, length, 3), np.int64)
+        pos[:, 0] = starts
+        occ[starts[:, 0], starts[:, 1], starts[:, 2]] = True
+        if zdir is not None:
+            up = zdir[:, None] * _NEIGH[None, :, 2]
+            wdir = np.where(up > 0, 3.0, np.where(up < 0, 0.3, 1.0))
+        else:
+            wdir = np.ones((c, _NW))
+        wdir = wdir * np.where(np.abs(_NEIGH).sum(1) == 1, 1.0, _EDGE_W)[None, :]
+        for k in range(1, length):
+            cur = pos[:, k - 1]
+            cand = cur[:, None, :] + _NEIGH[None, :, :]
+            cand[:, :, 0] %= nx
+            cand[:, :, 1] %= nx
+            inz = (cand[:, :, 2] >= 0) & (cand[:, :, 2] < nz)
+            cz = np.clip(cand[:, :, 2], 0, nz - 1)
+            todo = np.arange(c)
+            for _ in range(64):  # all chains claim at once; a site wanted twice goes to one of them
+                free = inz[todo] & ~occ[cand[todo, :, 0], cand[todo, :, 1], cz[todo]]
+                w = np.where(free, wdir[todo], 0.0)
+                cw = np.cumsum(w, axis=1)
+                stuck = cw[:, -1] <= 0
+                if np.any(stuck):
+                    # a walk trapped itself: regrow that chain alone (beads 1..k) from its anchor
+                    for ci in todo[stuck]:
+                        regrow(pos, ci, k, wdir[ci])
+                    todo = todo[~stuck]
+                    if len(todo) == 0:
+                        break
+                    continue
+                j = np.argmax(cw >= rng.random(len(todo))[:, None] * cw[:, -1:], axis=1)
+                tgt = cand[todo, j]
+                flat = (tgt[:, 0] * nx + tgt[:, 1]) * nz + tgt[:, 2]
+                _, first = np.unique(flat, return_index=True)
+                win = np.zeros(len(todo), bool)
+                win[first] = True
+                pos[todo[win], k] = tgt[win]
+                occ[tgt[win, 0], tgt[win, 1], tgt[win, 2]] = True
+                todo = todo[~win]
+                if len(todo) == 0:
+                    break
+            if len(todo):
+                raise RuntimeError("lattice walk could not resolve site conflicts")
+        return pos
+
+    # brush anchors: random distinct sites on the bottom (z=0) and top (z=nz-1) layers
+    half = n_chain // 2
+    cells = rng.choice(nx * nx, size=half, replace=False)
+    cells_t = rng.choice(nx * nx, size=n_chain - half, replace=False)
+    starts = np.concatenate([
+        np.stack([cells // nx, cells % nx, np.zeros(half, np.int64)], 1),
+        np.stack([cells_t // nx, cells_t % nx, np.full(n_chain - half, nz - 1, np.int64)], 1)])
+    zdir = np.concatenate([np.ones(half), -np.ones(n_chain - half)])
+    k = 0
+    if n_chain:
+        pos = grow(starts, n_mon, zdir)
+        sites[:n_brush] = pos.reshape(-1, 3)
+        k = n_brush
+    if n_melt:
+        free_idx = np.flatnonzero(~occ.ravel())
+        pick = rng.choice(free_idx, size=n_chain_d, replace=False)
+        st = np.stack(np.unravel_index(pick, occ.shape), 1).astype(np.int64)
+        if n_mon_d == 1:
+            occ[st[:, 0], st[:, 1], st[:, 2]] = True
+            sites[k:k + n_melt] = st
+        else:
+            sites[k:k + n_melt] = grow(st, n_mon_d, None).reshape(-1, 3)
+    r0 = np.empty((n, 3))
+    r0[:, 0] = (sites[:, 0] + 0.5) * ax
+    r0[:, 1] = (sites[:, 1] + 0.5) * ax
+    r0[:, 2] = Z_LO + sites[:, 2] * az
+    a_type = np.full(n, solvent_type if n_mon_d == 1 else melt_type, np.int32)
+    if n_chain:
+        a_type[:n_brush] = 2
+        a_type[0:n_brush:n_mon] = 1
+    v = rng.normal(0.0, np.sqrt(kT), size=(n, 3))
+    if n_chain:
+        v[0:n_brush:n_mon] = 0.0
+    s = abi.System()
+    s.boundary[0] = s.boundary[1] = L
+    s.boundary[2] = D
+    s.n_mon, s.n_chain = n_mon, n_chain
+    s.n_mon_d, s.n_chain_d = n_mon_d, n_chain_d
+    s.n_mon_e = s.n_chain_e = 0
+    s.n_mon_tot = s.n_part = n
+    s.s_time = 1
+    s.seed = int(rng.integers(1, 2**63 - 1))
+    return s, a_type, r0, v
+
+
+def wca_inputs(gamma=5.0, kT=1.0, dt=0.005, a_w=-3.2, sigma_w=1.0, k_chain=30.0, r_chain=1.5,
+               bending=False, k_bend=0.0, thermostat=0):
+    """abi.Inputs of the WCA + FENE + DPD brush model expressed with the reference's own switches:
+    SYSTEM 0, WALL 2 (repulsive 9-3 walls, A_w < 0), SOLVENT 1 (every pair cut at 2^(1/6) sigma),
+    DPD inside the LJ cut-off with gamma = friction(1)."""
+    inp = abi.Inputs()
+    f = inp.flags
+    f.system, f.symmetry, f.wall, f.solvent = 0, 0, 2, 1
+    f.thermostat, f.dpd_weight, f.dpd_cut_off = thermostat, 0, 0.0
+    f.bending = 1 if bending else 0
+    f.bin_type, f.l_box = 2, 1
+    inp.dt, inp.temp = dt, kT
+    inp.x_space = inp.y_space = 1.0
+    inp.n_cell_w_x = inp.n_cell_w_y = 1
+    inp.z_space_wall = 1.0
+    for t in range(4):
+        inp.mass_type[t] = 1.0
+        inp.sigma_ii[t] = 1.0
+        inp.friction[t] = gamma
+        for u in range(4):
+            inp.epsil[t * abi.MAXT + u] = 1.0
+    inp.a_w, inp.sigma_w = a_w, sigma_w
+    inp.k_chain, inp.r_chain = k_chain, r_chain
+    inp.k_bend = k_bend
+    inp.hist_dim = 200
+    return inp
+
+
+def wca_params(**kw):
+    p, _ = md.derive(wca_inputs(**kw))
+    return p
+
+
+def draw_replica_shapes(n_rep, seed, rho=0.8, max_brush_frac=0.7):
+    """(sigma_g, N, D, L) per replica drawn from the seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n_rep:
+        sg = rng.uniform(0.05, 0.3)
+        N = int(rng.integers(10, 101))
+        D = rng.uniform(10.0, 40.0)
+        L = rng.uniform(15.0, 40.0)
+        if 2 * sg * N > max_brush_frac * rho * D:
+            continue
+        out.append((sg, N, D, L))
+    return out
+
+
+def replicas(n_rep=256, seed=2024, rho=0.8, shapes=None):
+    """The batched workload: list of (System, a_type, r0, v), one per replica.  A lattice walk
+    that traps itself is regrown from the next sub-seed (deterministic for a given seed)."""
+    shapes = shapes or draw_replica_shapes(n_rep, seed, rho)
+    reps = []
+    for k, (sg, N, D, L) in enumerate(shapes):
+        for attempt in range(50):
+            try:
+                reps.append(brush_channel(L, D, sg, N, rho=rho, seed=(seed * 100003 + k) * 64 + attempt))
+                break
+            except RuntimeError:
+                continue
+        else:
+            raise RuntimeError("replica %d (%s) could not be generated" % (k, (sg, N, D, L)))
+    return reps
+
+
+def concat(reps):
+    """Concatenates replicas into the batched host arrays of mfa_batch_init."""
+    systems = [r[0] for r in reps]
+    a_type = np.concatenate([r[1] for r in reps]).astype(np.int32)
+    r0 = np.concatenate([r[2] for r in reps])
+    v = np.concatenate([r[3] for r in reps])
+    return systems, a_type, r0, v
+
+
+def small_channel(seed=1):
+    """20x20x20 channel, 40 chains of 30 beads per wall (grafting density 0.1), solvent to 0.8."""
+    return brush_channel(20.0, 20.0, 0.1, 30, rho=0.8, seed=seed)

@@ -1,0 +1,1066 @@
+// mfa_api.cu -- the C ABI of include/mfa_gpu.h: contexts, per-routine drop-ins, the fused
+// graph-captured step, host<->device movement, parity exports and timing.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/mfa_gpu.h"
+#include "mfa_state.cuh"
+
+using namespace mfa;
+
+struct mfa_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  mfa_params P;
+  mfa_options opt;
+  std::vector<mfa_system> sys;
+  int nrep = 0, N = 0, Np = 0;
+  SimConst C;
+  DevState S;
+  std::vector<RepDesc> hreps;
+  RepDesc* dreps = nullptr;
+  PairEntry<float>* dtabf = nullptr;
+  PairEntry<double>* dtabd = nullptr;
+  double* acc_step = nullptr;  // [NOBS][nrep]
+  double* acc_call = nullptr;
+  double* rec = nullptr;       // [NOBS][nrep] last record of mfa_step
+  double* prof = nullptr;
+  long long n_obs = 0;
+  std::vector<double> v_coul_self, v_ww;
+  KSpace K;
+  bool kspace = false;
+  unsigned* h_status = nullptr;  // pinned
+  long long* h_rebuilds = nullptr;
+  long long* d_rebuilds = nullptr;
+  long long last_rebuilds = 0;
+  long long host_steps = 0;      // steps completed (host view)
+  int last_source = 0;           // 0 none, 1 mfa_step record, 2 per-routine accumulators
+  std::map<std::tuple<int, int, int, int>, std::pair<cudaGraphExec_t, long long>> graphs;
+  cudaEvent_t ev[16];
+  long long launches = 0;
+  std::vector<void*> allocs;
+  std::string err;
+  double rl_max = 0.;
+};
+
+namespace {
+
+const char* kFamNames[MFA_NKFAM] = {"rebuild", "pair", "bonded", "integrate", "kspace", "profiles", "record",
+                                    "positions"};
+
+int fail(mfa_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return fail(ctx, MFA_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+#define RET(x)              \
+  do {                      \
+    int r__ = (x);          \
+    if (r__) return r__;    \
+  } while (0)
+
+template <typename T>
+int dalloc(mfa_ctx* ctx, T** p, size_t n) {
+  void* q = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+  if (e != cudaSuccess) return fail(ctx, MFA_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  ctx->allocs.push_back(q);
+  *p = (T*)q;
+  return MFA_OK;
+}
+
+#define DA(p, n)                                   \
+  do {                                             \
+    int r_ = dalloc(ctx, &(p), (size_t)(n));       \
+    if (r_ != MFA_OK) return r_;                   \
+  } while (0)
+
+Acc acc_of(double* a, int nrep) { return Acc{a, nrep}; }
+
+int check_status(mfa_ctx* ctx) {
+  CK(cudaStreamSynchronize(ctx->st));
+  unsigned s = *ctx->h_status;
+  if (s & ST_NAN) return fail(ctx, MFA_ERR_NAN, "non-finite position detected");
+  if (s & ST_OUT_OF_BOX) return fail(ctx, MFA_ERR_OUT_OF_BOX, "a particle left the channel");
+  if (s & ST_NLIST_OVERFLOW) return fail(ctx, MFA_ERR_NLIST_OVERFLOW, "neighbour list capacity exceeded");
+  return MFA_OK;
+}
+
+int post_status(mfa_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_status, ctx->S.status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  return MFA_OK;
+}
+
+__global__ void k_count_rebuild(int* flag, long long* n) {
+  if (*flag) *n += 1;
+  *flag = 0;
+}
+
+// rebuild (conditional) + clear flag
+void rebuild(mfa_ctx* ctx, bool force) {
+  launch_rebuild(ctx->S, ctx->st, force);
+  k_count_rebuild<<<1, 1, 0, ctx->st>>>(ctx->S.rebuild_flag, ctx->d_rebuilds);
+  ctx->launches += 11;
+}
+
+int bonded_mask(const mfa_ctx* ctx) {
+  int m = 1;
+  if (ctx->P.flags.bending) m |= 2;
+  if (ctx->P.flags.bending_melt) m |= 4;
+  if (ctx->P.flags.orientation) m |= 8;
+  return m;
+}
+
+bool any_chains(const mfa_ctx* ctx) {
+  for (auto& s : ctx->sys)
+    if ((s.n_mon > 1 && s.n_chain > 0) || (s.n_mon_d > 1 && s.n_chain_d > 0) || (s.n_mon_e > 1 && s.n_chain_e > 0))
+      return true;
+  return false;
+}
+
+void fill_energies(const mfa_ctx* ctx, const double* acc, int rep, mfa_energies* e) {
+  const int R = ctx->nrep;
+  auto A = [&](int slot) { return acc[(size_t)slot * R + rep]; };
+  std::memset(e, 0, sizeof *e);
+  e->step = ctx->sys[rep].s_time + ctx->host_steps;
+  e->v_fluid_fluid = A(O_VFF);
+  if (ctx->P.flags.bin_type == 1) e->v_fluid_fluid *= 1.0;  // full-list sums are already single-counted
+  e->v_fluid_wall = A(O_VFW);
+  e->v_wall_wall = ctx->v_ww[rep];
+  e->v_intra_molec = A(O_VINTRA);
+  e->v_bend = A(O_VBEND);
+  e->v_bend_melt = A(O_VBENDM);
+  e->v_or = A(O_VOR);
+  const bool charged = ctx->P.flags.system == 2 || ctx->P.flags.system == 3;
+  e->v_coul = charged ? A(O_VCOUL) + ctx->v_coul_self[rep] + A(O_VCOULK) + A(O_VDIP) : 0.;
+  e->t_fluid = A(O_TFLUID);
+  e->v_total = e->v_wall_wall + e->v_fluid_wall + e->v_fluid_fluid + e->v_intra_molec;
+  if (ctx->P.flags.bending) e->v_total += e->v_bend;
+  if (ctx->P.flags.orientation) e->v_total += e->v_or;
+  if (ctx->P.flags.bending_melt) e->v_total += e->v_bend_melt;
+  if (charged) e->v_total += e->v_coul;
+  e->e_total = e->v_total + e->t_fluid;
+  e->inv_n = ctx->hreps[rep].inv_n;
+}
+
+// ewald_k(0) (ewald_k.f90:37-124): the k-vectors in the reference's enumeration order, G(k),
+// and the list of charged particles (replica 0).
+int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
+  const mfa_system& s = ctx->sys[0];
+  const mfa_params& p = ctx->P;
+  const double pi = (double)3.1415926536f;  // mfa_common.f90:315
+  const double* L = s.boundary;
+  const double z_slab = 2.;
+  const double dk[3] = {2. * pi * (1. / L[0]), 2. * pi * (1. / L[1]), 2. * pi / (L[2] + z_slab * L[2])};
+  const double k_c = (dk[0] + dk[1]) * (double)p.n_kmax / 2.;
+  const int nx = (int)(k_c / dk[0]), ny = (int)(k_c / dk[1]), nz = (int)(k_c / dk[2]);
+  const double fac_alpha = 1. / (4. * p.alpha_c);
+  std::vector<int4> kn;
+  std::vector<double> kv, kf;
+  for (int kz = 0; kz <= nz; ++kz)
+    for (int ky = -ny; ky <= ny; ++ky)
+      for (int kx = -nx; kx <= nx; ++kx) {
+        const double a1 = (double)kx * dk[0], b1 = (double)ky * dk[1], c1 = (double)kz * dk[2];
+        const double rk2 = a1 * a1 + b1 * b1 + c1 * c1;
+        if (rk2 > k_c * k_c) continue;
+        if (kz == 0 && ky == 0 && kx == 0) continue;
+        if (kz == 0 && kx + ky < 0) continue;
+        if (kz == 0 && -kx == ky && ky > 0) continue;
+        kn.push_back(make_int4(kx, ky, kz, 0));
+        const double k0 = dk[0] * kx, k1 = dk[1] * ky, k2 = dk[2] * kz;
+        kv.push_back(k0);
+        kv.push_back(k1);
+        kv.push_back(k2);
+        const double kk = k0 * k0 + k1 * k1 + k2 * k2;
+        kf.push_back((1. / kk) * std::exp(-kk * fac_alpha));
+      }
+  KSpace& K = ctx->K;
+  std::memset(&K, 0, sizeof K);
+  K.nk = (int)kn.size();
+  K.nxm = nx;
+  K.nym = ny;
+  K.nzm = nz;
+  K.ncol = (nx + 1) + (ny + 1) + (nz + 1);
+  K.cx = dk[0] / (2. * M_PI);
+  K.cy = dk[1] / (2. * M_PI);
+  K.cz = dk[2] / (2. * M_PI);
+  K.inv_V = (1. / L[0]) * (1. / L[1]) / (L[2] * (1. + z_slab));
+  K.lz_half = L[2] / 2.;
+  K.rep = 0;
+  std::vector<int> qt;
+  for (int t = 0; t < s.n_mon_tot; ++t)
+    if (p.charge[a_type[t] - 1] != 0.) qt.push_back(t);
+  K.nq = (int)qt.size();
+  DA(K.kn, K.nk);
+  DA(K.kvec, 3 * K.nk);
+  DA(K.kfac, K.nk);
+  DA(K.rho, 2 * K.nk);
+  DA(K.mz, 1);
+  DA(K.qtag, K.nq);
+  if (ctx->S.mixed) DA(K.tabf, (size_t)K.nq * K.ncol); else DA(K.tabd, (size_t)K.nq * K.ncol);
+  cudaStream_t st = ctx->st;
+  CK(cudaMemcpyAsync(K.kn, kn.data(), sizeof(int4) * K.nk, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.kvec, kv.data(), sizeof(double) * 3 * K.nk, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.kfac, kf.data(), sizeof(double) * K.nk, cudaMemcpyHostToDevice, st));
+  if (K.nq) CK(cudaMemcpyAsync(K.qtag, qt.data(), sizeof(int) * K.nq, cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->kspace = true;
+  return MFA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mfa_version(void) { return "mfa_gb300 1.0 (sm_103a)"; }
+
+int mfa_device_count(int32_t* n) {
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (e != cudaSuccess) c = 0;
+  if (n) *n = c;
+  return MFA_OK;
+}
+
+void mfa_default_options(mfa_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->precision = MFA_PREC_MIXED;
+  o->device = 0;
+  o->skin = 0.3;
+  o->nbr_capacity = 0;
+  o->energy_every = 10;
+  o->use_graphs = 1;
+  o->block_size = 0;
+  o->profile_from_step = 0;
+}
+
+int mfa_init(const mfa_params* p, const mfa_system* sys, const int32_t* a_type, const double* r0, const double* v,
+             const double* a, const mfa_options* opt, mfa_ctx** out) {
+  return mfa_batch_init(p, 1, sys, a_type, r0, v, a, opt, out);
+}
+
+int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, const int32_t* a_type,
+                   const double* r0, const double* v, const double* a, const mfa_options* opt, mfa_ctx** out) {
+  if (!out) return MFA_ERR_ARG;
+  *out = nullptr;
+  if (!p || n_rep < 1 || !sysv || !a_type || !r0) return MFA_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MFA_ERR_NO_DEVICE;
+  mfa_ctx* ctx = new mfa_ctx();
+  *out = ctx;
+  ctx->P = *p;
+  if (opt) ctx->opt = *opt; else mfa_default_options(&ctx->opt);
+  if (ctx->opt.energy_every < 1) ctx->opt.energy_every = 10;
+  if (ctx->opt.skin <= 0) ctx->opt.skin = 0.3;
+  ctx->device = ctx->opt.device;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+  for (int k = 0; k < 16; ++k) CK(cudaEventCreate(&ctx->ev[k]));
+  const mfa_flags& F = p->flags;
+  if (p->n_type < 1 || p->n_type > MFA_MAX_TYPES) return fail(ctx, MFA_ERR_ARG, "n_type out of range");
+  if (F.symmetry != 0) return fail(ctx, MFA_ERR_UNSUPPORTED, "only SYMMETRY 0 (channel) is built");
+  if (p->compat & MFA_COMPAT_EWALD_I_ONLY)
+    return fail(ctx, MFA_ERR_UNSUPPORTED, "Coulomb force on i only depends on the reference's loop order");
+  const bool charged = F.system == 2 || F.system == 3;
+  if (charged && n_rep != 1) return fail(ctx, MFA_ERR_UNSUPPORTED, "k-space Ewald is built for one replica");
+  ctx->nrep = n_rep;
+  ctx->sys.assign(sysv, sysv + n_rep);
+  long long N = 0;
+  for (auto& s : ctx->sys) {
+    if (s.n_part < s.n_mon_tot || s.n_mon_tot < 0) return fail(ctx, MFA_ERR_ARG, "n_part < n_mon_tot");
+    N += s.n_part;
+  }
+  if (N < 1 || N > (1ll << 30)) return fail(ctx, MFA_ERR_ARG, "particle count out of range");
+  ctx->N = (int)N;
+  ctx->Np = (int)((N + 31) / 32 * 32);
+  // ---- scalars --------------------------------------------------------------------------------
+  SimConst& C = ctx->C;
+  std::memset(&C, 0, sizeof C);
+  C.n_type = p->n_type;
+  C.thermostat_dpd = F.thermostat == 0;
+  C.dpd_weight1 = F.dpd_weight == 1;
+  C.force_switch_on = F.force_switch_on;
+  C.poiseuille = F.poiseuille;
+  C.bending = F.bending;
+  C.bending_melt = F.bending_melt;
+  C.orientation = F.orientation;
+  C.bend_form = p->bend_form;
+  C.charged = charged;
+  C.wall = F.wall;
+  C.dt = p->dt;
+  C.half_dt = 0.5 * p->dt;
+  C.half_dt2 = 0.5 * (p->dt * p->dt);
+  for (int t = 0; t < MAXT; ++t) {
+    C.mass[t] = p->mass_type[t];
+    C.inv_mass[t] = p->mass_type[t] != 0. ? 1. / p->mass_type[t] : 0.;
+    C.sigma_wall[t] = p->sigma_wall[t];
+    C.a_wall[t] = p->a_wall[t];
+    C.charge[t] = p->charge[t];
+  }
+  C.gamma = p->friction1;
+  C.sig = p->sig;
+  C.r2min_init = p->r_2_min_init;
+  C.r2min_time = p->r_2_min_time;
+  C.a_w = p->a_w;
+  C.k_chain = p->k_chain;
+  C.inv_r_chain_2 = p->inv_r_chain_2;
+  C.fene_xmax = (double)0.98f;
+  C.k_bend = p->k_bend;
+  C.alpha_eq = p->alpha_eq;
+  C.k_or = p->k_or;
+  C.alpha_or = p->alpha_or;
+  C.bend_small = (double)0.000001f;
+  for (int d = 0; d < 3; ++d) C.const_force[d] = p->const_force[d];
+  C.sqrt_alpha = p->sqrt_alpha;
+  C.alpha_c = p->alpha_c;
+  C.inv_sqrt_pi = p->inv_sqrt_pi;
+  C.coul_rc2 = p->rc_coul_2;
+  const double skin = ctx->opt.skin;
+  C.skin_half2 = 0.25 * skin * skin;
+  C.hist_dim = p->hist_dim > 0 ? p->hist_dim : 200;
+  if (C.hist_dim > MFA_HIST_DIM_MAX) return fail(ctx, MFA_ERR_CAPACITY, "hist_dim exceeds MFA_HIST_DIM_MAX");
+  // ---- pair tables ----------------------------------------------------------------------------
+  std::vector<PairEntry<float>> tf(NPAIR);
+  std::vector<PairEntry<double>> td(NPAIR);
+  const int W = p->n_type - 1;
+  double rl_max = 0.;
+  for (int i = 0; i < MAXT; ++i)
+    for (int j = 0; j < MAXT; ++j) {
+      PairEntry<double> e;
+      std::memset(&e, 0, sizeof e);
+      const int k = i * MAXT + j;
+      if (i < p->n_type && j < p->n_type) {
+        e.range2 = p->range_2[k];
+        e.eps4 = p->epsil[k];
+        e.sig2 = p->sigma_2[k];
+        e.shift = p->e_shift[k];
+        e.inv_rc = std::sqrt(p->inv_range_2[k]);
+        const bool wallpair = F.wall == 1 && (i == W || j == W);
+        int fl = 0;
+        if (e.range2 > 0.) fl |= PF_LJ;
+        double rc = std::sqrt(e.range2);
+        if (F.thermostat == 0) {
+          if (p->r_cut_dpd_2 == 0.) {
+            if (e.range2 > 0. && !wallpair) fl |= PF_DPD_LJ;
+          } else if (i != 0 && j != 0 && !wallpair) {
+            fl |= PF_DPD_OWN;
+            e.dpd_rc2 = p->r_cut_dpd_2;
+            e.inv_dpd_rc = 1. / std::sqrt(p->r_cut_dpd_2);
+            rc = std::max(rc, std::sqrt(p->r_cut_dpd_2));
+          }
+        }
+        if (charged && p->charge[i] * p->charge[j] != 0.) {
+          fl |= PF_COUL;
+          e.qq = p->charge[i] * p->charge[j];
+          if (p->rc_coul_2 > 0.) rc = std::max(rc, std::sqrt(p->rc_coul_2));
+        }
+        e.flags = fl;
+        e.rlist2 = rc > 0. ? (rc + skin) * (rc + skin) : 0.;
+        if (rc > 0.) rl_max = std::max(rl_max, rc + skin);
+      }
+      td[k] = e;
+      PairEntry<float>& g = tf[k];
+      g.range2 = (float)e.range2; g.eps4 = (float)e.eps4; g.sig2 = (float)e.sig2; g.shift = (float)e.shift;
+      g.inv_rc = (float)e.inv_rc; g.rlist2 = (float)e.rlist2; g.dpd_rc2 = (float)e.dpd_rc2;
+      g.inv_dpd_rc = (float)e.inv_dpd_rc; g.qq = (float)e.qq; g.flags = e.flags;
+    }
+  if (rl_max <= 0.) rl_max = 1.0 + skin;
+  ctx->rl_max = rl_max;
+  // ---- replicas -------------------------------------------------------------------------------
+  ctx->hreps.resize(n_rep);
+  ctx->v_coul_self.assign(n_rep, 0.);
+  ctx->v_ww.assign(n_rep, 0.);
+  int cell_off = 0, p0 = 0;
+  double dens_max = 0.;
+  for (int r = 0; r < n_rep; ++r) {
+    const mfa_system& s = ctx->sys[r];
+    RepDesc& R = ctx->hreps[r];
+    std::memset(&R, 0, sizeof R);
+    for (int d = 0; d < 3; ++d) {
+      if (!(s.boundary[d] > 0.)) return fail(ctx, MFA_ERR_ARG, "box length must be positive");
+      R.L[d] = s.boundary[d];
+      R.invL[d] = 1. / s.boundary[d];
+      R.sfx[d] = (d < 2) ? 4294967296.0 / s.boundary[d] : 1073741824.0 / s.boundary[d];
+      R.ufx[d] = 1. / R.sfx[d];
+      R.ufx_f[d] = (float)R.ufx[d];
+      int nc = (int)std::floor(s.boundary[d] / rl_max);
+      if (nc < 1) nc = 1;
+      if (d < 2 && nc < 3)
+        return fail(ctx, MFA_ERR_UNSUPPORTED, "box shorter than 3 list cells (3*(r_cut_max+skin)) in x or y");
+      R.nc[d] = nc;
+      R.inv_lc[d] = (double)nc / s.boundary[d];
+    }
+    R.ncell = R.nc[0] * R.nc[1] * R.nc[2];
+    R.cell_off = cell_off;
+    cell_off += R.ncell;
+    R.p0 = p0;
+    R.n_part = s.n_part;
+    R.n_mon_tot = s.n_mon_tot;
+    R.n_mon = s.n_mon; R.n_chain = s.n_chain; R.n_mon_d = s.n_mon_d; R.n_chain_d = s.n_chain_d;
+    R.n_mon_e = s.n_mon_e; R.n_chain_e = s.n_chain_e;
+    R.part_init_d = s.n_mon * s.n_chain;
+    R.part_init_e = R.part_init_d + s.n_mon_d * s.n_chain_d;
+    if (R.part_init_e + s.n_mon_e * s.n_chain_e != s.n_mon_tot)
+      return fail(ctx, MFA_ERR_ARG, "n_mon_tot differs from the chain counts");
+    R.seed = s.seed;
+    R.s_time = s.s_time;
+    R.lz_half = s.boundary[2] / 2.;
+    const double D = s.boundary[2];
+    if (F.wall == 2)  // wall_wall.f90:45-48
+      ctx->v_ww[r] = 2.0 * (std::fabs(p->a_w) * std::pow(p->sigma_w / D, 9) - p->a_w * std::pow(p->sigma_w / D, 3));
+    R.v_ww = ctx->v_ww[r];
+    R.inv_n = (F.system == 2) ? 1. / (double)s.n_mon_tot : 1. / (double)(s.n_mon_tot - s.n_chain);
+    R.hist_inv_dz = 1. / (D / (double)C.hist_dim);
+    p0 += s.n_part;
+    dens_max = std::max(dens_max, (double)s.n_part / (s.boundary[0] * s.boundary[1] * D));
+    if (charged) {
+      double vs = 0.;
+      for (int t = 0; t < s.n_mon_tot; ++t) vs -= p->charge[a_type[R.p0 + t] - 1] * p->charge[a_type[R.p0 + t] - 1];
+      ctx->v_coul_self[r] = vs * p->sqrt_alpha / std::sqrt((double)3.1415926536f);
+    }
+  }
+  // ---- per-particle info ----------------------------------------------------------------------
+  std::vector<int> info(ctx->N), iota(ctx->N);
+  for (int r = 0; r < n_rep; ++r) {
+    const RepDesc& R = ctx->hreps[r];
+    for (int t = 0; t < R.n_part; ++t) {
+      int g = R.p0 + t;
+      int ty = a_type[g] - 1;
+      if (ty < 0 || ty >= p->n_type) return fail(ctx, MFA_ERR_ARG, "particle type out of range");
+      int mob = t < R.n_mon_tot;
+      int head = (t < R.part_init_d && R.n_mon > 0 && t % R.n_mon == 0) ? 1 : 0;
+      int sp = (t < R.part_init_d) ? 0 : (t < R.part_init_e ? 1 : (t < R.n_mon_tot ? 2 : 3));
+      info[g] = ty | (mob << 4) | (head << 5) | (sp << 6) | (r << 8);
+      iota[g] = g;
+    }
+  }
+  // ---- device memory --------------------------------------------------------------------------
+  DevState& S = ctx->S;
+  std::memset(&S, 0, sizeof S);
+  S.N = ctx->N;
+  S.Np = ctx->Np;
+  S.nrep = n_rep;
+  S.mixed = ctx->opt.precision == MFA_PREC_MIXED;
+  const size_t Nn = ctx->Np;
+  double** dst[12] = {&S.rx, &S.ry, &S.rz, &S.vx, &S.vy, &S.vz, &S.ax, &S.ay, &S.az, &S.fx, &S.fy, &S.fz};
+  for (auto d : dst) DA(*d, Nn);
+  for (int k = 0; k < 9; ++k) DA(S.tmp[k], Nn);
+  DA(S.tag, Nn); DA(S.info, Nn); DA(S.tmp_tag, Nn); DA(S.tmp_info, Nn); DA(S.slot_of_tag, Nn);
+  if (S.mixed) { DA(S.pfx, Nn); DA(S.vf, Nn); } else { DA(S.pd, Nn); DA(S.vd, Nn); }
+  DA(S.ref, Nn);
+  DA(S.nn, Nn);
+  DA(S.cell_of, Nn); DA(S.rank, Nn); DA(S.perm, Nn);
+  S.ncell_tot = cell_off;
+  DA(S.cell_count, cell_off + 1);
+  DA(S.cell_start, cell_off + 1);
+  DA(S.scan_blk, (cell_off + 1023) / 1024 + 1);
+  DA(S.rebuild_flag, 1);
+  DA(S.status, 1);
+  DA(S.steps_done, 1);
+  DA(ctx->d_rebuilds, 1);
+  DA(ctx->dreps, n_rep);
+  DA(ctx->dtabf, NPAIR);
+  DA(ctx->dtabd, NPAIR);
+  DA(ctx->acc_step, NOBS * n_rep);
+  DA(ctx->acc_call, NOBS * n_rep);
+  DA(ctx->rec, NOBS * n_rep);
+  DA(ctx->prof, (size_t)n_rep * C.hist_dim * 21);
+  CK(cudaMallocHost(&ctx->h_status, sizeof(unsigned)));
+  CK(cudaMallocHost(&ctx->h_rebuilds, sizeof(long long)));
+  *ctx->h_status = 0;
+  S.reps = ctx->dreps;
+  S.tabf = ctx->dtabf;
+  S.tabd = ctx->dtabd;
+  // neighbour capacity: 2x the mean count of the densest replica + 32, at least 48
+  int cap = ctx->opt.nbr_capacity;
+  if (cap <= 0) {
+    double est = 4. / 3. * M_PI * rl_max * rl_max * rl_max * dens_max;
+    cap = (int)std::ceil(2.0 * est) + 32;
+    cap = std::max(cap, 48);
+  }
+  S.nbr_cap = cap;
+  DA(S.nbr, (size_t)cap * Nn);
+  cudaStream_t st = ctx->st;
+  CK(cudaMemcpyAsync(ctx->dreps, ctx->hreps.data(), sizeof(RepDesc) * n_rep, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->dtabf, tf.data(), sizeof(PairEntry<float>) * NPAIR, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(ctx->dtabd, td.data(), sizeof(PairEntry<double>) * NPAIR, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(S.info, info.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(S.tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(S.slot_of_tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(S.rebuild_flag, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(S.status, 0, sizeof(unsigned), st));
+  CK(cudaMemsetAsync(S.steps_done, 0, sizeof(long long), st));
+  CK(cudaMemsetAsync(ctx->d_rebuilds, 0, sizeof(long long), st));
+  CK(cudaMemsetAsync(ctx->acc_step, 0, sizeof(double) * NOBS * n_rep, st));
+  CK(cudaMemsetAsync(ctx->acc_call, 0, sizeof(double) * NOBS * n_rep, st));
+  CK(cudaMemsetAsync(ctx->rec, 0, sizeof(double) * NOBS * n_rep, st));
+  CK(cudaMemsetAsync(ctx->prof, 0, sizeof(double) * n_rep * C.hist_dim * 21, st));
+  for (int k = 9; k < 12; ++k) CK(cudaMemsetAsync(*dst[k], 0, sizeof(double) * Nn, st));
+  // ---- state upload (canonical AoS -> slots) --------------------------------------------------
+  {
+    double *dr = nullptr, *dv = nullptr, *dac = nullptr;
+    size_t n3 = 3 * (size_t)ctx->N;
+    CK(cudaMalloc(&dr, n3 * 8));
+    CK(cudaMalloc(&dv, n3 * 8));
+    CK(cudaMalloc(&dac, n3 * 8));
+    CK(cudaMemcpyAsync(dr, r0, n3 * 8, cudaMemcpyHostToDevice, st));
+    if (v) CK(cudaMemcpyAsync(dv, v, n3 * 8, cudaMemcpyHostToDevice, st)); else CK(cudaMemsetAsync(dv, 0, n3 * 8, st));
+    if (a) CK(cudaMemcpyAsync(dac, a, n3 * 8, cudaMemcpyHostToDevice, st)); else CK(cudaMemsetAsync(dac, 0, n3 * 8, st));
+    launch_scatter_state(S, st, dr, dv, dac);
+    launch_init_views(S, st);
+    CK(cudaStreamSynchronize(st));
+    cudaFree(dr);
+    cudaFree(dv);
+    cudaFree(dac);
+  }
+  // ---- k-space --------------------------------------------------------------------------------
+  if (charged && p->n_kmax > 0) {
+    int r = setup_kspace(ctx, a_type);
+    if (r != MFA_OK) return r;
+  }
+  // ---- initial sort + list, then size the list from the observed maximum ------------------------
+  rebuild(ctx, true);
+  RET(post_status(ctx));
+  int rc = check_status(ctx);
+  if (rc == MFA_ERR_NLIST_OVERFLOW || rc == MFA_OK) {
+    std::vector<int> nn(ctx->N);
+    CK(cudaMemcpy(nn.data(), S.nn, sizeof(int) * ctx->N, cudaMemcpyDeviceToHost));
+    int mx = 0;
+    for (int x : nn) mx = std::max(mx, x);
+    if (rc == MFA_ERR_NLIST_OVERFLOW || (ctx->opt.nbr_capacity <= 0 && mx * 3 / 2 + 16 > cap)) {
+      // grow and redo: count beyond the capacity is not stored, so retry with a larger one
+      int newcap = std::max(cap * 2, mx * 3 / 2 + 32);
+      if (rc == MFA_ERR_NLIST_OVERFLOW) newcap = std::max(newcap, cap * 3);
+      auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void*)S.nbr);
+      if (it != ctx->allocs.end()) { cudaFree(*it); ctx->allocs.erase(it); }
+      S.nbr_cap = newcap;
+      DA(S.nbr, (size_t)newcap * Nn);
+      CK(cudaMemsetAsync(S.status, 0, sizeof(unsigned), st));
+      *ctx->h_status = 0;
+      rebuild(ctx, true);
+      RET(post_status(ctx));
+      rc = check_status(ctx);
+    }
+  }
+  if (rc != MFA_OK) return rc;
+  CK(cudaMemcpy(ctx->h_rebuilds, ctx->d_rebuilds, sizeof(long long), cudaMemcpyDeviceToHost));
+  ctx->last_rebuilds = *ctx->h_rebuilds;
+  return MFA_OK;
+}
+
+int mfa_destroy(mfa_ctx* ctx) {
+  if (!ctx) return MFA_OK;
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  for (auto& g : ctx->graphs) cudaGraphExecDestroy(g.second.first);
+  for (void* p : ctx->allocs) cudaFree(p);
+  if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  if (ctx->h_rebuilds) cudaFreeHost(ctx->h_rebuilds);
+  for (int k = 0; k < 16; ++k)
+    if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+  return MFA_OK;
+}
+
+const char* mfa_last_error(const mfa_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int mfa_synchronize(mfa_ctx* ctx) {
+  if (!ctx) return MFA_ERR_ARG;
+  RET(post_status(ctx));
+  return check_status(ctx);
+}
+
+void* mfa_stream(mfa_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
+
+int mfa_n_particles(const mfa_ctx* ctx, int64_t* n_total, int32_t* n_rep) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (n_total) *n_total = ctx->N;
+  if (n_rep) *n_rep = ctx->nrep;
+  return MFA_OK;
+}
+
+// ---- per-routine drop-ins -------------------------------------------------------------------
+static int zero_call_slot(mfa_ctx* ctx, int slot) {
+  CK(cudaMemsetAsync(ctx->acc_call + (size_t)slot * ctx->nrep, 0, sizeof(double) * ctx->nrep, ctx->st));
+  return MFA_OK;
+}
+
+static int read_call_slot(mfa_ctx* ctx, int slot, double* out, double add_self) {
+  if (!out) return MFA_OK;
+  CK(cudaMemcpyAsync(out, ctx->acc_call + (size_t)slot * ctx->nrep, sizeof(double) * ctx->nrep,
+                     cudaMemcpyDeviceToHost, ctx->st));
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (r != MFA_OK) return r;
+  if (add_self != 0.)
+    for (int k = 0; k < ctx->nrep; ++k) out[k] += ctx->v_coul_self[k];
+  return MFA_OK;
+}
+
+int mfa_verlet_positions(mfa_ctx* ctx) {
+  if (!ctx) return MFA_ERR_ARG;
+  launch_integrate(ctx->S, ctx->C, ctx->st, 0, false, false, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 1;
+  rebuild(ctx, false);
+  CK(cudaGetLastError());
+  return MFA_OK;
+}
+
+int mfa_check_skin(mfa_ctx* ctx, int32_t* rebuilt) {
+  if (!ctx) return MFA_ERR_ARG;
+  rebuild(ctx, false);
+  CK(cudaMemcpyAsync(ctx->h_rebuilds, ctx->d_rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (rebuilt) *rebuilt = (*ctx->h_rebuilds != ctx->last_rebuilds) ? 1 : 0;
+  ctx->last_rebuilds = *ctx->h_rebuilds;
+  return MFA_OK;
+}
+
+int mfa_zero_force(mfa_ctx* ctx) {
+  if (!ctx) return MFA_ERR_ARG;
+  CK(cudaMemsetAsync(ctx->S.fx, 0, sizeof(double) * ctx->N, ctx->st));
+  CK(cudaMemsetAsync(ctx->S.fy, 0, sizeof(double) * ctx->N, ctx->st));
+  CK(cudaMemsetAsync(ctx->S.fz, 0, sizeof(double) * ctx->N, ctx->st));
+  return MFA_OK;
+}
+
+int mfa_fluid_fluid(mfa_ctx* ctx, double* v_ff, double* v_coul) {
+  if (!ctx) return MFA_ERR_ARG;
+  int r;
+  if ((r = zero_call_slot(ctx, O_VFF)) || (r = zero_call_slot(ctx, O_VCOUL))) return r;
+  launch_pair(ctx->S, ctx->C, ctx->st, true, true, acc_of(ctx->acc_call, ctx->nrep), ctx->opt.block_size);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  ctx->last_source = 2;
+  if ((r = read_call_slot(ctx, O_VFF, v_ff, 0.))) return r;
+  if ((r = read_call_slot(ctx, O_VCOUL, v_coul, ctx->C.charged ? 1. : 0.))) return r;
+  return MFA_OK;
+}
+
+int mfa_fluid_wall(mfa_ctx* ctx, int32_t wall_type, double* v_fw) {
+  if (!ctx) return MFA_ERR_ARG;
+  int r;
+  if ((r = zero_call_slot(ctx, O_VFW))) return r;
+  if (wall_type == 2 && ctx->C.wall == 2) {
+    launch_wall(ctx->S, ctx->C, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
+    ctx->launches += 1;
+  } else if (wall_type != 1) {
+    return fail(ctx, MFA_ERR_UNSUPPORTED, "fluid_wall: only wall types 1 (in the pair kernel) and 2 are built");
+  }
+  CK(cudaGetLastError());
+  return read_call_slot(ctx, O_VFW, v_fw, 0.);
+}
+
+int mfa_wall_wall(mfa_ctx* ctx, int32_t wall_type, double* v_ww) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (v_ww)
+    for (int k = 0; k < ctx->nrep; ++k) v_ww[k] = (wall_type == 2) ? ctx->v_ww[k] : 0.;
+  return MFA_OK;
+}
+
+static int bonded_call(mfa_ctx* ctx, int mask, int slot, double* out) {
+  int r;
+  if ((r = zero_call_slot(ctx, slot))) return r;
+  launch_bonded(ctx->S, ctx->C, ctx->st, mask, true, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return read_call_slot(ctx, slot, out, 0.);
+}
+
+int mfa_intra_molec(mfa_ctx* ctx, double* v) { return ctx ? bonded_call(ctx, 1, O_VINTRA, v) : MFA_ERR_ARG; }
+int mfa_bending(mfa_ctx* ctx, int32_t mode, double* v) {
+  if (!ctx) return MFA_ERR_ARG;
+  return mode == 0 ? MFA_OK : bonded_call(ctx, 2, O_VBEND, v);
+}
+int mfa_bending_melt(mfa_ctx* ctx, int32_t mode, double* v) {
+  if (!ctx) return MFA_ERR_ARG;
+  return mode == 0 ? MFA_OK : bonded_call(ctx, 4, O_VBENDM, v);
+}
+int mfa_orientation(mfa_ctx* ctx, int32_t mode, double* v) {
+  if (!ctx) return MFA_ERR_ARG;
+  return mode == 0 ? MFA_OK : bonded_call(ctx, 8, O_VOR, v);
+}
+
+int mfa_ewald_k(mfa_ctx* ctx, int32_t mode, double* v) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (mode == 0) return MFA_OK;
+  if (!ctx->kspace) return fail(ctx, MFA_ERR_STATE, "ewald_k: not a charged system");
+  int r;
+  if ((r = zero_call_slot(ctx, O_VCOULK))) return r;
+  launch_kspace(ctx->S, ctx->C, ctx->K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 4;
+  CK(cudaGetLastError());
+  return read_call_slot(ctx, O_VCOULK, v, 0.);
+}
+
+int mfa_dipolar_correction(mfa_ctx* ctx, double* v) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (!ctx->kspace) return fail(ctx, MFA_ERR_STATE, "dipolar_correction: not a charged system");
+  int r;
+  if ((r = zero_call_slot(ctx, O_VDIP))) return r;
+  launch_dipolar(ctx->S, ctx->C, ctx->K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 2;
+  CK(cudaGetLastError());
+  return read_call_slot(ctx, O_VDIP, v, 0.);
+}
+
+int mfa_constant_force(mfa_ctx* ctx, int32_t mode) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (mode != 1) return fail(ctx, MFA_ERR_UNSUPPORTED, "constant_force: only mode 1 (Poiseuille) is built");
+  launch_const_force(ctx->S, ctx->C, ctx->st);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return MFA_OK;
+}
+
+int mfa_verlet_velocities(mfa_ctx* ctx, mfa_energies* e) {
+  if (!ctx) return MFA_ERR_ARG;
+  int r;
+  if ((r = zero_call_slot(ctx, O_TFLUID))) return r;
+  launch_integrate(ctx->S, ctx->C, ctx->st, 1, false, true, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  ctx->host_steps += 1;
+  ctx->last_source = 2;
+  if (e) {
+    std::vector<double> h(NOBS * ctx->nrep);
+    CK(cudaMemcpyAsync(h.data(), ctx->acc_call, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+    RET(post_status(ctx));
+    if ((r = check_status(ctx))) return r;
+    for (int k = 0; k < ctx->nrep; ++k) fill_energies(ctx, h.data(), k, &e[k]);
+  }
+  return MFA_OK;
+}
+
+int mfa_profiles_accumulate(mfa_ctx* ctx) {
+  if (!ctx) return MFA_ERR_ARG;
+  launch_profiles(ctx->S, ctx->C, ctx->st, ctx->prof, ctx->C.hist_dim);
+  ctx->launches += 1;
+  ctx->n_obs += 1;
+  CK(cudaGetLastError());
+  return MFA_OK;
+}
+
+// ---- fused step -----------------------------------------------------------------------------
+// Issues the kernels of `n` steps; eflag on steps where (absolute step) % energy_every == 0 and
+// on the last step.  Returns the number of launches issued.
+static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof) {
+  const DevState& S = ctx->S;
+  const SimConst& C = ctx->C;
+  cudaStream_t st = ctx->st;
+  Acc acc = acc_of(ctx->acc_step, ctx->nrep);
+  const int mask = any_chains(ctx) ? bonded_mask(ctx) : 0;
+  long long L = 0;
+  launch_integrate(S, C, st, 0, false, false, acc);
+  L += 1;
+  for (int k = 1; k <= n; ++k) {
+    const bool ef = ((phase + k) % ctx->opt.energy_every == 0) || k == n;
+    launch_rebuild(S, st, false);
+    k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
+    L += 11;
+    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
+    L += 1;
+    if (mask) { launch_bonded(S, C, st, mask, ef, acc); L += 1; }
+    if (ctx->kspace) {
+      launch_kspace(S, C, ctx->K, st, ef, acc);
+      launch_dipolar(S, C, ctx->K, st, ef, acc);
+      L += 6;
+    }
+    if (k < n && !prof) {
+      launch_integrate(S, C, st, 2, true, ef, acc);
+      L += 1;
+    } else {
+      launch_integrate(S, C, st, 1, true, ef, acc);
+      L += 1;
+      if (prof) { launch_profiles(S, C, st, ctx->prof, C.hist_dim); L += 1; }
+      if (k < n) { launch_integrate(S, C, st, 0, false, false, acc); L += 1; }
+    }
+    if (ef) { launch_record(acc, ctx->rec, st); L += 1; }
+  }
+  return L;
+}
+
+int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (nsteps <= 0) return MFA_OK;
+  const long long s0 = ctx->sys[0].s_time + ctx->host_steps;
+  bool prof = ctx->P.flags.profiles && (ctx->host_steps >= ctx->opt.profile_from_step);
+  if (ctx->P.flags.profiles && !prof && ctx->host_steps + nsteps > ctx->opt.profile_from_step) {
+    // split at the start of the observation phase (md_main.f90:202)
+    int first = (int)(ctx->opt.profile_from_step - ctx->host_steps);
+    int r = mfa_step(ctx, first);
+    if (r) return r;
+    return mfa_step(ctx, nsteps - first);
+  }
+  const int phase = (int)(s0 % ctx->opt.energy_every);
+  long long L = 0;
+  if (ctx->opt.use_graphs) {
+    auto key = std::make_tuple(nsteps, phase, (int)prof, 0);
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+      L = issue_steps(ctx, nsteps, phase, prof);
+      CK(cudaStreamEndCapture(ctx->st, &g));
+      cudaGraphExec_t ge;
+      CK(cudaGraphInstantiate(&ge, g, 0));
+      cudaGraphDestroy(g);
+      it = ctx->graphs.emplace(key, std::make_pair(ge, L)).first;
+    }
+    CK(cudaGraphLaunch(it->second.first, ctx->st));
+    L = it->second.second;
+  } else {
+    L = issue_steps(ctx, nsteps, phase, prof);
+    CK(cudaGetLastError());
+  }
+  ctx->launches += L;
+  ctx->host_steps += nsteps;
+  if (prof) ctx->n_obs += nsteps;
+  ctx->last_source = 1;
+  return post_status(ctx);
+}
+
+int mfa_get_step(mfa_ctx* ctx, int64_t* step) {
+  if (!ctx || !step) return MFA_ERR_ARG;
+  *step = ctx->sys[0].s_time + ctx->host_steps;
+  return MFA_OK;
+}
+
+// ---- data movement --------------------------------------------------------------------------
+int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* force) {
+  if (!ctx) return MFA_ERR_ARG;
+  size_t n3 = 3 * (size_t)ctx->N;
+  double* buf = nullptr;
+  int nb = (r0 != nullptr) + (v != nullptr) + (a != nullptr) + (force != nullptr);
+  if (nb == 0) return mfa_synchronize(ctx);
+  CK(cudaMallocAsync(&buf, n3 * 8 * nb, ctx->st));
+  double* p = buf;
+  double *dr = r0 ? p : nullptr;
+  if (r0) p += n3;
+  double *dv = v ? p : nullptr;
+  if (v) p += n3;
+  double *da = a ? p : nullptr;
+  if (a) p += n3;
+  double *df = force ? p : nullptr;
+  launch_gather_state(ctx->S, ctx->st, dr, dv, da, df);
+  if (r0) CK(cudaMemcpyAsync(r0, dr, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
+  if (v) CK(cudaMemcpyAsync(v, dv, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
+  if (a) CK(cudaMemcpyAsync(a, da, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
+  if (force) CK(cudaMemcpyAsync(force, df, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaFreeAsync(buf, ctx->st));
+  RET(post_status(ctx));
+  return check_status(ctx);
+}
+
+int mfa_set_state(mfa_ctx* ctx, const double* r0, const double* v, const double* a) {
+  if (!ctx) return MFA_ERR_ARG;
+  size_t n3 = 3 * (size_t)ctx->N;
+  double *dr = nullptr, *dv = nullptr, *da = nullptr;
+  if (r0) { CK(cudaMallocAsync(&dr, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(dr, r0, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
+  if (v) { CK(cudaMallocAsync(&dv, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(dv, v, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
+  if (a) { CK(cudaMallocAsync(&da, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(da, a, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
+  launch_scatter_state(ctx->S, ctx->st, dr, dv, da);
+  launch_init_views(ctx->S, ctx->st);
+  rebuild(ctx, true);
+  if (dr) CK(cudaFreeAsync(dr, ctx->st));
+  if (dv) CK(cudaFreeAsync(dv, ctx->st));
+  if (da) CK(cudaFreeAsync(da, ctx->st));
+  return mfa_synchronize(ctx);
+}
+
+int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out) {
+  if (!ctx || !out) return MFA_ERR_ARG;
+  std::vector<double> h(NOBS * ctx->nrep);
+  const double* src = ctx->last_source == 2 ? ctx->acc_call : ctx->rec;
+  CK(cudaMemcpyAsync(h.data(), src, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (r) return r;
+  for (int k = 0; k < ctx->nrep; ++k) fill_energies(ctx, h.data(), k, &out[k]);
+  return MFA_OK;
+}
+
+int mfa_get_profiles(mfa_ctx* ctx, int32_t rep, double* dens, double* vsum, double* v2sum, int64_t* n_obs) {
+  if (!ctx || rep < 0 || rep >= ctx->nrep) return MFA_ERR_ARG;
+  const int H = ctx->C.hist_dim;
+  std::vector<double> h((size_t)H * 21);
+  CK(cudaMemcpyAsync(h.data(), ctx->prof + (size_t)rep * H * 21, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
+                     ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  for (int b = 0; b < H; ++b)
+    for (int sp = 0; sp < 3; ++sp) {
+      const double* q = &h[(b * 3 + sp) * 7];
+      if (dens) dens[b * 3 + sp] = q[0];
+      for (int d = 0; d < 3; ++d) {
+        if (vsum) vsum[(b * 3 + sp) * 3 + d] = q[1 + d];
+        if (v2sum) v2sum[(b * 3 + sp) * 3 + d] = q[4 + d];
+      }
+    }
+  if (n_obs) *n_obs = ctx->n_obs;
+  return MFA_OK;
+}
+
+int mfa_reset_profiles(mfa_ctx* ctx) {
+  if (!ctx) return MFA_ERR_ARG;
+  CK(cudaMemsetAsync(ctx->prof, 0, sizeof(double) * ctx->nrep * ctx->C.hist_dim * 21, ctx->st));
+  ctx->n_obs = 0;
+  return MFA_OK;
+}
+
+// ---- parity exports -------------------------------------------------------------------------
+int mfa_cell_list(mfa_ctx* ctx, int32_t rep, int32_t l_box, int32_t* cell_of, int32_t* counts, int32_t counts_cap,
+                  int32_t* n_cells) {
+  if (!ctx || rep < 0 || rep >= ctx->nrep || !cell_of || !n_cells || (l_box != 1 && l_box != 2)) return MFA_ERR_ARG;
+  const mfa_system& s = ctx->sys[rep];
+  const double rc = ctx->P.r_cut_max;
+  int nc[3];
+  double il[3];
+  for (int d = 0; d < 3; ++d) {  // make_binning (cell_list.f90:137-151)
+    nc[d] = (l_box == 1) ? (int)(s.boundary[d] / rc) : (int)(s.boundary[d] / (rc / 2.));
+    if (nc[d] < 1) nc[d] = 1;
+    double l = s.boundary[d] / (double)(float)nc[d];
+    il[d] = 1 / l;
+    n_cells[d] = nc[d];
+  }
+  const int nct = nc[0] * nc[1] * nc[2];
+  if (counts && counts_cap < nct + 1) return fail(ctx, MFA_ERR_CAPACITY, "counts_cap < n_cells_tot + 1");
+  int *dco = nullptr, *dcnt = nullptr;
+  CK(cudaMallocAsync(&dco, sizeof(int) * std::max(1, s.n_mon_tot), ctx->st));
+  CK(cudaMallocAsync(&dcnt, sizeof(int) * (nct + 1), ctx->st));
+  CK(cudaMemsetAsync(dcnt, 0, sizeof(int) * (nct + 1), ctx->st));
+  launch_ref_cells(ctx->S, ctx->st, rep, il, nc, dco, dcnt);
+  ctx->launches += 1;
+  CK(cudaMemcpyAsync(cell_of, dco, sizeof(int) * s.n_mon_tot, cudaMemcpyDeviceToHost, ctx->st));
+  if (counts) CK(cudaMemcpyAsync(counts, dcnt, sizeof(int) * (nct + 1), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaFreeAsync(dco, ctx->st));
+  CK(cudaFreeAsync(dcnt, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return MFA_OK;
+}
+
+int mfa_cell_neigh_list(const int32_t* n_cells, int32_t n_nei, int32_t* out) {
+  if (!n_cells || !out || (n_nei != 13 && n_nei != 62)) return MFA_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MFA_ERR_NO_DEVICE;
+  const long long nct = (long long)n_cells[0] * n_cells[1] * n_cells[2];
+  if (nct <= 0 || nct > (1ll << 26)) return MFA_ERR_ARG;
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int) * nct * n_nei) != cudaSuccess) return MFA_ERR_ALLOC;
+  launch_cell_neigh(n_cells, n_nei, d, 0);
+  cudaError_t e = cudaMemcpy(out, d, sizeof(int) * nct * n_nei, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? MFA_OK : MFA_ERR_CUDA;
+}
+
+int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n) {
+  if (!ctx || rep < 0 || rep >= ctx->nrep || !n || cap < 0) return MFA_ERR_ARG;
+  int* dp = nullptr;
+  unsigned long long* dc = nullptr;
+  CK(cudaMallocAsync(&dp, sizeof(int) * 2 * std::max<int64_t>(cap, 1), ctx->st));
+  CK(cudaMallocAsync(&dc, sizeof(unsigned long long), ctx->st));
+  CK(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), ctx->st));
+  launch_pair_list(ctx->S, ctx->C, ctx->st, rep, dp, cap, dc);
+  ctx->launches += 1;
+  unsigned long long hc = 0;
+  CK(cudaMemcpyAsync(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  *n = (int64_t)hc;
+  if (pairs && cap > 0)
+    CK(cudaMemcpyAsync(pairs, dp, sizeof(int) * 2 * std::min<int64_t>(cap, (int64_t)hc), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaFreeAsync(dp, ctx->st));
+  CK(cudaFreeAsync(dc, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return MFA_OK;
+}
+
+// ---- timing ---------------------------------------------------------------------------------
+int mfa_event_record(mfa_ctx* ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot >= 16) return MFA_ERR_ARG;
+  CK(cudaEventRecord(ctx->ev[slot], ctx->st));
+  return MFA_OK;
+}
+
+int mfa_event_elapsed(mfa_ctx* ctx, int32_t a, int32_t b, float* ms) {
+  if (!ctx || !ms || a < 0 || b < 0 || a >= 16 || b >= 16) return MFA_ERR_ARG;
+  CK(cudaEventSynchronize(ctx->ev[b]));
+  CK(cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
+  return MFA_OK;
+}
+
+const char* mfa_kernel_name(int32_t fam) { return (fam >= 0 && fam < MFA_NKFAM) ? kFamNames[fam] : "?"; }
+
+int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* launches) {
+  if (!ctx || nsteps < 1 || !mean_ms) return MFA_ERR_ARG;
+  const DevState& S = ctx->S;
+  const SimConst& C = ctx->C;
+  cudaStream_t st = ctx->st;
+  Acc acc = acc_of(ctx->acc_step, ctx->nrep);
+  const int mask = any_chains(ctx) ? bonded_mask(ctx) : 0;
+  std::vector<cudaEvent_t> evs;
+  std::vector<int> fam;
+  auto mark = [&](int f) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, st);
+    evs.push_back(e);
+    fam.push_back(f);
+  };
+  // the first position update belongs to the "positions" family; each step then runs
+  // rebuild, pair, bonded, kspace and the fused velocity+position kernel
+  mark(-1);
+  launch_integrate(S, C, st, 0, false, false, acc);
+  mark(7);
+  for (int k = 1; k <= nsteps; ++k) {
+    const bool ef = (k == nsteps);
+    launch_rebuild(S, st, false);
+    k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
+    mark(0);
+    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
+    mark(1);
+    if (mask) { launch_bonded(S, C, st, mask, ef, acc); mark(2); }
+    if (ctx->kspace) { launch_kspace(S, C, ctx->K, st, ef, acc); launch_dipolar(S, C, ctx->K, st, ef, acc); mark(4); }
+    launch_integrate(S, C, st, k < nsteps ? 2 : 1, true, ef, acc);
+    mark(3);
+    if (ef) { launch_record(acc, ctx->rec, st); mark(6); }
+  }
+  CK(cudaStreamSynchronize(st));
+  std::vector<double> tot(MFA_NKFAM, 0.);
+  std::vector<int> cnt(MFA_NKFAM, 0);
+  for (size_t k = 1; k < evs.size(); ++k) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, evs[k - 1], evs[k]);
+    tot[fam[k]] += ms;
+    cnt[fam[k]] += 1;
+  }
+  for (auto e : evs) cudaEventDestroy(e);
+  for (int f = 0; f < MFA_NKFAM; ++f) {
+    mean_ms[f] = cnt[f] ? (float)(tot[f] / cnt[f]) : 0.f;
+    if (launches) launches[f] = cnt[f];
+  }
+  ctx->host_steps += nsteps;
+  ctx->last_source = 1;
+  return post_status(ctx);
+}
+
+int mfa_launch_count(mfa_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return MFA_ERR_ARG;
+  *n = ctx->launches;
+  return MFA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// mfa_dev.cuh -- device-side data layout and helpers of the GB300 MD-DPD step.
+//
+// Layout in HBM (one context = R replicas sharing one parameter set):
+//   * particles of all replicas live in ONE sorted order ("slots"): replica-major, then by
+//     neighbour-list cell, then by tag; the order is rebuilt by a counting sort when any particle
+//     moved more than skin/2 since the last rebuild (check_skin.f90:11-24 semantics);
+//   * master state in slot order, FP64 structure-of-arrays: r[3][Np], v[3][Np], a[3][Np], f[3][Np];
+//   * pair-kernel views, rewritten by every position update:
+//       mixed: int4  {x,y,z fixed point, info}  + float4  {vx,vy,vz, tag}
+//       fp64 : double4{x,y,z, info bits}        + double4 {vx,vy,vz, tag bits}
+//     Fixed point: x,y use 2^32 units per box length, so an int32 difference is the minimum
+//     image (fluid_fluid.f90:111-112) for free; z uses 2^30 units per channel width D.
+//   * full Verlet list in column-major "ELL" form: nbr[k*Np + slot], count nn[slot].
+// info word: bits 0-3 type (0-based), bit 4 mobile, bit 5 brush head, bits 6-7 profile species
+// (0 brush, 1 melt, 2 particle 4, 3 none), bits 8-31 replica index.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mfa {
+
+constexpr int MAXT = 6;
+constexpr int NPAIR = MAXT * MAXT;
+constexpr int NOBS = 12;  // per-replica energy accumulator slots
+enum Obs { O_VFF = 0, O_VFW, O_VWW, O_VINTRA, O_VBEND, O_VBENDM, O_VOR, O_VCOUL, O_TFLUID, O_VCOULK, O_VDIP };
+
+// status bits
+constexpr unsigned ST_NLIST_OVERFLOW = 1u, ST_OUT_OF_BOX = 2u, ST_NAN = 4u;
+
+// pair flags
+constexpr int PF_LJ = 1, PF_DPD_LJ = 2, PF_DPD_OWN = 4, PF_COUL = 8;
+
+// 32-byte aligned double quadruple (one 256-bit load on sm_100 and later)
+using dbl4 = double4_32a;
+__host__ __device__ inline dbl4 mk_dbl4(double x, double y, double z, double w) {
+  dbl4 r;
+  r.x = x; r.y = y; r.z = z; r.w = w;
+  return r;
+}
+
+__host__ __device__ inline int info_type(int w) { return w & 15; }
+__host__ __device__ inline bool info_mobile(int w) { return (w >> 4) & 1; }
+__host__ __device__ inline bool info_head(int w) { return (w >> 5) & 1; }
+__host__ __device__ inline int info_species(int w) { return (w >> 6) & 3; }
+__host__ __device__ inline int info_rep(int w) { return (int)((unsigned)w >> 8); }
+
+template <typename T>
+struct PairEntry {
+  T range2, eps4, sig2, shift, inv_rc;  // LJ; inv_rc = 1/sqrt(range2) for the DPD weight
+  T rlist2;                             // (cut-off + skin)^2 for the neighbour list
+  T dpd_rc2, inv_dpd_rc;                // own DPD cut-off (DPD_CUT_OFF)
+  T qq;                                 // charge product (real-space Ewald)
+  int flags;
+};
+
+// Scalars shared by every replica (passed by value).
+struct SimConst {
+  int n_type;
+  int thermostat_dpd, dpd_weight1, force_switch_on, poiseuille, bending, bending_melt, orientation;
+  int bend_form, charged, compat_i_only, wall;
+  double dt, half_dt, half_dt2;
+  double mass[MAXT], inv_mass[MAXT];
+  double gamma, sig;             // DPD friction and noise amplitude sqrt(2 kT gamma/dt)
+  double r2min_init, r2min_time; // force switch-on ramp
+  double sigma_wall[MAXT], a_wall[MAXT], a_w;
+  double k_chain, inv_r_chain_2, fene_xmax;
+  double k_bend, alpha_eq, k_or, alpha_or, bend_small;
+  double const_force[3];
+  double charge[MAXT];
+  double sqrt_alpha, alpha_c, inv_sqrt_pi;
+  double coul_rc2;                // own Coulomb cut-off^2 (0: inside LJ range)
+  double skin_half2;              // (skin/2)^2
+  int hist_dim;
+};
+
+// Per replica (device array, read through the L1).
+struct RepDesc {
+  double L[3], invL[3];
+  double sfx[3];        // fixed-point units per sigma
+  double ufx[3];        // sigma per fixed-point unit
+  float ufx_f[3];
+  double inv_lc[3];     // neighbour-list grid
+  int nc[3];
+  int cell_off, ncell;
+  int p0, n_part, n_mon_tot;
+  int n_mon, n_chain, n_mon_d, n_chain_d, n_mon_e, n_chain_e, part_init_d, part_init_e;
+  unsigned long long seed;
+  long long s_time;
+  double lz_half, v_ww, inv_n;
+  double hist_inv_dz;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) keyed on the replica seed; counter (step, tag_lo, tag_hi).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
+                                              uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) { k0 += W0; k1 += W1; }
+    uint32_t hi0 = __umulhi(M0, c0), lo0 = M0 * c0;
+    uint32_t hi1 = __umulhi(M1, c2), lo1 = M1 * c2;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+}
+
+// Two 23-bit uniforms of the unordered pair (ta, tb): u1 in (0,1), u2 in [0,1), exact in FP32.
+__device__ __forceinline__ void pair_uniform_bits(unsigned long long seed, long long step, int ta, int tb,
+                                                  uint32_t& b1, uint32_t& b2) {
+  uint32_t lo = (uint32_t)min(ta, tb), hi = (uint32_t)max(ta, tb);
+  uint32_t c0 = (uint32_t)(unsigned long long)step, c1 = (uint32_t)((unsigned long long)step >> 32);
+  uint32_t c2 = lo, c3 = hi;
+  philox4x32_10(c0, c1, c2, c3, (uint32_t)seed, (uint32_t)(seed >> 32));
+  b1 = c0 >> 9;
+  b2 = c1 >> 9;
+}
+
+__device__ __forceinline__ float pair_gauss_f(unsigned long long seed, long long step, int ta, int tb) {
+  uint32_t b1, b2;
+  pair_uniform_bits(seed, step, ta, tb, b1, b2);
+  float u1 = ((float)b1 + 0.5f) * (1.0f / 8388608.0f);
+  float u2 = (float)b2 * (1.0f / 8388608.0f);
+  return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+}
+
+__device__ __forceinline__ double pair_gauss_d(unsigned long long seed, long long step, int ta, int tb) {
+  uint32_t b1, b2;
+  pair_uniform_bits(seed, step, ta, tb, b1, b2);
+  double u1 = ((double)b1 + 0.5) * (1.0 / 8388608.0);
+  double u2 = (double)b2 * (1.0 / 8388608.0);
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fixed-point positions
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int to_fx_periodic(double x, double s) {
+  // x in [0, L] -> [0, 2^32) modulo 2^32
+  long long v = __double2ll_rn(x * s);
+  return (int)(unsigned int)(unsigned long long)v;
+}
+__device__ __forceinline__ int to_fx_z(double z, double s) { return (int)__double2ll_rn(z * s); }
+__device__ __forceinline__ int fx_diff(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
+
+// Minimum image of the reference: d - L*int(2 d / L) (fluid_fluid.f90:111-112).
+__device__ __forceinline__ double mic_ref(double d, double L, double invL) {
+  return d - L * (double)(long long)(2. * d * invL);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Reductions
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Adds v into col[rep] (one accumulator column of the slot-major [NOBS][nrep] array).  Must be called by all 32 lanes of the warp (kernels keep
+// every lane alive and mask work with `active`); lanes sharing a replica are summed first, so
+// the common case (one replica per warp) costs one warp reduction and one FP64 atomic.
+__device__ __forceinline__ void add_obs(double* col, int rep, double v, bool active, int nrep = 0) {
+  (void)nrep;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int key = active ? rep : -1;
+  unsigned todo = FULL;
+  while (todo) {
+    int l = __ffs(todo) - 1;
+    int k = __shfl_sync(FULL, key, l);
+    bool mine = (key == k);
+    unsigned grp = __ballot_sync(FULL, mine);
+    double s = warp_sum(mine ? v : 0.);
+    if (k >= 0 && lane == l) atomicAdd(&col[k], s);
+    todo &= ~grp;
+  }
+}
+
+}  // namespace mfa

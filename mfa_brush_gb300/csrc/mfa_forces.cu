@@ -1,0 +1,513 @@
+// mfa_forces.cu -- force kernels of the MD-DPD step.
+//
+// k_pair   : fluid_fluid.f90:97-261 with dpd_forces.f90:45-115 and ewald_real.f90:15-33 fused.
+//            One thread per particle walks its full Verlet list (no atomics, no Newton-3 scatter);
+//            each unordered pair is therefore evaluated from both sides, and the DPD noise is a
+//            Philox draw keyed on (seed, step, min tag, max tag) so both sides see the same g and
+//            momentum is conserved exactly in exact arithmetic.  Energies are halved per visit.
+//            MIXED: positions are fixed-point int4 (the int32 difference is the x,y minimum image),
+//            all pair arithmetic is FP32, the per-particle sum is FP32 and stored as FP64.
+// k_bonded : intra_molec.f90:16-188 (FENE), bending.f90:19-121 / bending_melt.f90:22-108 and
+//            orientation.f90:24-88.  Owner computes: the thread of bead m evaluates every bond,
+//            angle and orientation term that acts on m (terms centred on m-1, m, m+1) and adds
+//            its own share, so no two threads write one particle.
+// k_wall   : fluid_wall.f90:77-125 (implicit 9-3 walls), FP64.
+// k_cforce : constant_force.f90:17-21 (Poiseuille body force m*g on every non-head bead).
+#include <type_traits>
+
+#include "mfa_state.cuh"
+
+namespace mfa {
+
+template <bool MIXED>
+using real_t = typename std::conditional<MIXED, float, double>::type;
+
+__device__ __forceinline__ double r2min_of(const SimConst& C, long long step) {
+  if (!C.force_switch_on) return 0.;
+  double r_time = (double)step * C.dt;
+  return (r_time < C.r2min_time) ? (1. - r_time / C.r2min_time) * C.r2min_init : 0.;
+}
+
+template <bool MIXED, bool EFLAG>
+__global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accumulate, Acc acc) {
+  using real = real_t<MIXED>;
+  __shared__ PairEntry<real> tab[NPAIR];
+  for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
+    if constexpr (MIXED) tab[k] = s.tabf[k]; else tab[k] = s.tabd[k];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool inside = i < s.N;
+  const int w = inside ? __ldg(&s.info[i]) : 0;
+  const bool active = inside && info_mobile(w);
+  const int rep = info_rep(w);
+  real fx = 0, fy = 0, fz = 0;
+  real e_lj = 0, e_c = 0;
+  if (active) {
+    const RepDesc& R = s.reps[rep];
+    const long long step = R.s_time + *s.steps_done;
+    const real r2min = (real)r2min_of(C, step);
+    const int ti = info_type(w);
+    const int n = __ldg(&s.nn[i]);
+    const real sig = (real)C.sig, gam = (real)C.gamma;
+    const int p0 = R.p0;
+    // own position / velocity
+    int4 qi;
+    dbl4 pi;
+    real vix, viy, viz;
+    int tag_i;
+    real ux = 0, uy = 0, uz = 0;
+    if constexpr (MIXED) {
+      qi = __ldg(&s.pfx[i]);
+      float4 v4 = __ldg(&s.vf[i]);
+      vix = v4.x; viy = v4.y; viz = v4.z;
+      tag_i = __float_as_int(v4.w) - p0;
+      ux = R.ufx_f[0]; uy = R.ufx_f[1]; uz = R.ufx_f[2];
+    } else {
+      pi = s.pd[i];
+      dbl4 v4 = s.vd[i];
+      vix = v4.x; viy = v4.y; viz = v4.z;
+      tag_i = (int)__double_as_longlong(v4.w) - p0;
+    }
+    const double L0 = R.L[0], L1 = R.L[1], iL0 = R.invL[0], iL1 = R.invL[1];
+    const unsigned long long seed = R.seed;
+    const int* __restrict__ nb = s.nbr + i;
+    for (int k = 0; k < n; ++k) {
+      const int j = __ldg(nb + (size_t)k * s.Np);
+      real dx, dy, dz;
+      int wj;
+      if constexpr (MIXED) {
+        int4 qj = __ldg(&s.pfx[j]);
+        wj = qj.w;
+        dx = (float)fx_diff(qi.x, qj.x) * ux;
+        dy = (float)fx_diff(qi.y, qj.y) * uy;
+        dz = (float)fx_diff(qi.z, qj.z) * uz;
+      } else {
+        dbl4 pj = s.pd[j];
+        wj = (int)__double_as_longlong(pj.w);
+        dx = mic_ref(pi.x - pj.x, L0, iL0);
+        dy = mic_ref(pi.y - pj.y, L1, iL1);
+        dz = pi.z - pj.z;
+      }
+      const real r2raw = dx * dx + dy * dy + dz * dz;
+      const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
+      const int fl = e.flags;
+      real r2 = r2raw;
+      const bool in_lj = r2raw < e.range2;
+      real fs = 0;  // force factor along d = r_i - r_j
+      if (in_lj) {
+        r2 = r2raw < r2min ? r2min : r2raw;
+        const real inv_r2 = (real)1 / r2;
+        const real s2 = e.sig2 * inv_r2;
+        const real s6 = s2 * s2 * s2;
+        const real s12 = s6 * s6;
+        fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
+        if (EFLAG) e_lj += (real)0.5 * e.eps4 * ((s12 - s6) - e.shift);
+      }
+      const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
+      if (dpd) {
+        real vjx, vjy, vjz;
+        int tag_j;
+        if constexpr (MIXED) {
+          float4 v4 = __ldg(&s.vf[j]);
+          vjx = v4.x; vjy = v4.y; vjz = v4.z;
+          tag_j = __float_as_int(v4.w) - p0;
+        } else {
+          dbl4 v4 = s.vd[j];
+          vjx = v4.x; vjy = v4.y; vjz = v4.z;
+          tag_j = (int)__double_as_longlong(v4.w) - p0;
+        }
+        const real r = sqrt(r2);
+        const real ir = (real)1 / r;
+        real wr, wd;
+        if (C.dpd_weight1) {
+          wr = wd = 1;
+        } else {
+          wr = (real)1 - r * ((fl & PF_DPD_OWN) ? e.inv_dpd_rc : e.inv_rc);
+          wd = wr * wr;
+        }
+        real g;
+        if constexpr (MIXED) g = pair_gauss_f(seed, step, tag_i, tag_j);
+        else g = pair_gauss_d(seed, step, tag_i, tag_j);
+        const real rdot = ((vix - vjx) * dx + (viy - vjy) * dy + (viz - vjz) * dz) * ir;
+        fs += (sig * wr * g - gam * wd * rdot) * ir;
+      }
+      if (fl & PF_COUL) {
+        const bool in_c = (C.coul_rc2 > 0.) ? (r2raw < (real)C.coul_rc2) : in_lj;
+        if (in_c) {
+          const real rc2 = in_lj ? r2 : r2raw;
+          const real r = sqrt(rc2), ir = (real)1 / r;
+          const real qq = e.qq;
+          const real ec = erfc((real)C.sqrt_alpha * r);
+          if (EFLAG) e_c += (real)0.5 * qq * ec * ir;
+          fs += (qq * (real)C.sqrt_alpha * (real)C.inv_sqrt_pi * (real)2 * exp(-(real)C.alpha_c * rc2) * ir +
+                 qq * ec * ir * ir) * ir;
+        }
+      }
+      fx += fs * dx;
+      fy += fs * dy;
+      fz += fs * dz;
+    }
+  }
+  if (inside) {
+    if (accumulate) {
+      if (active) {
+        s.fx[i] += (double)fx;
+        s.fy[i] += (double)fy;
+        s.fz[i] += (double)fz;
+      }
+    } else {
+      s.fx[i] = (double)fx;
+      s.fy[i] = (double)fy;
+      s.fz[i] = (double)fz;
+    }
+  }
+  if (EFLAG) {
+    add_obs(acc.col(O_VFF), rep, (double)e_lj, active, acc.nrep);
+    if (C.charged) add_obs(acc.col(O_VCOUL), rep, (double)e_c, active, acc.nrep);
+  }
+}
+
+void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag, Acc acc,
+                 int block) {
+  (void)block;
+  int B = 128;
+  int g = (s.N + B - 1) / B;
+  if (s.mixed) {
+    if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
+    else k_pair<true, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
+  } else {
+    if (eflag) k_pair<false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
+    else k_pair<false, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bonded terms
+// ---------------------------------------------------------------------------------------------
+template <bool MIXED>
+struct BeadPos;
+template <>
+struct BeadPos<true> {
+  int4 q;
+  __device__ void load(const DevState& s, int slot) { q = __ldg(&s.pfx[slot]); }
+};
+template <>
+struct BeadPos<false> {
+  double x, y, z;
+  __device__ void load(const DevState& s, int slot) { x = s.rx[slot]; y = s.ry[slot]; z = s.rz[slot]; }
+};
+
+// a - b with the x,y minimum image
+template <bool MIXED>
+__device__ __forceinline__ void bead_delta(const BeadPos<MIXED>& a, const BeadPos<MIXED>& b, const RepDesc& R,
+                                           real_t<MIXED>* d) {
+  if constexpr (MIXED) {
+    d[0] = (float)fx_diff(a.q.x, b.q.x) * R.ufx_f[0];
+    d[1] = (float)fx_diff(a.q.y, b.q.y) * R.ufx_f[1];
+    d[2] = (float)fx_diff(a.q.z, b.q.z) * R.ufx_f[2];
+  } else {
+    d[0] = mic_ref(a.x - b.x, R.L[0], R.invL[0]);
+    d[1] = mic_ref(a.y - b.y, R.L[1], R.invL[1]);
+    d[2] = a.z - b.z;
+  }
+}
+
+// One angle term of bending.f90:47-109 with r_prev = r_c - r_{c-1}, r_next = r_{c+1} - r_c.
+// fa acts on c-1, fc on c+1 (c gets -fa-fc).  MIXED computes the angle as atan2(|p x n|, p.n),
+// which keeps FP32 accurate for the nearly straight chains that stiff brushes produce.
+template <bool MIXED>
+__device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, const SimConst& C, real_t<MIXED> kb,
+                          real_t<MIXED> aeq, real_t<MIXED>* fa, real_t<MIXED>* fc, real_t<MIXED>& e) {
+  using real = real_t<MIXED>;
+  real dot = 0, rp2 = 0, rn2 = 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dot += rn[j] * rp[j];
+    rp2 += rp[j] * rp[j];
+    rn2 += rn[j] * rn[j];
+  }
+  real dn[3], dp[3], dn2 = 0, dp2 = 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dn[j] = rp[j] * rn2 - rn[j] * dot;
+    dp[j] = -rn[j] * rp2 + rp[j] * dot;
+    dn2 += dn[j] * dn[j];
+    dp2 += dp[j] * dp[j];
+  }
+  const real small = (real)C.bend_small;
+  const real srp = sqrt(rp2), srn = sqrt(rn2);
+  if (dn2 < small) {
+    real u[3], nu = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
+    nu = sqrt(nu);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dn[j] = (nu != 0) ? u[j] / nu / srn : (real)0;
+  } else {
+    const real sc = (real)1 / sqrt(dn2 * rn2);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dn[j] *= sc;
+  }
+  if (dp2 < small) {
+    real u[3], nu = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
+    nu = sqrt(nu);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dp[j] = (nu != 0) ? u[j] / nu / srp : (real)0;
+  } else {
+    const real sc = (real)1 / sqrt(dp2 * rp2);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dp[j] *= sc;
+  }
+  real alpha;
+  if constexpr (MIXED) {
+    real cx = rp[1] * rn[2] - rp[2] * rn[1];
+    real cy = rp[2] * rn[0] - rp[0] * rn[2];
+    real cz = rp[0] * rn[1] - rp[1] * rn[0];
+    alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
+  } else {
+    real ca = dot / sqrt(rp2 * rn2);
+    alpha = (ca >= 1.0) ? aeq : acos(ca);  // bending.f90:93-98 guard: delta_alpha = 0
+  }
+  real fm;
+  if (C.bend_form == 1) {
+    fm = kb * sin(alpha);
+    e = kb * ((real)1 - cos(alpha));
+  } else {
+    real da = alpha - aeq;
+    fm = kb * da;
+    e = (real)0.5 * fm * da;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    fa[j] = fm * dp[j];
+    fc[j] = fm * dn[j];
+  }
+}
+
+template <bool MIXED, bool EFLAG>
+__global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask, Acc acc) {
+  using real = real_t<MIXED>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool inside = i < s.N;
+  const int w = inside ? __ldg(&s.info[i]) : 0;
+  bool active = inside && info_mobile(w);
+  const int rep = info_rep(w);
+  real F[3] = {0, 0, 0};
+  real e_fene = 0, e_bend = 0, e_bendm = 0, e_or = 0;
+  int kind = -1, m = 0, n = 0, t0 = 0;
+  const RepDesc* Rp = nullptr;
+  if (active) {
+    Rp = &s.reps[rep];
+    const RepDesc& R = *Rp;
+    int t = __ldg(&s.tag[i]);
+    int lt = t - R.p0;
+    if (lt < R.part_init_d) {
+      kind = 0; n = R.n_mon; m = lt % n;
+    } else if (lt < R.part_init_e) {
+      kind = 1; n = R.n_mon_d; m = (lt - R.part_init_d) % n;
+    } else if (lt < R.n_mon_tot) {
+      kind = 2; n = R.n_mon_e; m = (lt - R.part_init_e) % n;
+    }
+    t0 = t - m;
+    if (n < 2) kind = -1;
+  }
+  if (kind >= 0) {
+    const RepDesc& R = *Rp;
+    const bool do_fene = mask & 1;
+    const bool do_bend = (kind == 0 && (mask & 2)) || (kind == 1 && (mask & 4));
+    const bool do_or = kind == 0 && (mask & 8) && m <= 1;
+    const int lo = max(0, m - ((do_bend) ? 2 : 1)), hi = min(n - 1, m + ((do_bend) ? 2 : 1));
+    BeadPos<MIXED> P[5];  // beads m-2 .. m+2
+    for (int b = lo; b <= hi; ++b) P[b - m + 2].load(s, __ldg(&s.slot_of_tag[t0 + b]));
+    if (do_fene) {
+      const real kc = (real)C.k_chain, ir2 = (real)C.inv_r_chain_2, xm = (real)C.fene_xmax;
+      if (m > 0) {  // bond (m-1, m): this bead is the second partner
+        real d[3];
+        bead_delta<MIXED>(P[1], P[2], R, d);
+        real x = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * ir2;
+        x = x < xm ? x : xm;
+        real fac = kc / ((real)1 - x) * ir2;
+        F[0] += fac * d[0]; F[1] += fac * d[1]; F[2] += fac * d[2];
+      }
+      if (m < n - 1) {  // bond (m, m+1): first partner; energy counted here
+        real d[3];
+        bead_delta<MIXED>(P[2], P[3], R, d);
+        real x = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * ir2;
+        x = x < xm ? x : xm;
+        real fac = kc / ((real)1 - x) * ir2;
+        F[0] -= fac * d[0]; F[1] -= fac * d[1]; F[2] -= fac * d[2];
+        if (EFLAG) e_fene += kc * ((real)-0.5 * log((real)1 - x));
+      }
+    }
+    if (do_bend) {
+      const real kb = (real)C.k_bend, aeq = (real)C.alpha_eq;
+      for (int c = m - 1; c <= m + 1; ++c) {
+        if (c < 1 || c > n - 2) continue;
+        real rp[3], rn[3], fa[3], fc[3], e;
+        bead_delta<MIXED>(P[c - m + 2], P[c - 1 - m + 2], R, rp);
+        bead_delta<MIXED>(P[c + 1 - m + 2], P[c - m + 2], R, rn);
+        bend_term<MIXED>(rp, rn, C, kb, aeq, fa, fc, e);
+        if (c == m + 1) { F[0] += fa[0]; F[1] += fa[1]; F[2] += fa[2]; }
+        else if (c == m) {
+          F[0] -= fa[0] + fc[0]; F[1] -= fa[1] + fc[1]; F[2] -= fa[2] + fc[2];
+          if (EFLAG) { if (kind == 0) e_bend += e; else e_bendm += e; }
+        } else { F[0] += fc[0]; F[1] += fc[1]; F[2] += fc[2]; }
+      }
+    }
+    if (do_or) {
+      // orientation.f90:35-88: ghost bond head -> head -/+ z, against bond 1
+      const BeadPos<MIXED>& H = P[2 - m];
+      const BeadPos<MIXED>& B1 = P[3 - m];
+      real rp[3], rn[3];
+      bead_delta<MIXED>(B1, H, R, rn);
+      double hz;
+      if constexpr (MIXED) hz = (double)H.q.z * R.ufx[2]; else hz = H.z;
+      if constexpr (MIXED) {
+        rp[0] = 0; rp[1] = 0; rp[2] = (hz > R.L[2] / 2) ? -1.f : 1.f;
+      } else {
+        double g = (hz > R.L[2] / 2) ? hz + 1.0 : hz - 1.0;
+        rp[0] = 0; rp[1] = 0; rp[2] = hz - g;
+      }
+      real dot = 0, rp2 = 0, rn2 = 0, dn[3], dn2 = 0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { dot += rn[j] * rp[j]; rp2 += rp[j] * rp[j]; rn2 += rn[j] * rn[j]; }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { dn[j] = rp[j] * rn2 - rn[j] * dot; dn2 += dn[j] * dn[j]; }
+      const real srp = sqrt(rp2), srn = sqrt(rn2);
+      if (dn2 < (real)C.bend_small) {
+        real u[3], nu = 0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
+        nu = sqrt(nu);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) dn[j] = (nu != 0) ? u[j] / nu / srn : (real)0;
+      } else {
+        const real sc = (real)1 / sqrt(dn2 * rn2);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) dn[j] *= sc;
+      }
+      real alpha;
+      if constexpr (MIXED) {
+        real cx = rp[1] * rn[2] - rp[2] * rn[1];
+        real cy = rp[2] * rn[0] - rp[0] * rn[2];
+        real cz = rp[0] * rn[1] - rp[1] * rn[0];
+        alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
+      } else {
+        real ca = dot / sqrt(rp2 * rn2);
+        alpha = (ca >= 1.0) ? 0. : acos(ca);
+      }
+      const real da = alpha - (real)C.alpha_or;
+      const real fm = (real)C.k_or * da;
+      const real sgn = (m == 0) ? (real)-1 : (real)1;
+      F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
+      if (EFLAG && m == 0) e_or += (real)0.5 * fm * da;
+    }
+    s.fx[i] += (double)F[0];
+    s.fy[i] += (double)F[1];
+    s.fz[i] += (double)F[2];
+  }
+  if (EFLAG) {
+    active = active && kind >= 0;
+    if (mask & 1) add_obs(acc.col(O_VINTRA), rep, (double)e_fene, active, acc.nrep);
+    if (mask & 2) add_obs(acc.col(O_VBEND), rep, (double)e_bend, active, acc.nrep);
+    if (mask & 4) add_obs(acc.col(O_VBENDM), rep, (double)e_bendm, active, acc.nrep);
+    if (mask & 8) add_obs(acc.col(O_VOR), rep, (double)e_or, active, acc.nrep);
+  }
+}
+
+void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc) {
+  if (!mask) return;
+  int B = 128, g = (s.N + B - 1) / B;
+  if (s.mixed) {
+    if (eflag) k_bonded<true, true><<<g, B, 0, st>>>(s, C, mask, acc);
+    else k_bonded<true, false><<<g, B, 0, st>>>(s, C, mask, acc);
+  } else {
+    if (eflag) k_bonded<false, true><<<g, B, 0, st>>>(s, C, mask, acc);
+    else k_bonded<false, false><<<g, B, 0, st>>>(s, C, mask, acc);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Implicit 9-3 walls and the constant body force
+// ---------------------------------------------------------------------------------------------
+template <bool EFLAG>
+__global__ void k_wall(DevState s, SimConst C, Acc acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool inside = i < s.N;
+  const int w = inside ? s.info[i] : 0;
+  const bool active = inside && info_mobile(w);
+  double e = 0.;
+  if (active) {
+    const RepDesc& R = s.reps[info_rep(w)];
+    s.fz[i] += wall93(C, info_type(w), s.rz[i], R.L[2], e);
+  }
+  if (EFLAG) add_obs(acc.col(O_VFW), info_rep(w), e, active, acc.nrep);
+}
+
+void launch_wall(const DevState& s, const SimConst& C, cudaStream_t st, bool eflag, Acc acc) {
+  int B = 256, g = (s.N + B - 1) / B;
+  if (eflag) k_wall<true><<<g, B, 0, st>>>(s, C, acc);
+  else k_wall<false><<<g, B, 0, st>>>(s, C, acc);
+}
+
+__global__ void k_cforce(DevState s, SimConst C) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  const int w = s.info[i];
+  if (!info_mobile(w) || info_type(w) == 0) return;
+  const double m = C.mass[info_type(w)];
+  s.fx[i] += m * C.const_force[0];
+  s.fy[i] += m * C.const_force[1];
+  s.fz[i] += m * C.const_force[2];
+}
+
+void launch_const_force(const DevState& s, const SimConst& C, cudaStream_t st) {
+  int B = 256, g = (s.N + B - 1) / B;
+  k_cforce<<<g, B, 0, st>>>(s, C);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Pair list export: every interacting pair (local tags, i<j) of replica `rep`, FP64 distances.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_pair_list(DevState s, SimConst C, int rep, int* __restrict__ out, long long cap,
+                            unsigned long long* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  const int w = s.info[i];
+  if (info_rep(w) != rep || !info_mobile(w)) return;
+  const RepDesc& R = s.reps[rep];
+  const int ti = info_type(w), tgi = s.tag[i];
+  const int n = s.nn[i];
+  for (int k = 0; k < n; ++k) {
+    int j = s.nbr[(size_t)k * s.Np + i];
+    int wj = s.info[j];
+    int tgj = s.tag[j];
+    if (!info_mobile(wj) || tgj <= tgi) continue;
+    double dx = mic_ref(s.rx[i] - s.rx[j], R.L[0], R.invL[0]);
+    double dy = mic_ref(s.ry[i] - s.ry[j], R.L[1], R.invL[1]);
+    double dz = s.rz[i] - s.rz[j];
+    double r2 = dx * dx + dy * dy + dz * dz;
+    const PairEntry<double>& e = s.tabd[ti * MAXT + info_type(wj)];
+    bool hit = r2 < e.range2;
+    if (!hit && (e.flags & PF_DPD_OWN)) hit = r2 < e.dpd_rc2;
+    if (!hit && (e.flags & PF_COUL) && C.coul_rc2 > 0.) hit = r2 < C.coul_rc2;
+    if (hit) {
+      unsigned long long k2 = atomicAdd(count, 1ull);
+      if ((long long)k2 < cap) {
+        out[2 * k2] = tgi - R.p0;
+        out[2 * k2 + 1] = tgj - R.p0;
+      }
+    }
+  }
+}
+
+void launch_pair_list(const DevState& s, const SimConst& C, cudaStream_t st, int rep, int* pairs, long long cap,
+                      unsigned long long* count) {
+  int B = 128, g = (s.N + B - 1) / B;
+  k_pair_list<<<g, B, 0, st>>>(s, C, rep, pairs, cap, count);
+}
+
+}  // namespace mfa

@@ -1,0 +1,259 @@
+// mfa_integrate.cu -- velocity-Verlet integration, profiles and host-layout kernels.
+//
+// k_integrate<MODE>:
+//   MODE 0  verlet_positions.f90:150-209: r += dt v + dt^2/2 a, x,y wrapped into [0,L),
+//           v += dt/2 a; then the pair-kernel views and the skin test (displacement since the
+//           last rebuild > skin/2 raises the rebuild flag; check_skin.f90:11-24).
+//   MODE 1  verlet_velocities.f90:25-153: a = F/m, v += dt/2 a, brush heads held fixed
+//           (v = a = F = 0, the POISEUILLE branch :113-120; without POISEUILLE the implicit-wall
+//           heads move with va_spring_twall, which must be 0 here), kinetic energy.
+//   MODE 2  MODE 1 of step n followed by MODE 0 of step n+1 in one pass (the fused step): one
+//           read of r, v, F and one write of r, v and the views per particle per step.
+//   add_ext adds the 9-3 wall force (fluid_wall.f90:96-121) and the body force
+//           (constant_force.f90:17-21) inside the kernel instead of separate passes.
+// All integration is FP64 in both precision modes.
+#include "mfa_state.cuh"
+
+namespace mfa {
+
+__device__ __forceinline__ void store_views(const DevState& s, int i, const RepDesc& R, double x, double y,
+                                            double z, double vx, double vy, double vz, int w, int t, int4& q) {
+  q.x = to_fx_periodic(x, R.sfx[0]);
+  q.y = to_fx_periodic(y, R.sfx[1]);
+  q.z = to_fx_z(z, R.sfx[2]);
+  q.w = w;
+  if (s.mixed) {
+    s.pfx[i] = q;
+    s.vf[i] = make_float4((float)vx, (float)vy, (float)vz, __int_as_float(t));
+  } else {
+    s.pd[i] = mk_dbl4(x, y, z, __longlong_as_double((long long)w));
+    s.vd[i] = mk_dbl4(vx, vy, vz, __longlong_as_double((long long)t));
+  }
+}
+
+template <int MODE, bool ADDEXT, bool EFLAG>
+__global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool inside = i < s.N;
+  const int w = inside ? s.info[i] : 0;
+  const bool mob = inside && info_mobile(w);
+  const int rep = info_rep(w);
+  double ke = 0., efw = 0.;
+  if (mob) {
+    const RepDesc& R = s.reps[rep];
+    const int t = info_type(w);
+    double x = s.rx[i], y = s.ry[i], z = s.rz[i];
+    double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+    double ax, ay, az;
+    if (MODE >= 1) {
+      double Fx = s.fx[i], Fy = s.fy[i], Fz = s.fz[i];
+      if (ADDEXT) {
+        if (C.wall == 2) {
+          double e;
+          Fz += wall93(C, t, z, R.L[2], e);
+          efw = e;
+        }
+        if (C.poiseuille && t != 0) {
+          const double m = C.mass[t];
+          Fx += m * C.const_force[0];
+          Fy += m * C.const_force[1];
+          Fz += m * C.const_force[2];
+        }
+      }
+      const double im = C.inv_mass[t];
+      ax = Fx * im; ay = Fy * im; az = Fz * im;
+      vx = vx + C.half_dt * ax;
+      vy = vy + C.half_dt * ay;
+      vz = vz + C.half_dt * az;
+      if (info_head(w)) {
+        vx = vy = vz = 0.;
+        ax = ay = az = 0.;
+        if (MODE == 1) { s.fx[i] = 0.; s.fy[i] = 0.; s.fz[i] = 0.; }
+      }
+      if (EFLAG) ke = 0.5 * C.mass[t] * (vx * vx + vy * vy + vz * vz);
+      if (MODE == 1) {
+        s.ax[i] = ax; s.ay[i] = ay; s.az[i] = az;
+        s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
+      }
+    } else {
+      ax = s.ax[i]; ay = s.ay[i]; az = s.az[i];
+    }
+    if (MODE == 0 || MODE == 2) {
+      x = x + C.dt * vx + C.half_dt2 * ax;
+      y = y + C.dt * vy + C.half_dt2 * ay;
+      z = z + C.dt * vz + C.half_dt2 * az;
+      if (x > R.L[0]) x -= R.L[0]; else if (x < 0.) x += R.L[0];
+      if (y > R.L[1]) y -= R.L[1]; else if (y < 0.) y += R.L[1];
+      vx = vx + C.half_dt * ax;
+      vy = vy + C.half_dt * ay;
+      vz = vz + C.half_dt * az;
+      s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
+      s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
+      int4 q;
+      store_views(s, i, R, x, y, z, vx, vy, vz, w, s.tag[i], q);
+      const int4 q0 = s.ref[i];
+      const float dx = (float)fx_diff(q.x, q0.x) * R.ufx_f[0];
+      const float dy = (float)fx_diff(q.y, q0.y) * R.ufx_f[1];
+      const float dz = (float)fx_diff(q.z, q0.z) * R.ufx_f[2];
+      if (dx * dx + dy * dy + dz * dz > (float)C.skin_half2) *s.rebuild_flag = 1;
+      if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(s.status, ST_NAN);
+    }
+  }
+  if (MODE >= 1 && i == 0) *s.steps_done += 1;
+  if (EFLAG && MODE >= 1) {
+    add_obs(acc.col(O_TFLUID), rep, ke, mob, acc.nrep);
+    if (ADDEXT && C.wall == 2) add_obs(acc.col(O_VFW), rep, efw, mob, acc.nrep);
+  }
+}
+
+template <int MODE>
+static void launch_mode(const DevState& s, const SimConst& C, cudaStream_t st, bool add_ext, bool eflag, Acc acc) {
+  const int B = 256, g = (s.N + B - 1) / B;
+  if (add_ext) {
+    if (eflag) k_integrate<MODE, true, true><<<g, B, 0, st>>>(s, C, acc);
+    else k_integrate<MODE, true, false><<<g, B, 0, st>>>(s, C, acc);
+  } else {
+    if (eflag) k_integrate<MODE, false, true><<<g, B, 0, st>>>(s, C, acc);
+    else k_integrate<MODE, false, false><<<g, B, 0, st>>>(s, C, acc);
+  }
+}
+
+void launch_integrate(const DevState& s, const SimConst& C, cudaStream_t st, int mode, bool add_ext, bool eflag,
+                      Acc acc) {
+  if (mode == 0) launch_mode<0>(s, C, st, false, false, acc);
+  else if (mode == 1) launch_mode<1>(s, C, st, add_ext, eflag, acc);
+  else launch_mode<2>(s, C, st, add_ext, eflag, acc);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Profiles: histo(2) + velocity_prof(2) (functions.f90:157-214, 319-365).  Each block takes a
+// contiguous run of slots, accumulates [bin][species][count, sum v, sum v^2] in shared memory
+// and flushes to the replica's global FP64 profile whenever the replica changes.
+// prof layout per replica: [hist][3 species][7] (count, vx, vy, vz, vx^2, vy^2, vz^2).
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_profiles(DevState s, SimConst C, double* __restrict__ prof, int H,
+                                                  int chunk) {
+  extern __shared__ double sh[];
+  const int n_sh = H * 3 * 7;
+  const int b0 = blockIdx.x * chunk, b1 = min(s.N, b0 + chunk);
+  if (b0 >= s.N) return;
+  for (int k = threadIdx.x; k < n_sh; k += blockDim.x) sh[k] = 0.;
+  __syncthreads();
+  int cur = info_rep(s.info[b0]);
+  int pos = b0;
+  while (pos < b1) {
+    // [pos, seg_end): slots of replica `cur` inside this block's chunk
+    int seg_end = b1;
+    if (info_rep(s.info[b1 - 1]) != cur) {
+      int lo = pos, hi = b1 - 1;  // last slot with replica == cur
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (info_rep(s.info[mid]) == cur) lo = mid; else hi = mid - 1;
+      }
+      seg_end = lo + 1;
+    }
+    const RepDesc& R = s.reps[cur];
+    for (int i = pos + threadIdx.x; i < seg_end; i += blockDim.x) {
+      const int w = s.info[i];
+      const int sp = info_species(w);
+      if (!info_mobile(w) || sp == 3) continue;
+      int zi = (int)(s.rz[i] * R.hist_inv_dz) + 1;
+      zi = min(max(zi, 1), H) - 1;
+      double* h = sh + (zi * 3 + sp) * 7;
+      const double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+      atomicAdd(h + 0, 1.);
+      atomicAdd(h + 1, vx);
+      atomicAdd(h + 2, vy);
+      atomicAdd(h + 3, vz);
+      atomicAdd(h + 4, vx * vx);
+      atomicAdd(h + 5, vy * vy);
+      atomicAdd(h + 6, vz * vz);
+    }
+    __syncthreads();
+    double* g = prof + (size_t)cur * n_sh;
+    for (int k = threadIdx.x; k < n_sh; k += blockDim.x) {
+      double v = sh[k];
+      if (v != 0.) atomicAdd(g + k, v);
+      sh[k] = 0.;
+    }
+    __syncthreads();
+    pos = seg_end;
+    if (pos < b1) cur = info_rep(s.info[pos]);
+  }
+}
+
+void launch_profiles(const DevState& s, const SimConst& C, cudaStream_t st, double* prof, int H) {
+  const int chunk = 16384;
+  const int g = (s.N + chunk - 1) / chunk;
+  const size_t shm = sizeof(double) * H * 3 * 7;
+  static size_t shm_set = 48 * 1024;
+  if (shm > shm_set) {  // above 48 KB dynamic shared memory needs an explicit opt-in
+    cudaFuncSetAttribute(k_profiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    shm_set = shm;
+  }
+  k_profiles<<<g, 512, shm, st>>>(s, C, prof, H, chunk);
+}
+
+// energy record: out[k*nrep + r] = acc, acc = 0
+__global__ void k_record(Acc acc, double* out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = NOBS * acc.nrep;
+  if (k >= n) return;
+  out[k] = acc.a[k];
+  acc.a[k] = 0.;
+}
+
+void launch_record(Acc acc, double* out, cudaStream_t st) {
+  int n = NOBS * acc.nrep;
+  k_record<<<(n + 255) / 256, 256, 0, st>>>(acc, out);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host layout <-> slot order
+// ---------------------------------------------------------------------------------------------
+__global__ void k_scatter(DevState s, const double* __restrict__ r, const double* __restrict__ v,
+                          const double* __restrict__ a) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.N) return;
+  int i = s.slot_of_tag[t];
+  if (r) { s.rx[i] = r[3 * (size_t)t]; s.ry[i] = r[3 * (size_t)t + 1]; s.rz[i] = r[3 * (size_t)t + 2]; }
+  if (v) { s.vx[i] = v[3 * (size_t)t]; s.vy[i] = v[3 * (size_t)t + 1]; s.vz[i] = v[3 * (size_t)t + 2]; }
+  if (a) { s.ax[i] = a[3 * (size_t)t]; s.ay[i] = a[3 * (size_t)t + 1]; s.az[i] = a[3 * (size_t)t + 2]; }
+}
+
+void launch_scatter_state(const DevState& s, cudaStream_t st, const double* r, const double* v, const double* a) {
+  k_scatter<<<(s.N + 255) / 256, 256, 0, st>>>(s, r, v, a);
+}
+
+__global__ void k_gather(DevState s, double* __restrict__ r, double* __restrict__ v, double* __restrict__ a,
+                         double* __restrict__ f) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= s.N) return;
+  int i = s.slot_of_tag[t];
+  size_t o = 3 * (size_t)t;
+  if (r) { r[o] = s.rx[i]; r[o + 1] = s.ry[i]; r[o + 2] = s.rz[i]; }
+  if (v) { v[o] = s.vx[i]; v[o + 1] = s.vy[i]; v[o + 2] = s.vz[i]; }
+  if (a) { a[o] = s.ax[i]; a[o + 1] = s.ay[i]; a[o + 2] = s.az[i]; }
+  if (f) { f[o] = s.fx[i]; f[o + 1] = s.fy[i]; f[o + 2] = s.fz[i]; }
+}
+
+void launch_gather_state(const DevState& s, cudaStream_t st, double* r, double* v, double* a, double* f) {
+  k_gather<<<(s.N + 255) / 256, 256, 0, st>>>(s, r, v, a, f);
+}
+
+__global__ void k_init_views(DevState s) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  int w = s.info[i];
+  const RepDesc& R = s.reps[info_rep(w)];
+  int4 q;
+  store_views(s, i, R, s.rx[i], s.ry[i], s.rz[i], s.vx[i], s.vy[i], s.vz[i], w, s.tag[i], q);
+  q.w = 0;
+  s.ref[i] = q;
+}
+
+void launch_init_views(const DevState& s, cudaStream_t st) {
+  k_init_views<<<(s.N + 255) / 256, 256, 0, st>>>(s);
+}
+
+}  // namespace mfa

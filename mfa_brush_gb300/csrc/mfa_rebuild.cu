@@ -1,0 +1,372 @@
+// mfa_rebuild.cu -- cell sort and Verlet-list rebuild on the device.
+//
+// Replaces the reference's neighbour bookkeeping: the linked cells of cell_list.f90:56-268
+// (BIN_TYPE 2, rebuilt incrementally every step) and the skin-based Verlet lists of
+// binning.f90 / check_skin.f90 (BIN_TYPE 0, rebuilt when a particle moved > skin/2).  Here the
+// list is rebuilt when the position kernel has raised `rebuild_flag` (displacement > skin/2):
+//   1. bin:      cell of every particle on the replica's list grid (cell edge >= r_cut_max+skin),
+//                per-cell counts with one atomic per particle;
+//   2. scan:     exclusive prefix sum of the counts (three kernels);
+//   3. place:    particle -> (cell start + atomic rank);
+//   4. order:    each cell's segment sorted by tag (cells hold a handful of particles), so the
+//                final order (replica, cell, tag) and every later FP sum order are deterministic;
+//   5. permute:  FP64 state gathered into the new order, views and rebuild references rewritten;
+//   6. list:     full neighbour list over the 27 surrounding cells (x,y periodic, z bounded).
+// Every kernel reads the flag first and exits when it is clear, so the sequence can sit inside a
+// captured CUDA graph and cost a few microseconds on steps that need no rebuild.
+#include "mfa_state.cuh"
+
+namespace mfa {
+
+__device__ __forceinline__ bool skip(const int* flag, bool force) { return !force && *flag == 0; }
+
+__device__ __forceinline__ void cell_coords(const RepDesc& R, double x, double y, double z, int& ix, int& iy,
+                                            int& iz) {
+  ix = (int)(x * R.inv_lc[0]);
+  iy = (int)(y * R.inv_lc[1]);
+  iz = (int)(z * R.inv_lc[2]);
+  ix = min(max(ix, 0), R.nc[0] - 1);
+  iy = min(max(iy, 0), R.nc[1] - 1);
+  iz = min(max(iz, 0), R.nc[2] - 1);
+}
+
+__global__ void k_zero_counts(int n, int* __restrict__ count, const int* flag, bool force) {
+  if (skip(flag, force)) return;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) count[c] = 0;
+}
+
+__global__ void k_bin(DevState s, bool force) {
+  if (skip(s.rebuild_flag, force)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  int w = s.info[i];
+  const RepDesc& R = s.reps[info_rep(w)];
+  double x = s.rx[i], y = s.ry[i], z = s.rz[i];
+  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+    atomicOr(s.status, ST_NAN);
+    x = y = z = 0.;
+  }
+  double lz = 1. / R.inv_lc[2];
+  if (z < -lz || z > R.L[2] + lz) atomicOr(s.status, ST_OUT_OF_BOX);
+  int ix, iy, iz;
+  cell_coords(R, x, y, z, ix, iy, iz);
+  int c = R.cell_off + (iz * R.nc[1] + iy) * R.nc[0] + ix;
+  s.cell_of[i] = c;
+  s.rank[i] = atomicAdd(&s.cell_count[c], 1);
+}
+
+// exclusive scan, 1024 elements per block
+__global__ void __launch_bounds__(1024) k_scan_local(int n, const int* __restrict__ in, int* __restrict__ out,
+                                                     int* __restrict__ blk, const int* flag, bool force) {
+  if (skip(flag, force)) return;
+  __shared__ int warp_tot[32];
+  int i = blockIdx.x * 1024 + threadIdx.x;
+  int v = (i < n) ? in[i] : 0;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = warp_tot[lane];
+    int u = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, u, o);
+      if (lane >= o) u += y;
+    }
+    warp_tot[lane] = u - t;  // exclusive warp offsets
+    if (lane == 31) blk[blockIdx.x] = u;
+  }
+  __syncthreads();
+  if (i < n) out[i] = x - v + warp_tot[wid];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(int nb, int* __restrict__ blk, const int* flag, bool force) {
+  if (skip(flag, force)) return;
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int base = 0; base < nb; base += 1024) {
+    int i = base + threadIdx.x;
+    int v = (i < nb) ? blk[i] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int t = warp_tot[lane];
+      int u = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, u, o);
+        if (lane >= o) u += y;
+      }
+      warp_tot[lane] = u - t;
+    }
+    __syncthreads();
+    int excl = x - v + warp_tot[wid] + carry;
+    __syncthreads();
+    if (i < nb) blk[i] = excl;
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+}
+
+__global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__ blk, const int* flag, bool force) {
+  if (skip(flag, force)) return;
+  int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += blk[blockIdx.x];
+}
+
+__global__ void k_place(DevState s, bool force) {
+  if (skip(s.rebuild_flag, force)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  s.perm[s.cell_start[s.cell_of[i]] + s.rank[i]] = i;
+}
+
+__global__ void k_sort_cells(DevState s, bool force) {
+  if (skip(s.rebuild_flag, force)) return;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= s.ncell_tot) return;
+  int b = s.cell_start[c], n = s.cell_count[c];
+  for (int k = 1; k < n; ++k) {  // insertion sort by tag
+    int p = s.perm[b + k];
+    int t = s.tag[p];
+    int m = k - 1;
+    while (m >= 0 && s.tag[s.perm[b + m]] > t) {
+      s.perm[b + m + 1] = s.perm[b + m];
+      --m;
+    }
+    s.perm[b + m + 1] = p;
+  }
+}
+
+__global__ void k_permute(DevState s, bool force) {
+  if (skip(s.rebuild_flag, force)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  int o = s.perm[i];
+  s.tmp[0][i] = s.rx[o];
+  s.tmp[1][i] = s.ry[o];
+  s.tmp[2][i] = s.rz[o];
+  s.tmp[3][i] = s.vx[o];
+  s.tmp[4][i] = s.vy[o];
+  s.tmp[5][i] = s.vz[o];
+  s.tmp[6][i] = s.ax[o];
+  s.tmp[7][i] = s.ay[o];
+  s.tmp[8][i] = s.az[o];
+  s.tmp_tag[i] = s.tag[o];
+  s.tmp_info[i] = s.info[o];
+}
+
+__device__ __forceinline__ void write_views(const DevState& s, int i, const RepDesc& R, double x, double y, double z,
+                                            double vx, double vy, double vz, int w, int t) {
+  int4 q;
+  q.x = to_fx_periodic(x, R.sfx[0]);
+  q.y = to_fx_periodic(y, R.sfx[1]);
+  q.z = to_fx_z(z, R.sfx[2]);
+  q.w = w;
+  if (s.mixed) {
+    s.pfx[i] = q;
+    s.vf[i] = make_float4((float)vx, (float)vy, (float)vz, __int_as_float(t));
+  } else {
+    s.pd[i] = mk_dbl4(x, y, z, __longlong_as_double((long long)w));
+    s.vd[i] = mk_dbl4(vx, vy, vz, __longlong_as_double((long long)t));
+  }
+}
+
+__global__ void k_copyback(DevState s, bool force) {
+  if (skip(s.rebuild_flag, force)) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  double x = s.tmp[0][i], y = s.tmp[1][i], z = s.tmp[2][i];
+  double vx = s.tmp[3][i], vy = s.tmp[4][i], vz = s.tmp[5][i];
+  s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
+  s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
+  s.ax[i] = s.tmp[6][i]; s.ay[i] = s.tmp[7][i]; s.az[i] = s.tmp[8][i];
+  int t = s.tmp_tag[i], w = s.tmp_info[i];
+  s.tag[i] = t;
+  s.info[i] = w;
+  s.slot_of_tag[t] = i;
+  const RepDesc& R = s.reps[info_rep(w)];
+  write_views(s, i, R, x, y, z, vx, vy, vz, w, t);
+  int4 q;
+  q.x = to_fx_periodic(x, R.sfx[0]);
+  q.y = to_fx_periodic(y, R.sfx[1]);
+  q.z = to_fx_z(z, R.sfx[2]);
+  q.w = 0;
+  s.ref[i] = q;
+}
+
+// Full Verlet list: every mobile particle lists all j (mobile or wall) with r^2 < (rc_ij+skin)^2.
+template <bool MIXED>
+__global__ void __launch_bounds__(128) k_nlist(DevState s, bool force) {
+  if (skip(s.rebuild_flag, force)) return;
+  __shared__ double rl2[NPAIR];
+  for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) rl2[k] = s.tabd[k].rlist2;
+  __syncthreads();
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  int w = s.info[i];
+  if (!info_mobile(w)) {
+    s.nn[i] = 0;
+    return;
+  }
+  const RepDesc& R = s.reps[info_rep(w)];
+  int ti = info_type(w);
+  double x = s.rx[i], y = s.ry[i], z = s.rz[i];
+  int ix, iy, iz;
+  cell_coords(R, x, y, z, ix, iy, iz);
+  int4 qi = s.pfx ? s.pfx[i] : make_int4(0, 0, 0, 0);
+  float ux = R.ufx_f[0], uy = R.ufx_f[1], uz = R.ufx_f[2];
+  int cnt = 0;
+  const int cap = s.nbr_cap;
+  for (int dz = -1; dz <= 1; ++dz) {
+    int cz = iz + dz;
+    if (cz < 0 || cz >= R.nc[2]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int cy = iy + dy;
+      cy += (cy < 0) ? R.nc[1] : 0;
+      cy -= (cy >= R.nc[1]) ? R.nc[1] : 0;
+      for (int dx = -1; dx <= 1; ++dx) {
+        int cx = ix + dx;
+        cx += (cx < 0) ? R.nc[0] : 0;
+        cx -= (cx >= R.nc[0]) ? R.nc[0] : 0;
+        int c = R.cell_off + (cz * R.nc[1] + cy) * R.nc[0] + cx;
+        int b = s.cell_start[c], e = b + s.cell_count[c];
+        for (int j = b; j < e; ++j) {
+          if (j == i) continue;
+          int wj;
+          double r2;
+          if (MIXED) {
+            int4 qj = s.pfx[j];
+            wj = qj.w;
+            float ddx = (float)fx_diff(qi.x, qj.x) * ux;
+            float ddy = (float)fx_diff(qi.y, qj.y) * uy;
+            float ddz = (float)fx_diff(qi.z, qj.z) * uz;
+            r2 = (double)(ddx * ddx + ddy * ddy + ddz * ddz);
+          } else {
+            wj = s.info[j];
+            double ddx = mic_ref(x - s.rx[j], R.L[0], R.invL[0]);
+            double ddy = mic_ref(y - s.ry[j], R.L[1], R.invL[1]);
+            double ddz = z - s.rz[j];
+            r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+          }
+          if (r2 < rl2[ti * MAXT + info_type(wj)]) {
+            if (cnt < cap) s.nbr[(size_t)cnt * s.Np + i] = j;
+            ++cnt;
+          }
+        }
+      }
+    }
+  }
+  if (cnt > cap) {
+    atomicOr(s.status, ST_NLIST_OVERFLOW);
+    cnt = cap;
+  }
+  s.nn[i] = cnt;
+}
+
+__global__ void k_clear_flag(int* flag) { *flag = 0; }
+
+void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
+  const int B = 256;
+  int gN = (s.N + B - 1) / B;
+  int gC = (s.ncell_tot + B - 1) / B;
+  int nb = (s.ncell_tot + 1023) / 1024;
+  k_zero_counts<<<min(gC, 4096), B, 0, st>>>(s.ncell_tot, s.cell_count, s.rebuild_flag, force);
+  k_bin<<<gN, B, 0, st>>>(s, force);
+  k_scan_local<<<nb, 1024, 0, st>>>(s.ncell_tot, s.cell_count, s.cell_start, s.scan_blk, s.rebuild_flag, force);
+  k_scan_blocks<<<1, 1024, 0, st>>>(nb, s.scan_blk, s.rebuild_flag, force);
+  k_scan_add<<<nb, 1024, 0, st>>>(s.ncell_tot, s.cell_start, s.scan_blk, s.rebuild_flag, force);
+  k_place<<<gN, B, 0, st>>>(s, force);
+  k_sort_cells<<<gC, B, 0, st>>>(s, force);
+  k_permute<<<gN, B, 0, st>>>(s, force);
+  k_copyback<<<gN, B, 0, st>>>(s, force);
+  if (s.mixed)
+    k_nlist<true><<<(s.N + 127) / 128, 128, 0, st>>>(s, force);
+  else
+    k_nlist<false><<<(s.N + 127) / 128, 128, 0, st>>>(s, force);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Parity exports with the reference's own grid (cell_list.f90:129-213, 285-433)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_ref_cells(DevState s, int rep, double il0, double il1, double il2, int n0, int n1, int n2,
+                            int* __restrict__ cell_of_tag, int* __restrict__ counts) {
+  const RepDesc& R = s.reps[rep];
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= R.n_mon_tot) return;
+  int i = s.slot_of_tag[R.p0 + t];
+  double r[3] = {s.rx[i], s.ry[i], s.rz[i]};
+  double il[3] = {il0, il1, il2};
+  int nc[3] = {n0, n1, n2};
+  int pc = 1, pf = 1;
+  for (int d = 0; d < 3; ++d) {
+    int c = (int)(r[d] * il[d]);
+    c = min(max(c, 0), nc[d] - 1);
+    pc += pf * c;
+    pf *= nc[d];
+  }
+  cell_of_tag[t] = pc;
+  atomicAdd(&counts[pc], 1);
+}
+
+void launch_ref_cells(const DevState& s, cudaStream_t st, int rep, const double* il, const int* nc, int* cell_of_tag,
+                      int* counts) {
+  int n = s.N;  // upper bound; the kernel checks the replica's own count
+  k_ref_cells<<<(n + 255) / 256, 256, 0, st>>>(s, rep, il[0], il[1], il[2], nc[0], nc[1], nc[2], cell_of_tag, counts);
+}
+
+__global__ void k_cell_neigh(int n0, int n1, int n2, int n_nei, int* __restrict__ out) {
+  int in_cell = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int nct = n0 * n1 * n2;
+  if (in_cell > nct) return;
+  int z_cell = (in_cell - 1) / (n0 * n1) + 1;
+  int y_cell = (in_cell - n0 * n1 * (z_cell - 1) - 1) / n0 + 1;
+  int x_cell = in_cell - n0 * n1 * (z_cell - 1) - n0 * (y_cell - 1);
+  int* o = out + (size_t)(in_cell - 1) * n_nei;
+  int il = 0;
+  int lo = (n_nei == 13) ? 1 : 0, hi = (n_nei == 13) ? 3 : 4, ilo = 2, ihi = (n_nei == 13) ? 3 : 4;
+  for (int i = ilo; i <= ihi; ++i)
+    for (int j = lo; j <= hi; ++j) {
+      if (i == 2 && j <= 1) continue;
+      for (int k = lo; k <= hi; ++k) {
+        if (i == 2 && j == 2 && k >= 3) continue;
+        int jc = in_cell + i - 2 + (j - 2) * n0 + (k - 2) * n1 * n0;
+        if (jc == in_cell) continue;
+        if (n_nei == 13) {
+          if (x_cell == 1 && i == 1) jc += n0;
+          if (x_cell == n0 && i == 3) jc -= n0;
+          if (y_cell == 1 && j == 1) jc += n0 * n1;
+          if (y_cell == n1 && j == 3) jc -= n0 * n1;
+        } else {
+          if (x_cell + i - 2 > n0) jc -= n0;
+          if (y_cell + j - 2 < 1) jc += n0 * n1;
+          if (y_cell + j - 2 > n1) jc -= n0 * n1;
+        }
+        if (z_cell + k - 2 < 1) jc = 0;
+        if (z_cell + k - 2 > n2) jc = 0;
+        o[il++] = jc;
+      }
+    }
+}
+
+void launch_cell_neigh(const int* nc, int n_nei, int* out, cudaStream_t st) {
+  int nct = nc[0] * nc[1] * nc[2];
+  k_cell_neigh<<<(nct + 127) / 128, 128, 0, st>>>(nc[0], nc[1], nc[2], n_nei, out);
+}
+
+}  // namespace mfa

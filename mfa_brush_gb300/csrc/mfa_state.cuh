@@ -1,0 +1,120 @@
+// mfa_state.cuh -- device state of one context and the kernel launchers (host-callable).
+#pragma once
+#include "mfa_dev.cuh"
+
+namespace mfa {
+
+// All device pointers of a context; passed by value to kernels.
+struct DevState {
+  int N;       // particles (all replicas)
+  int Np;      // padded stride of the neighbour list (multiple of 32)
+  int nrep;
+  int mixed;   // MFA_PREC_MIXED
+  // master state, slot order, FP64
+  double *rx, *ry, *rz, *vx, *vy, *vz, *ax, *ay, *az, *fx, *fy, *fz;
+  int *tag, *info;
+  // permutation scratch
+  double* tmp[9];
+  int *tmp_tag, *tmp_info;
+  int* slot_of_tag;
+  // pair-kernel views
+  int4* pfx;
+  float4* vf;
+  dbl4* pd;
+  dbl4* vd;
+  int4* ref;   // fixed-point position at the last rebuild
+  // neighbour list
+  int *nn, *nbr;
+  int nbr_cap;
+  // cells
+  int *cell_of, *rank, *perm, *cell_count, *cell_start, *scan_blk;
+  int ncell_tot;
+  // control words
+  int* rebuild_flag;
+  unsigned* status;
+  long long* steps_done;
+  // tables
+  const RepDesc* reps;
+  const PairEntry<float>* tabf;
+  const PairEntry<double>* tabd;
+};
+
+// energy accumulators: slot-major [NOBS][nrep]
+struct Acc {
+  double* a;
+  int nrep;
+  __host__ __device__ double* col(int slot) const { return a + (size_t)slot * nrep; }
+};
+
+// ---- rebuild (cell sort + neighbour list); `force` runs it even when the flag is clear -------
+void launch_rebuild(const DevState& s, cudaStream_t st, bool force);
+// ---- forces ------------------------------------------------------------------------------------
+// pair forces (fluid_fluid); accumulate = add into f, else overwrite; eflag = energies into acc
+void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag,
+                 Acc acc, int block);
+// bonded terms: mask bit 1 FENE, 2 brush bending, 4 melt bending, 8 orientation
+void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc);
+// implicit 9-3 walls (fluid_wall 2) and constant body force (constant_force 1)
+void launch_wall(const DevState& s, const SimConst& C, cudaStream_t st, bool eflag, Acc acc);
+void launch_const_force(const DevState& s, const SimConst& C, cudaStream_t st);
+// ---- integration -------------------------------------------------------------------------------
+// mode 0: verlet_positions; 1: verlet_velocities; 2: velocities(n) + positions(n+1) fused.
+// add_ext: add the 9-3 wall and constant body forces inside the kernel (fused path).
+void launch_integrate(const DevState& s, const SimConst& C, cudaStream_t st, int mode, bool add_ext,
+                      bool eflag, Acc acc);
+void launch_profiles(const DevState& s, const SimConst& C, cudaStream_t st, double* prof, int hist);
+void launch_record(Acc acc, double* out, cudaStream_t st);
+// ---- host <-> device layout ----------------------------------------------------------------------
+// canonical AoS (3*tag+d) <-> slot order
+void launch_scatter_state(const DevState& s, cudaStream_t st, const double* r, const double* v,
+                          const double* a);
+void launch_gather_state(const DevState& s, cudaStream_t st, double* r, double* v, double* a, double* f);
+void launch_init_views(const DevState& s, cudaStream_t st);
+// ---- parity exports ----------------------------------------------------------------------------
+void launch_ref_cells(const DevState& s, cudaStream_t st, int rep, const double* inv_l, const int* nc,
+                      int* cell_of_tag, int* counts);
+void launch_cell_neigh(const int* nc, int n_nei, int* out, cudaStream_t st);
+void launch_pair_list(const DevState& s, const SimConst& C, cudaStream_t st, int rep, int* pairs,
+                      long long cap, unsigned long long* count);
+// ---- k-space Ewald (ewald_k.f90, dipolar_correction.f90) ------------------------------------
+// exp(i k.r) = X(nx) Y(ny) Z(nz) per charged particle: the tables hold X for nx = 0..nxm,
+// Y for ny = 0..nym and Z for nz = 0..nzm (negative n by conjugation), so a (k, particle) term
+// costs two complex products instead of a sin/cos of a large argument.
+struct KSpace {
+  int nk, nq, nxm, nym, nzm, ncol;
+  int4* kn;             // [nk] (nx, ny, nz, 0) in the reference's enumeration order
+  double* kvec;         // [3*nk]
+  double* kfac;         // [nk] exp(-k^2/(4 alpha_c)) / k^2
+  double* rho;          // [2*nk] Re, Im of sum_q q exp(i k.r)
+  float2* tabf;         // [nq][ncol] (mixed)
+  double2* tabd;        // [nq][ncol] (fp64)
+  int* qtag;            // [nq] tags of the charged particles
+  double cx, cy, cz;    // dk/(2 pi) per axis
+  double inv_V, lz_half;
+  double* mz;           // [1] dipole moment M_z
+  int rep;
+};
+void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc);
+void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc);
+
+// implicit 9-3 walls (fluid_wall.f90:93-121): returns F_z, e = energy of both walls
+__device__ __forceinline__ double wall93(const SimConst& C, int t, double z, double D, double& e) {
+  const double sw = C.sigma_wall[t], awt = C.a_wall[t], aw = fabs(awt);
+  const double sw3 = sw * sw * sw, sw9 = sw3 * sw3 * sw3;
+  double f = 0.;
+  double iz = 1. / z;
+  double iz2 = iz * iz, iz4 = iz2 * iz2, iz8 = iz4 * iz4, iz10 = iz8 * iz2;
+  double rd = sw * iz, rd3 = rd * rd * rd, rd9 = rd3 * rd3 * rd3;
+  e = aw * rd9 - C.a_w * rd3;
+  f += 9. * aw * sw9 * iz10;
+  f -= 3. * awt * sw3 * iz4;
+  iz = 1. / (D - z);
+  iz2 = iz * iz; iz4 = iz2 * iz2; iz8 = iz4 * iz4; iz10 = iz8 * iz2;
+  rd = sw * iz; rd3 = rd * rd * rd; rd9 = rd3 * rd3 * rd3;
+  e += aw * rd9 - C.a_w * rd3;
+  f -= 9. * aw * sw9 * iz10;
+  f += 3. * awt * sw3 * iz4;
+  return f;
+}
+
+}  // namespace mfa

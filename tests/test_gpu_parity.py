@@ -1,0 +1,211 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same inputs.
+
+Tolerances: FP64 path -- forces 1e-9 relative to max(|F_i|, 1e-3 F_rms), energies 1e-10;
+mixed path -- forces 2e-5 on the same measure, energies 1e-5 relative.  Cell assignment,
+half-shell tables and interacting-pair sets are compared exactly."""
+import numpy as np
+import pytest
+
+from conftest import rel_force_err
+from mfa_brush_gb300 import configs, md
+
+pytestmark = pytest.mark.gpu
+
+TOL_F = {"fp64": 1e-9, "mixed": 2e-5}
+TOL_E = {"fp64": 1e-10, "mixed": 1e-5}
+
+
+def gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, precision):
+    g = md.MdSystem(p, s, a_type, r0, v, a, precision=precision)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v, a)
+    return g, o
+
+
+def rel(x, y):
+    return abs(x - y) / max(abs(y), 1e-300)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_try_fluid_fluid(gpu, try_deck, oracle_mod, precision):
+    """LJ + DPD (own cut-off, Philox noise) on try/conf_old."""
+    inp, p, s, a_type, r0, v, a = try_deck
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, precision)
+    g.zero_force()
+    vff, _ = g.fluid_fluid()
+    f = g.state()[3]
+    o.zero_force()
+    o.fluid_fluid()
+    fo = o.state()[3]
+    assert rel(vff[0], o.energies()["v_fluid_fluid"]) < TOL_E[precision]
+    assert rel(vff[0], -1131.60193205932) < max(TOL_E[precision], 1e-12)
+    assert rel_force_err(f, fo) < TOL_F[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("routine,key", [("intra_molec", "v_intra_molec"), ("bending", "v_bend"),
+                                         ("orientation", "v_or"), ("fluid_wall", "v_fluid_wall")])
+def test_try_single_routines(gpu, try_deck, oracle_mod, precision, routine, key):
+    inp, p, s, a_type, r0, v, a = try_deck
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, precision)
+    g.zero_force()
+    e = getattr(g, routine)()
+    o.zero_force()
+    getattr(o, routine)()
+    tol_e = 1e-10 if (routine == "fluid_wall" or precision == "fp64") else TOL_E[precision]
+    assert rel(e[0], o.energies()[key]) < tol_e
+    tol_f = 1e-9 if (routine == "fluid_wall" or precision == "fp64") else TOL_F[precision]
+    assert rel_force_err(g.state()[3], o.state()[3]) < tol_f
+
+
+def test_try_md_steps_fp64(gpu, try_deck, oracle_mod):
+    """Five md_main iterations through the per-routine drop-ins vs the oracle."""
+    inp, p, s, a_type, r0, v, a = try_deck
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, "fp64")
+    for _ in range(5):
+        eg = g.md_step()[0]
+    o.step(5, 1, 0)
+    r, vv, aa, f = g.state()
+    ro, vo, ao, fo = o.state()
+    d = r - ro
+    d[:, :2] -= np.array(list(s.boundary))[:2] * np.round(d[:, :2] / np.array(list(s.boundary))[:2])
+    assert np.abs(d).max() < 1e-9
+    assert np.abs(vv - vo).max() < 1e-7 * max(1.0, np.abs(vo).max())
+    eo = o.energies()
+    for k in ("v_fluid_fluid", "v_intra_molec", "v_bend", "v_or", "v_fluid_wall", "t_fluid"):
+        assert rel(eg[k], eo[k]) < 1e-8, k
+
+
+def test_fused_step_matches_drop_ins(gpu, try_deck):
+    """mfa_step(n) (graph-captured, fused integrator) reproduces n per-routine md_main steps."""
+    inp, p, s, a_type, r0, v, a = try_deck
+    g1 = md.MdSystem(p, s, a_type, r0, v, a, precision="fp64")
+    g2 = md.MdSystem(p, s, a_type, r0, v, a, precision="fp64")
+    for _ in range(7):
+        e1 = g1.md_step()[0]
+    g2.step(7)
+    e2 = g2.energies()[0]
+    s1, s2 = g1.state(), g2.state()
+    assert np.abs(s1[0] - s2[0]).max() < 1e-10
+    assert np.abs(s1[1] - s2[1]).max() < 1e-8
+    for k in ("v_fluid_fluid", "v_intra_molec", "v_bend", "v_or", "v_fluid_wall", "t_fluid", "e_total"):
+        assert rel(e1[k], e2[k]) < 1e-9, k
+    assert g2.step_index() == s.s_time + 7
+
+
+@pytest.mark.parametrize("l_box", [1, 2])
+def test_reference_cell_list_bit_exact(gpu, try_deck, oracle_mod, l_box):
+    """get_cell on the reference's own grid (make_binning with r_cut_max): identical cells."""
+    inp, p, s, a_type, r0, v, a = try_deck
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, "fp64")
+    o.make_cell_list(l_box)
+    cg, ng, ncg = g.cell_list(0, l_box)
+    co, no, nco = o.cell_info()
+    assert list(ncg) == list(nco)
+    assert np.array_equal(cg, co)
+    assert np.array_equal(ng, no)
+
+
+@pytest.mark.parametrize("n_cells,n_nei", [((11, 7, 15), 13), ((13, 8, 17), 13), ((26, 17, 35), 62)])
+def test_half_shell_table_bit_exact(gpu, oracle_mod, n_cells, n_nei):
+    assert np.array_equal(md.cell_neigh_list(n_cells, n_nei), oracle_mod.cell_neigh_list(n_cells, n_nei))
+
+
+def test_interacting_pairs_identical(gpu, try_deck, oracle_mod):
+    inp, p, s, a_type, r0, v, a = try_deck
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, "fp64")
+    pg = g.pair_list(0)
+    po = o.pair_list()
+    sg = set(map(tuple, np.sort(pg, axis=1).tolist()))
+    so = set(map(tuple, po.tolist()))
+    assert len(pg) == len(sg) and sg == so
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_replicas_equal_single(gpu, precision):
+    """A replica inside a batch gets bit-identical forces to the same replica run alone."""
+    p = configs.wca_params(gamma=5.0)
+    reps = [configs.brush_channel(15.0, 12.0, 0.2, 20, seed=11),
+            configs.brush_channel(18.0, 15.0, 0.1, 35, seed=12),
+            configs.brush_channel(16.0, 10.0, 0.05, 50, seed=13)]
+    systems, a_type, r0, v = configs.concat(reps)
+    gb = md.MdSystem(p, systems, a_type, r0, v, precision=precision)
+    gb.step(3)
+    rb, vb, ab, fb = gb.state()
+    off = 0
+    for (s, at, r, vv) in reps:
+        g1 = md.MdSystem(p, s, at, r, vv, precision=precision)
+        g1.step(3)
+        r1, v1, a1, f1 = g1.state()
+        n = s.n_part
+        assert np.array_equal(r1, rb[off:off + n])
+        assert np.array_equal(v1, vb[off:off + n])
+        off += n
+
+
+def test_profiles_match_oracle(gpu, oracle_mod):
+    p = configs.wca_params(gamma=5.0)
+    p.flags.profiles = 1
+    s, a_type, r0, v = configs.small_channel()
+    g = md.MdSystem(p, s, a_type, r0, v, precision="fp64")
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    for _ in range(6):
+        g.md_step(profiles=True)
+    o.step(6, 1, 1)
+    dg, vg, v2g, ng = g.profiles(0)
+    do, vo, v2o, no = o.profiles()
+    assert ng == no == 6
+    assert np.array_equal(dg, do)
+    assert np.abs(vg - vo).max() < 1e-9 and np.abs(v2g - v2o).max() < 1e-9
+
+
+def charged_system(n_kmax=5):
+    inp = configs.wca_inputs(gamma=1.0, thermostat=0)
+    inp.flags.system = 3
+    inp.charge[1] = -1.0  # brush beads
+    inp.charge[2] = 1.0   # solvent
+    inp.alpha_c = 0.81
+    inp.n_kmax = n_kmax
+    inp.rc_coul = 3.0
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(10.0, 10.0, 0.08, 10, rho=0.5, seed=21)
+    return p, s, a_type, r0, v
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ewald_matches_oracle(gpu, oracle_mod, precision):
+    p, s, a_type, r0, v = charged_system()
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, None, precision)
+    o.ewald_init()
+    # real space (inside fluid_fluid)
+    g.zero_force(); _, vc = g.fluid_fluid(); f_real = g.state()[3]
+    o.zero_force(); o.fluid_fluid(); fo_real = o.state()[3]; vco = o.energies()["v_coul"]
+    assert rel(vc[0], vco) < TOL_E[precision]
+    assert rel_force_err(f_real, fo_real) < TOL_F[precision]
+    # k space
+    g.zero_force(); uk = g.ewald_k()[0]; fk = g.state()[3]
+    o.zero_force(); uko = o.ewald_k(); fko = o.state()[3]
+    assert rel(uk, uko) < (1e-10 if precision == "fp64" else 1e-5)
+    assert rel_force_err(fk, fko) < (1e-9 if precision == "fp64" else 1e-4)
+    # slab dipole correction
+    g.zero_force(); ud = g.dipolar_correction()[0]; fd = g.state()[3]
+    o.zero_force(); udo = o.dipolar_correction(); fdo = o.state()[3]
+    assert rel(ud, udo) < 1e-10
+    assert np.abs(fd - fdo).max() < 1e-10 * max(1.0, np.abs(fdo).max())
+
+
+def test_deterministic_and_momentum(gpu):
+    """Two identical runs are bit-identical; pair forces conserve momentum (noise is antisymmetric)."""
+    p = configs.wca_params(gamma=5.0)
+    reps = configs.replicas(6, seed=5)
+    systems, a_type, r0, v = configs.concat(reps)
+    out = []
+    for _ in range(2):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed")
+        g.step(40)
+        out.append(g.state())
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
+    g.zero_force()
+    g.fluid_fluid()
+    f = g.state()[3]
+    assert np.abs(f.sum(0)).max() < 1e-5 * np.abs(f).sum()

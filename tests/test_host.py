@@ -1,0 +1,116 @@
+"""Host-side logic of the product (CPU only, no kernel launches): the C-ABI library loads and
+exports every entry point include/mfa_gpu.h declares, the input parsers read the reference's own
+deck, conf_old/conf_new round-trip, and the synthetic configurations are well formed."""
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "mfa_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mfa_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.mfa_version().decode().startswith("mfa_gb300")
+
+
+def test_abi_struct_sizes_match_header(lib):
+    """ctypes mirrors of the structs must have the C sizes (checked through a round trip)."""
+    import ctypes as C
+    from mfa_brush_gb300 import abi
+    o = abi.Options()
+    lib.mfa_default_options(C.byref(o))
+    assert (o.precision, o.skin, o.energy_every, o.use_graphs) == (abi.PREC_MIXED, 0.3, 10, 1)
+
+
+def test_header_flags(try_dir):
+    from mfa_brush_gb300 import md
+    f = md.flags_from_header(os.path.join(try_dir, "control_simulation.h"))
+    assert (f.system, f.wall, f.solvent, f.thermostat, f.bin_type) == (0, 2, 3, 0, 0)
+    assert (f.bending, f.orientation, f.brush_in_good_sv, f.poiseuille, f.particle_4) == (1, 1, 1, 0, 0)
+    assert f.dpd_cut_off == 2.24 and f.force_switch_on == 1 and f.profiles == 1
+
+
+def test_read_deck(try_deck):
+    inp, p, s, a_type, r0, v, a = try_deck
+    assert (inp.n_mon, inp.n_chain, inp.n_cell_w_x, inp.n_cell_w_y) == (10, 300, 30, 20)
+    assert (inp.n_mon_d, inp.n_chain_d) == (1, 3000)
+    assert inp.delta_sig[0] == 1.0 and (inp.a_w, inp.sigma_w) == (-3.2, 1.0)
+    assert (inp.s_time, inp.n_relax, inp.n_obser, inp.n_safe) == (2, 0, 500000, 1000)
+    assert inp.dt == 2e-4 and inp.temp == 0.8 and inp.z_space_wall == 40.0
+    assert inp.mass_type[3] == 50.0 and inp.epsil[0] == 0.0 and abs(inp.epsil[2] - 0.333) < 1e-15
+    assert (inp.k_bend, inp.alpha_eq, inp.iseed, inp.k_chain, inp.r_chain) == (80.0, 0.0, 311500357, 30.0, 1.5)
+    assert list(inp.f_twall) == [2, 2, 1]
+    assert np.bincount(a_type).tolist() == [0, 300, 2700, 3000]
+    assert r0[0].tolist() == [24.249925, 1.0, 38.8]
+    assert r0[:, 2].min() > 0 and r0[:, 2].max() < 40
+
+
+def test_conf_round_trip(try_deck, tmp_path):
+    from mfa_brush_gb300 import md
+    inp, p, s, a_type, r0, v, a = try_deck
+    path = str(tmp_path / "conf_new")
+    md.write_conf_new(path, inp, a_type, r0, v, a)
+    t2, r2, v2, a2 = md.read_conf_old(path, s.n_part)
+    assert np.array_equal(t2, a_type)
+    # f13.7 / f15.7 formats keep 7 decimals
+    assert np.abs(r2 - r0).max() < 5.1e-8 and np.abs(v2 - v).max() < 5.1e-8 and np.abs(a2 - a).max() < 5.1e-8
+
+
+def test_unsupported_flags_are_rejected(try_deck):
+    import ctypes as C
+    from mfa_brush_gb300 import abi, md
+    inp = try_deck[0]
+    bad = abi.Inputs.from_buffer_copy(inp)
+    bad.flags.symmetry = 1
+    p, s = abi.Params(), abi.System()
+    assert abi.load_library().mfa_derive_params(C.byref(bad), C.byref(p), C.byref(s)) == -9
+
+
+def test_init_without_gpu_fails_loudly(try_deck):
+    """On a machine without a GPU the context refuses to start (no CPU fallback)."""
+    from mfa_brush_gb300 import abi, md
+    if md.device_count() > 0:
+        return
+    inp, p, s, a_type, r0, v, a = try_deck
+    try:
+        md.MdSystem(p, s, a_type, r0, v, a)
+    except abi.MfaError as e:
+        assert e.code == -10
+    else:
+        raise AssertionError("context created without a device")
+
+
+def test_replica_workload_shapes():
+    from mfa_brush_gb300 import configs
+    shapes = configs.draw_replica_shapes(256, 2024)
+    sg, N, D, L = map(np.array, zip(*shapes))
+    assert sg.min() >= 0.05 and sg.max() <= 0.3 and N.min() >= 10 and N.max() <= 100
+    assert D.min() >= 10 and D.max() <= 40 and L.min() >= 15 and L.max() <= 40
+    assert np.all(2 * sg * N <= 0.7 * 0.8 * D)
+
+
+def test_small_channel_is_well_formed():
+    from mfa_brush_gb300 import configs
+    s, a_type, r0, v = configs.small_channel()
+    L = s.boundary[0]
+    assert s.n_part == len(a_type) == len(r0) and s.n_mon_tot == s.n_part
+    assert abs(s.n_part - 0.8 * 20 ** 3) <= 1
+    assert np.all((r0[:, 2] >= configs.Z_LO - 1e-12) & (r0[:, 2] <= s.boundary[2] - configs.Z_LO + 1e-12))
+    assert np.all(a_type[: s.n_mon * s.n_chain : s.n_mon] == 1)
+    nb = s.n_mon * s.n_chain
+    d = r0[1:nb] - r0[: nb - 1]
+    d[:, :2] -= L * np.round(d[:, :2] / L)
+    keep = np.ones(nb - 1, bool)
+    keep[s.n_mon - 1 :: s.n_mon] = False
+    bl = np.linalg.norm(d[keep], axis=1)
+    assert bl.max() < 1.5 and bl.min() > 0.9

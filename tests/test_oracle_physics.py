@@ -1,0 +1,119 @@
+"""Analytic checks of the oracle (CPU): forces are minus the gradient of the energies it reports,
+pair and bonded forces obey Newton's third law, the linked-cell traversal finds the same pairs as
+an O(N^2) search, and the half-shell cell table matches the reference's rules."""
+import numpy as np
+import pytest
+
+from mfa_brush_gb300 import configs
+
+
+def small_system(oracle_mod, thermostat=1, bending=True, seed=3, L=8.0, D=8.0):
+    inp = configs.wca_inputs(bending=bending, k_bend=2.0, thermostat=thermostat)
+    inp.flags.orientation = 1
+    from mfa_brush_gb300 import md
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(L, D, 0.15, 8, rho=0.7, seed=seed)
+    # jitter off the lattice so angles and distances are generic
+    rng = np.random.default_rng(seed)
+    r0 = r0 + rng.normal(0, 0.05, r0.shape)
+    return p, s, a_type, r0, v
+
+
+def total_energy(o, which):
+    o.zero_force()
+    getattr(o, which)()
+    e = o.energies()
+    key = {"fluid_fluid": "v_fluid_fluid", "fluid_wall": "v_fluid_wall", "intra_molec": "v_intra_molec",
+           "bending": "v_bend", "orientation": "v_or"}[which]
+    return e[key], o.state()[3]
+
+
+@pytest.mark.parametrize("which", ["fluid_fluid", "fluid_wall", "intra_molec", "bending", "orientation"])
+def test_force_is_minus_gradient(oracle_mod, which):
+    p, s, a_type, r0, v = small_system(oracle_mod)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    e0, f = total_energy(o, which)
+    rng = np.random.default_rng(1)
+    idx = rng.choice(s.n_mon_tot, 12, replace=False)
+    h = 1e-6
+    for i in idx:
+        for d in range(3):
+            rp = r0.copy(); rp[i, d] += h
+            rm = r0.copy(); rm[i, d] -= h
+            o.set_state(rp); ep, _ = total_energy(o, which)
+            o.set_state(rm); em, _ = total_energy(o, which)
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - f[i, d]) <= 1e-5 * max(1.0, abs(f[i, d])), (which, i, d, fd, f[i, d])
+    o.set_state(r0)
+
+
+@pytest.mark.parametrize("thermostat", [0, 1])
+def test_pair_newton3(oracle_mod, thermostat):
+    p, s, a_type, r0, v = small_system(oracle_mod, thermostat=thermostat)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    o.zero_force()
+    o.fluid_fluid()
+    f = o.state()[3]
+    assert np.abs(f.sum(0)).max() < 1e-9 * np.abs(f).sum()
+
+
+def test_cell_list_finds_all_pairs(oracle_mod):
+    """Every pair inside the cut-off is visited exactly once by the 13-cell traversal."""
+    p, s, a_type, r0, v = small_system(oracle_mod, L=9.0, D=9.0)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    o.zero_force()
+    o.fluid_fluid()
+    e_cell = o.energies()["v_fluid_fluid"]
+    e_n2 = o.check_fluid_fluid()
+    assert abs(e_cell - e_n2) <= 1e-12 * max(1.0, abs(e_n2))
+
+
+@pytest.mark.parametrize("n_cells,n_nei", [((5, 4, 6), 13), ((7, 6, 8), 62)])
+def test_half_shell_table(oracle_mod, n_cells, n_nei):
+    """make_cell_list2: each unordered pair of neighbouring cells appears once (x,y periodic,
+    z bounded with the phantom cell 0)."""
+    t = oracle_mod.cell_neigh_list(n_cells, n_nei)
+    nx, ny, nz = n_cells
+    reach = 1 if n_nei == 13 else 2
+    seen = set()
+    for c in range(1, nx * ny * nz + 1):
+        for j in t[c - 1]:
+            if j == 0:
+                continue
+            key = (min(c, j), max(c, j))
+            assert key not in seen
+            seen.add(key)
+    # expected: all distinct neighbour pairs within `reach` (periodic x,y)
+    def coords(c):
+        c -= 1
+        return c % nx, (c // nx) % ny, c // (nx * ny)
+    exp = set()
+    for c in range(1, nx * ny * nz + 1):
+        x, y, z = coords(c)
+        for dx in range(-reach, reach + 1):
+            for dy in range(-reach, reach + 1):
+                for dz in range(-reach, reach + 1):
+                    if (dx, dy, dz) == (0, 0, 0) or not 0 <= z + dz < nz:
+                        continue
+                    j = 1 + (x + dx) % nx + ((y + dy) % ny) * nx + (z + dz) * nx * ny
+                    exp.add((min(c, j), max(c, j)))
+    assert seen == exp
+
+
+def test_dpd_thermostat_temperature(oracle_mod):
+    """DPD drives a WCA channel to kT (statistical; the reference's own check is fort.60's T)."""
+    from mfa_brush_gb300 import md
+    inp = configs.wca_inputs(gamma=5.0, kT=1.0, dt=0.005)
+    inp.flags.dpd_cut_off = 1.5  # own DPD cut-off (DPD_CUT_OFF): a stronger thermostat than WCA range
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(8.0, 10.0, 0.1, 6, rho=0.6, seed=5)
+    v = v * 0.3  # start cold
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    o.step(1500, 1, 0)
+    ts = []
+    for _ in range(40):
+        o.step(25, 1, 0)
+        ts.append(o.energies()["t_fluid"])
+    n_free = s.n_mon_tot - s.n_chain
+    kT = 2 * np.mean(ts) / (3 * n_free)
+    assert abs(kT - 1.0) < 0.06, kT
