@@ -303,6 +303,8 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
 const char* mfa_kernel_name(int32_t fam);
 /* Number of kernel launches issued by the library since the context was created. */
 int mfa_launch_count(mfa_ctx* ctx, int64_t* n);
+/* Number of cell-sort + neighbour-list rebuilds since the context was created (synchronises). */
+int mfa_rebuild_count(mfa_ctx* ctx, int64_t* n);
 
 #ifdef __cplusplus
 }

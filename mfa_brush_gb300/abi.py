@@ -153,6 +153,7 @@ SIGNATURES = {
     "mfa_kernel_times": (i32, [vp, i32, P(C.c_float), ip]),
     "mfa_kernel_name": (C.c_char_p, [i32]),
     "mfa_launch_count": (i32, [vp, P(i64)]),
+    "mfa_rebuild_count": (i32, [vp, P(i64)]),
 }
 NKFAM = 8
 

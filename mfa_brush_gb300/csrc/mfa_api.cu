@@ -333,6 +333,16 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   const double skin = ctx->opt.skin;
   C.skin_half2 = 0.25 * skin * skin;
   C.hist_dim = p->hist_dim > 0 ? p->hist_dim : 200;
+  C.dt_f = (float)C.dt;
+  C.skin_half2_f = (float)C.skin_half2;
+  C.a_w_f = (float)C.a_w;
+  for (int t = 0; t < MAXT; ++t) {
+    C.mass_f[t] = (float)C.mass[t];
+    C.inv_mass_f[t] = (float)C.inv_mass[t];
+    C.sigma_wall_f[t] = (float)C.sigma_wall[t];
+    C.a_wall_f[t] = (float)C.a_wall[t];
+  }
+  for (int d = 0; d < 3; ++d) C.cforce_f[d] = (float)C.const_force[d];
   if (C.hist_dim > MFA_HIST_DIM_MAX) return fail(ctx, MFA_ERR_CAPACITY, "hist_dim exceeds MFA_HIST_DIM_MAX");
   // ---- pair tables ----------------------------------------------------------------------------
   std::vector<PairEntry<float>> tf(NPAIR);
@@ -1060,6 +1070,14 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
 int mfa_launch_count(mfa_ctx* ctx, int64_t* n) {
   if (!ctx || !n) return MFA_ERR_ARG;
   *n = ctx->launches;
+  return MFA_OK;
+}
+
+int mfa_rebuild_count(mfa_ctx* ctx, int64_t* n) {
+  if (!ctx || !n) return MFA_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->h_rebuilds, ctx->d_rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  *n = *ctx->h_rebuilds;
   return MFA_OK;
 }
 

@@ -71,6 +71,9 @@ struct SimConst {
   double coul_rc2;                // own Coulomb cut-off^2 (0: inside LJ range)
   double skin_half2;              // (skin/2)^2
   int hist_dim;
+  // FP32 copies for the mixed-precision integrator
+  float dt_f, skin_half2_f, a_w_f;
+  float mass_f[MAXT], inv_mass_f[MAXT], sigma_wall_f[MAXT], a_wall_f[MAXT], cforce_f[3];
 };
 
 // Per replica (device array, read through the L1).

@@ -106,9 +106,98 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
   }
 }
 
+// FP32 9-3 walls from the FP32 distances to the bottom (zl) and top (zh) wall; 9|A| s^9 z^-10 =
+// 9|A| (s/z)^9 / z, 3 A s^3 z^-4 = 3 A (s/z)^3 / z.
+__device__ __forceinline__ float wall93f(const SimConst& C, int t, float zl, float zh, float& e) {
+  const float sw = C.sigma_wall_f[t], awt = C.a_wall_f[t], aw = fabsf(awt), a_w = C.a_w_f;
+  float iz = 1.f / zl, rd = sw * iz, rd3 = rd * rd * rd, rd9 = rd3 * rd3 * rd3;
+  e = aw * rd9 - a_w * rd3;
+  float f = (9.f * aw * rd9 - 3.f * awt * rd3) * iz;
+  iz = 1.f / zh; rd = sw * iz; rd3 = rd * rd * rd; rd9 = rd3 * rd3 * rd3;
+  e += aw * rd9 - a_w * rd3;
+  f -= (9.f * aw * rd9 - 3.f * awt * rd3) * iz;
+  return f;
+}
+
+// The fused step of the mixed-precision path: velocities of step n and positions of step n+1 in
+// one pass with the FP64 work cut to the accumulators (GB300 issues FP64 at a small fraction of
+// the FP32 rate).  Forces, the wall term, accelerations and the velocity increment are FP32; the
+// half-kick pair v(n-1/2) -> v(n) -> v(n+1/2) is one FP64 add of dt*a, and the drift is
+// r(n+1) = r(n) + dt v(n+1/2), identical in exact arithmetic to verlet_velocities followed by
+// verlet_positions.  Kinetic energy (energy steps) uses v(n) = v(n+1/2) - dt/2 a.
+template <bool EFLAG>
+__global__ void __launch_bounds__(256) k_fused_mixed(DevState s, SimConst C, Acc acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool inside = i < s.N;
+  const int w = inside ? s.info[i] : 0;
+  const bool mob = inside && info_mobile(w);
+  const int rep = info_rep(w);
+  float ke = 0.f, efw = 0.f;
+  if (mob) {
+    const RepDesc& R = s.reps[rep];
+    const int t = info_type(w);
+    float Fx = (float)s.fx[i], Fy = (float)s.fy[i], Fz = (float)s.fz[i];
+    double x = s.rx[i], y = s.ry[i], z = s.rz[i];
+    if (C.wall == 2) {
+      float e;
+      Fz += wall93f(C, t, (float)z, (float)(R.L[2] - z), e);
+      efw = e;
+    }
+    if (C.poiseuille && t != 0) {
+      Fx += C.mass_f[t] * C.cforce_f[0];
+      Fy += C.mass_f[t] * C.cforce_f[1];
+      Fz += C.mass_f[t] * C.cforce_f[2];
+    }
+    const float sc = C.dt_f * C.inv_mass_f[t];
+    float dvx = Fx * sc, dvy = Fy * sc, dvz = Fz * sc;
+    double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+    if (info_head(w)) {
+      vx = vy = vz = 0.;
+      dvx = dvy = dvz = 0.f;
+    }
+    if (EFLAG) {
+      const float ux = (float)vx + 0.5f * dvx, uy = (float)vy + 0.5f * dvy, uz = (float)vz + 0.5f * dvz;
+      ke = 0.5f * C.mass_f[t] * (ux * ux + uy * uy + uz * uz);
+    }
+    vx += (double)dvx;
+    vy += (double)dvy;
+    vz += (double)dvz;
+    x = fma(C.dt, vx, x);
+    y = fma(C.dt, vy, y);
+    z = fma(C.dt, vz, z);
+    if (x > R.L[0]) x -= R.L[0]; else if (x < 0.) x += R.L[0];
+    if (y > R.L[1]) y -= R.L[1]; else if (y < 0.) y += R.L[1];
+    s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
+    s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
+    int4 q;
+    q.x = to_fx_periodic(x, R.sfx[0]);
+    q.y = to_fx_periodic(y, R.sfx[1]);
+    q.z = to_fx_z(z, R.sfx[2]);
+    q.w = w;
+    s.pfx[i] = q;
+    s.vf[i] = make_float4((float)vx, (float)vy, (float)vz, __int_as_float(s.tag[i]));
+    const int4 q0 = s.ref[i];
+    const float dx = (float)fx_diff(q.x, q0.x) * R.ufx_f[0];
+    const float dy = (float)fx_diff(q.y, q0.y) * R.ufx_f[1];
+    const float dz = (float)fx_diff(q.z, q0.z) * R.ufx_f[2];
+    if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) *s.rebuild_flag = 1;
+    if (!(isfinite(z) && isfinite(x))) atomicOr(s.status, ST_NAN);
+  }
+  if (i == 0) *s.steps_done += 1;
+  if (EFLAG) {
+    add_obs(acc.col(O_TFLUID), rep, (double)ke, mob, acc.nrep);
+    if (C.wall == 2) add_obs(acc.col(O_VFW), rep, (double)efw, mob, acc.nrep);
+  }
+}
+
 template <int MODE>
 static void launch_mode(const DevState& s, const SimConst& C, cudaStream_t st, bool add_ext, bool eflag, Acc acc) {
   const int B = 256, g = (s.N + B - 1) / B;
+  if (MODE == 2 && add_ext && s.mixed) {
+    if (eflag) k_fused_mixed<true><<<g, B, 0, st>>>(s, C, acc);
+    else k_fused_mixed<false><<<g, B, 0, st>>>(s, C, acc);
+    return;
+  }
   if (add_ext) {
     if (eflag) k_integrate<MODE, true, true><<<g, B, 0, st>>>(s, C, acc);
     else k_integrate<MODE, true, false><<<g, B, 0, st>>>(s, C, acc);

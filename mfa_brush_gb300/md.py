@@ -303,6 +303,11 @@ class MdSystem:
         self._ck(self.lib.mfa_kernel_times(self.ctx, nsteps, ms, cnt))
         return {self.lib.mfa_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(abi.NKFAM)}
 
+    def rebuild_count(self):
+        n = abi.i64(0)
+        self._ck(self.lib.mfa_rebuild_count(self.ctx, C.byref(n)))
+        return n.value
+
     def launch_count(self):
         n = abi.i64(0)
         self._ck(self.lib.mfa_launch_count(self.ctx, C.byref(n)))

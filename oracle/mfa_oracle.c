@@ -370,6 +370,10 @@ int orc_cell_neigh_list(const int32_t* n_cells, int32_t n_nei, int32_t* out) {
 int orc_make_cell_list(orc_sys* o, int l_box) {
   o->l_box = l_box;
   double rc = o->p.r_cut_max;
+  /* an own real-space Coulomb cut-off (not expressible in the reference) widens the cells */
+  if ((o->p.flags.system == 2 || o->p.flags.system == 3) && o->p.rc_coul_2 > 0. &&
+      !(o->p.compat & MFA_COMPAT_COUL_IN_LJ) && sqrt(o->p.rc_coul_2) > rc)
+    rc = sqrt(o->p.rc_coul_2);
   for (int d = 0; d < 3; ++d) {
     o->nc[d] = (l_box == 1) ? (int)(o->s.boundary[d] / rc) : (int)(o->s.boundary[d] / (rc / 2.));
     if (o->nc[d] < 1) o->nc[d] = 1;
