@@ -189,6 +189,7 @@ def main():
     barrier()
     clk = ClockSampler(local)
     clk.start()
+    rb0 = g.rebuild_count()
     l0 = g.launch_count()
     g.synchronize()
     g.event_record(0)
@@ -199,6 +200,7 @@ def main():
     g.synchronize()
     clocks = clk.stop()
     launches = g.launch_count() - l0
+    rebuilds = g.rebuild_count() - rb0
     t = ms / 1000.0
     if dist is not None:
         import torch
@@ -227,7 +229,8 @@ def main():
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": 0.3,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
-            "gpu_launches": int(launches),
+            "gpu_launches": int(launches + 10 * rebuilds),
+            "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None, "kernel": "k_pair (mixed)",

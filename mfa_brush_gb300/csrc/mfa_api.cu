@@ -17,6 +17,7 @@ using namespace mfa;
 struct mfa_ctx {
   int device = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;  // captures the bodies of conditional graph nodes
   mfa_params P;
   mfa_options opt;
   std::vector<mfa_system> sys;
@@ -115,6 +116,44 @@ void rebuild(mfa_ctx* ctx, bool force) {
   launch_rebuild(ctx->S, ctx->st, force);
   k_count_rebuild<<<1, 1, 0, ctx->st>>>(ctx->S.rebuild_flag, ctx->d_rebuilds);
   ctx->launches += 11;
+}
+
+// Graph form of the skin check: the IF body (the ten rebuild kernels) runs only on steps whose
+// position update raised the flag; other steps launch nothing.
+__global__ void k_cond_rebuild(int* flag, long long* n, cudaGraphConditionalHandle h) {
+  const int f = *flag;
+  cudaGraphSetConditional(h, f ? 1u : 0u);
+  if (f) {
+    *n += 1;
+    *flag = 0;
+  }
+}
+
+int capture_conditional_rebuild(mfa_ctx* ctx) {
+  cudaStream_t st = ctx->st;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t graph;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
+  k_cond_rebuild<<<1, 1, 0, st>>>(ctx->S.rebuild_flag, ctx->d_rebuilds, h);
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp = {};  // aggregate initialisation: all reserved fields zero
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, graph, deps, nullptr, nd, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(ctx->st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  launch_rebuild(ctx->S, ctx->st2, true);
+  cudaGraph_t captured;
+  CK(cudaStreamEndCapture(ctx->st2, &captured));
+  CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return MFA_OK;
 }
 
 int bonded_mask(const mfa_ctx* ctx) {
@@ -270,6 +309,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   ctx->device = ctx->opt.device;
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking));
   for (int k = 0; k < 16; ++k) CK(cudaEventCreate(&ctx->ev[k]));
   const mfa_flags& F = p->flags;
   if (p->n_type < 1 || p->n_type > MFA_MAX_TYPES) return fail(ctx, MFA_ERR_ARG, "n_type out of range");
@@ -503,6 +543,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     cap = (int)std::ceil(2.0 * est) + 32;
     cap = std::max(cap, 48);
   }
+  cap = std::min(cap, NL_CAP_MAX);
   S.nbr_cap = cap;
   DA(S.nbr, (size_t)cap * Nn);
   cudaStream_t st = ctx->st;
@@ -558,6 +599,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       if (rc == MFA_ERR_NLIST_OVERFLOW) newcap = std::max(newcap, cap * 3);
       auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void*)S.nbr);
       if (it != ctx->allocs.end()) { cudaFree(*it); ctx->allocs.erase(it); }
+      newcap = std::min(newcap, NL_CAP_MAX);
+      if (newcap <= cap) return fail(ctx, MFA_ERR_CAPACITY, "more neighbours per particle than the list builder holds");
       S.nbr_cap = newcap;
       DA(S.nbr, (size_t)newcap * Nn);
       CK(cudaMemsetAsync(S.status, 0, sizeof(unsigned), st));
@@ -583,6 +626,7 @@ int mfa_destroy(mfa_ctx* ctx) {
   for (int k = 0; k < 16; ++k)
     if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
   if (ctx->st) cudaStreamDestroy(ctx->st);
+  if (ctx->st2) cudaStreamDestroy(ctx->st2);
   delete ctx;
   return MFA_OK;
 }
@@ -769,7 +813,7 @@ int mfa_profiles_accumulate(mfa_ctx* ctx) {
 // ---- fused step -----------------------------------------------------------------------------
 // Issues the kernels of `n` steps; eflag on steps where (absolute step) % energy_every == 0 and
 // on the last step.  Returns the number of launches issued.
-static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof) {
+static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool capturing, int* err) {
   const DevState& S = ctx->S;
   const SimConst& C = ctx->C;
   cudaStream_t st = ctx->st;
@@ -780,9 +824,18 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof) {
   L += 1;
   for (int k = 1; k <= n; ++k) {
     const bool ef = ((phase + k) % ctx->opt.energy_every == 0) || k == n;
-    launch_rebuild(S, st, false);
-    k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
-    L += 11;
+    if (capturing) {
+      int r = capture_conditional_rebuild(ctx);
+      if (r != MFA_OK) {
+        *err = r;
+        return L;
+      }
+      L += 1;  // the rebuild body's launches are not counted: they run only when triggered
+    } else {
+      launch_rebuild(S, st, false);
+      k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
+      L += 11;
+    }
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
     L += 1;
     if (mask) { launch_bonded(S, C, st, mask, ef, acc); L += 1; }
@@ -824,9 +877,12 @@ int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
     auto it = ctx->graphs.find(key);
     if (it == ctx->graphs.end()) {
       cudaGraph_t g;
+      int err = MFA_OK;
       CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-      L = issue_steps(ctx, nsteps, phase, prof);
-      CK(cudaStreamEndCapture(ctx->st, &g));
+      L = issue_steps(ctx, nsteps, phase, prof, true, &err);
+      cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
+      if (err != MFA_OK) return err;
+      CK(ec);
       cudaGraphExec_t ge;
       CK(cudaGraphInstantiate(&ge, g, 0));
       cudaGraphDestroy(g);
@@ -835,7 +891,8 @@ int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
     CK(cudaGraphLaunch(it->second.first, ctx->st));
     L = it->second.second;
   } else {
-    L = issue_steps(ctx, nsteps, phase, prof);
+    int err = MFA_OK;
+    L = issue_steps(ctx, nsteps, phase, prof, false, &err);
     CK(cudaGetLastError());
   }
   ctx->launches += L;

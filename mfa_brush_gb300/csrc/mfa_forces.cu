@@ -72,23 +72,46 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
     const double L0 = R.L[0], L1 = R.L[1], iL0 = R.invL[0], iL1 = R.invL[1];
     const unsigned long long seed = R.seed;
     const int* __restrict__ nb = s.nbr + i;
-    for (int k = 0; k < n; ++k) {
-      const int j = __ldg(nb + (size_t)k * s.Np);
-      real dx, dy, dz;
-      int wj;
+    const real coul_rc2 = (real)C.coul_rc2;
+    auto delta = [&](int j, real& dx, real& dy, real& dz) -> int {
       if constexpr (MIXED) {
-        int4 qj = __ldg(&s.pfx[j]);
-        wj = qj.w;
+        const int4 qj = __ldg(&s.pfx[j]);
         dx = (float)fx_diff(qi.x, qj.x) * ux;
         dy = (float)fx_diff(qi.y, qj.y) * uy;
         dz = (float)fx_diff(qi.z, qj.z) * uz;
+        return qj.w;
       } else {
-        dbl4 pj = s.pd[j];
-        wj = (int)__double_as_longlong(pj.w);
+        const dbl4 pj = s.pd[j];
         dx = mic_ref(pi.x - pj.x, L0, iL0);
         dy = mic_ref(pi.y - pj.y, L1, iL1);
         dz = pi.z - pj.z;
+        return (int)__double_as_longlong(pj.w);
       }
+    };
+    // Two phases per batch: (1) screen list entries with the cheap distance test and keep the
+    // ones inside any interaction range, (2) evaluate LJ + DPD + Coulomb on the kept pairs only.
+    // Without the split a warp runs the Philox/DPD body whenever any lane has an interacting
+    // pair, i.e. on almost every list entry.
+    constexpr int BATCH = 16;
+    int jl[BATCH];
+    int k = 0;
+    while (k < n) {
+      int m = 0;
+      while (k < n && m < BATCH) {
+        const int j = __ldg(nb + (size_t)k * s.Np);
+        ++k;
+        real dx, dy, dz;
+        const int wj = delta(j, dx, dy, dz);
+        const real r2raw = dx * dx + dy * dy + dz * dz;
+        const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
+        const bool hit = r2raw < e.range2 || ((e.flags & PF_DPD_OWN) && r2raw < e.dpd_rc2) ||
+                         ((e.flags & PF_COUL) && r2raw < coul_rc2);
+        if (hit) jl[m++] = j;
+      }
+    for (int t = 0; t < m; ++t) {
+      const int j = jl[t];
+      real dx, dy, dz;
+      const int wj = delta(j, dx, dy, dz);
       const real r2raw = dx * dx + dy * dy + dz * dz;
       const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
       const int fl = e.flags;
@@ -133,7 +156,7 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
         fs += (sig * wr * g - gam * wd * rdot) * ir;
       }
       if (fl & PF_COUL) {
-        const bool in_c = (C.coul_rc2 > 0.) ? (r2raw < (real)C.coul_rc2) : in_lj;
+        const bool in_c = (coul_rc2 > 0) ? (r2raw < coul_rc2) : in_lj;
         if (in_c) {
           const real rc2 = in_lj ? r2 : r2raw;
           const real r = sqrt(rc2), ir = (real)1 / r;
@@ -147,6 +170,7 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
       fx += fs * dx;
       fy += fs * dy;
       fz += fs * dz;
+    }
     }
   }
   if (inside) {

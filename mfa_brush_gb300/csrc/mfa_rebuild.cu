@@ -49,7 +49,15 @@ __global__ void k_bin(DevState s, bool force) {
   double lz = 1. / R.inv_lc[2];
   if (z < -lz || z > R.L[2] + lz) atomicOr(s.status, ST_OUT_OF_BOX);
   int ix, iy, iz;
-  cell_coords(R, x, y, z, ix, iy, iz);
+  if (s.mixed) {  // the list builder's integer formula on the fixed-point view
+    const int4 q = s.pfx[i];
+    ix = (int)(((unsigned long long)(unsigned)q.x * (unsigned)R.nc[0]) >> 32);
+    iy = (int)(((unsigned long long)(unsigned)q.y * (unsigned)R.nc[1]) >> 32);
+    iz = (int)(((long long)q.z * R.nc[2]) >> 30);
+    iz = min(max(iz, 0), R.nc[2] - 1);
+  } else {
+    cell_coords(R, x, y, z, ix, iy, iz);
+  }
   int c = R.cell_off + (iz * R.nc[1] + iy) * R.nc[0] + ix;
   s.cell_of[i] = c;
   s.rank[i] = atomicAdd(&s.cell_count[c], 1);
@@ -211,73 +219,121 @@ __global__ void k_copyback(DevState s, bool force) {
 }
 
 // Full Verlet list: every mobile particle lists all j (mobile or wall) with r^2 < (rc_ij+skin)^2.
+// One thread per particle.  The 27 surrounding cells are walked as 9 x-rows: the three cells of a
+// row are consecutive in the sorted order unless the row wraps in x, so a row is one contiguous
+// slot range (two when it wraps).  Each thread stages its list in shared memory (row stride
+// cap|1 keeps the banks distinct) and the block writes the list out row by row: the k-th
+// neighbours of 128 consecutive particles are 128 consecutive ints of nbr, so every store is
+// coalesced (scattered 4-byte stores into the column-major list cost read-modify-writes in HBM).
+constexpr int NL_BLOCK = 128;
+
 template <bool MIXED>
-__global__ void __launch_bounds__(128) k_nlist(DevState s, bool force) {
+__global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
-  __shared__ double rl2[NPAIR];
-  for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) rl2[k] = s.tabd[k].rlist2;
-  __syncthreads();
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.N) return;
-  int w = s.info[i];
-  if (!info_mobile(w)) {
-    s.nn[i] = 0;
-    return;
+  extern __shared__ int nl_sh[];
+  __shared__ float rl2f[NPAIR];
+  __shared__ double rl2d[NPAIR];
+  __shared__ int blk_max;
+  const int cap = s.nbr_cap, pitch = cap | 1;
+  int* mine = nl_sh + threadIdx.x * pitch;
+  for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
+    rl2d[k] = s.tabd[k].rlist2;
+    rl2f[k] = s.tabf ? s.tabf[k].rlist2 : 0.f;
   }
-  const RepDesc& R = s.reps[info_rep(w)];
-  int ti = info_type(w);
-  double x = s.rx[i], y = s.ry[i], z = s.rz[i];
-  int ix, iy, iz;
-  cell_coords(R, x, y, z, ix, iy, iz);
-  int4 qi = s.pfx ? s.pfx[i] : make_int4(0, 0, 0, 0);
-  float ux = R.ufx_f[0], uy = R.ufx_f[1], uz = R.ufx_f[2];
+  if (threadIdx.x == 0) blk_max = 0;
+  __syncthreads();
+  const int i = blockIdx.x * NL_BLOCK + threadIdx.x;
+  const int w = (i < s.N) ? s.info[i] : 0;
   int cnt = 0;
-  const int cap = s.nbr_cap;
-  for (int dz = -1; dz <= 1; ++dz) {
-    int cz = iz + dz;
-    if (cz < 0 || cz >= R.nc[2]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      int cy = iy + dy;
-      cy += (cy < 0) ? R.nc[1] : 0;
-      cy -= (cy >= R.nc[1]) ? R.nc[1] : 0;
-      for (int dx = -1; dx <= 1; ++dx) {
-        int cx = ix + dx;
-        cx += (cx < 0) ? R.nc[0] : 0;
-        cx -= (cx >= R.nc[0]) ? R.nc[0] : 0;
-        int c = R.cell_off + (cz * R.nc[1] + cy) * R.nc[0] + cx;
-        int b = s.cell_start[c], e = b + s.cell_count[c];
-        for (int j = b; j < e; ++j) {
-          if (j == i) continue;
-          int wj;
-          double r2;
-          if (MIXED) {
-            int4 qj = s.pfx[j];
-            wj = qj.w;
-            float ddx = (float)fx_diff(qi.x, qj.x) * ux;
-            float ddy = (float)fx_diff(qi.y, qj.y) * uy;
-            float ddz = (float)fx_diff(qi.z, qj.z) * uz;
-            r2 = (double)(ddx * ddx + ddy * ddy + ddz * ddz);
-          } else {
-            wj = s.info[j];
-            double ddx = mic_ref(x - s.rx[j], R.L[0], R.invL[0]);
-            double ddy = mic_ref(y - s.ry[j], R.L[1], R.invL[1]);
-            double ddz = z - s.rz[j];
-            r2 = ddx * ddx + ddy * ddy + ddz * ddz;
-          }
-          if (r2 < rl2[ti * MAXT + info_type(wj)]) {
-            if (cnt < cap) s.nbr[(size_t)cnt * s.Np + i] = j;
-            ++cnt;
+  if (i < s.N && info_mobile(w)) {
+    const RepDesc& R = s.reps[info_rep(w)];
+    const int ti = info_type(w);
+    int ix, iy, iz;
+    int4 qi = make_int4(0, 0, 0, 0);
+    double x = 0., y = 0., z = 0.;
+    if (MIXED) {
+      qi = s.pfx[i];
+      ix = (int)(((unsigned long long)(unsigned)qi.x * (unsigned)R.nc[0]) >> 32);
+      iy = (int)(((unsigned long long)(unsigned)qi.y * (unsigned)R.nc[1]) >> 32);
+      iz = (int)(((long long)qi.z * R.nc[2]) >> 30);
+      iz = min(max(iz, 0), R.nc[2] - 1);
+    } else {
+      x = s.rx[i]; y = s.ry[i]; z = s.rz[i];
+      cell_coords(R, x, y, z, ix, iy, iz);
+    }
+    const float ux = R.ufx_f[0], uy = R.ufx_f[1], uz = R.ufx_f[2];
+    const int nx = R.nc[0];
+    const int xl = (ix == 0) ? nx - 1 : ix - 1, xr = (ix == nx - 1) ? 0 : ix + 1;
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int cz = iz + dz;
+      if (cz < 0 || cz >= R.nc[2]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int cy = iy + dy;
+        cy += (cy < 0) ? R.nc[1] : 0;
+        cy -= (cy >= R.nc[1]) ? R.nc[1] : 0;
+        const int row = R.cell_off + (cz * R.nc[1] + cy) * nx;
+        // segments of the row: [xl..xr] without wrap, else {xl} + [ix..xr] or [xl..ix] + {xr}
+        int sb[2], se[2], nseg;
+        if (xl < xr) {
+          sb[0] = s.cell_start[row + xl];
+          se[0] = s.cell_start[row + xr] + s.cell_count[row + xr];
+          nseg = 1;
+        } else if (ix == 0) {
+          sb[0] = s.cell_start[row + ix];
+          se[0] = s.cell_start[row + xr] + s.cell_count[row + xr];
+          sb[1] = s.cell_start[row + xl];
+          se[1] = sb[1] + s.cell_count[row + xl];
+          nseg = 2;
+        } else {
+          sb[0] = s.cell_start[row + xl];
+          se[0] = s.cell_start[row + ix] + s.cell_count[row + ix];
+          sb[1] = s.cell_start[row + xr];
+          se[1] = sb[1] + s.cell_count[row + xr];
+          nseg = 2;
+        }
+        for (int g = 0; g < nseg; ++g) {
+          for (int j = sb[g]; j < se[g]; ++j) {
+            if (j == i) continue;
+            int wj;
+            bool hit;
+            if (MIXED) {
+              const int4 qj = s.pfx[j];
+              wj = qj.w;
+              const float ddx = (float)fx_diff(qi.x, qj.x) * ux;
+              const float ddy = (float)fx_diff(qi.y, qj.y) * uy;
+              const float ddz = (float)fx_diff(qi.z, qj.z) * uz;
+              hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2f[ti * MAXT + info_type(wj)];
+            } else {
+              wj = s.info[j];
+              const double ddx = mic_ref(x - s.rx[j], R.L[0], R.invL[0]);
+              const double ddy = mic_ref(y - s.ry[j], R.L[1], R.invL[1]);
+              const double ddz = z - s.rz[j];
+              hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2d[ti * MAXT + info_type(wj)];
+            }
+            if (hit) {
+              if (cnt < cap) mine[cnt] = j;
+              ++cnt;
+            }
           }
         }
       }
     }
+    if (cnt > cap) {
+      atomicOr(s.status, ST_NLIST_OVERFLOW);
+      cnt = cap;
+    }
   }
-  if (cnt > cap) {
-    atomicOr(s.status, ST_NLIST_OVERFLOW);
-    cnt = cap;
+  atomicMax(&blk_max, cnt);
+  __syncthreads();
+  const int mx = blk_max;
+  if (i < s.N) {
+    for (int k = 0; k < mx; ++k)
+      if (k < cnt) s.nbr[(size_t)k * s.Np + i] = mine[k];
+    s.nn[i] = cnt;
   }
-  s.nn[i] = cnt;
 }
+
+size_t nlist_smem(int cap) { return (size_t)NL_BLOCK * (size_t)(cap | 1) * sizeof(int); }
 
 __global__ void k_clear_flag(int* flag) { *flag = 0; }
 
@@ -295,10 +351,18 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   k_sort_cells<<<gC, B, 0, st>>>(s, force);
   k_permute<<<gN, B, 0, st>>>(s, force);
   k_copyback<<<gN, B, 0, st>>>(s, force);
+  const size_t shm = nlist_smem(s.nbr_cap);
+  static size_t shm_set[2] = {48 * 1024, 48 * 1024};
+  if (shm > shm_set[s.mixed]) {  // above 48 KB of dynamic shared memory needs an opt-in
+    if (s.mixed) cudaFuncSetAttribute(k_nlist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    else cudaFuncSetAttribute(k_nlist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    shm_set[s.mixed] = shm;
+  }
+  const int gl = (s.N + NL_BLOCK - 1) / NL_BLOCK;
   if (s.mixed)
-    k_nlist<true><<<(s.N + 127) / 128, 128, 0, st>>>(s, force);
+    k_nlist<true><<<gl, NL_BLOCK, shm, st>>>(s, force);
   else
-    k_nlist<false><<<(s.N + 127) / 128, 128, 0, st>>>(s, force);
+    k_nlist<false><<<gl, NL_BLOCK, shm, st>>>(s, force);
 }
 
 // ---------------------------------------------------------------------------------------------
