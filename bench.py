@@ -150,6 +150,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
+    ap.add_argument("--skin", type=float, default=0.3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
@@ -174,7 +175,7 @@ def main():
     from mfa_brush_gb300 import configs
     systems, a_type, r0, v = configs.concat(reps)
     n_atoms = int(sum(s.n_part for s in systems))
-    g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=0.3)
+    g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin)
 
     def barrier():
         if dist is not None:
@@ -226,7 +227,7 @@ def main():
             "data": "synthetic (seeded brush channels)",
             "config": {"workload": "256 uneven brush-channel replicas, WCA+FENE+DPD, batched",
                        "replicas": len(systems) * world, "particles_per_gpu": n_atoms,
-                       "precision": args.precision, "chunk_steps": CHUNK, "skin": 0.3,
+                       "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
             "gpu_launches": int(launches + 10 * rebuilds),

@@ -249,6 +249,9 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   DA(K.kfac, K.nk);
   DA(K.rho, 2 * K.nk);
   DA(K.mz, 1);
+  K.kchunk = 512;
+  K.nkchunks = (K.nk + K.kchunk - 1) / K.kchunk;
+  DA(K.fpart, (size_t)K.nkchunks * std::max(K.nq, 1) * 3);
   DA(K.qtag, K.nq);
   if (ctx->S.mixed) DA(K.tabf, (size_t)K.nq * K.ncol); else DA(K.tabd, (size_t)K.nq * K.ncol);
   cudaStream_t st = ctx->st;
@@ -476,6 +479,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     R.v_ww = ctx->v_ww[r];
     R.inv_n = (F.system == 2) ? 1. / (double)s.n_mon_tot : 1. / (double)(s.n_mon_tot - s.n_chain);
     R.hist_inv_dz = 1. / (D / (double)C.hist_dim);
+    std::memcpy(&R.Lbits[0], &R.L[0], 8);
+    std::memcpy(&R.Lbits[1], &R.L[1], 8);
     p0 += s.n_part;
     dens_max = std::max(dens_max, (double)s.n_part / (s.boundary[0] * s.boundary[1] * D));
     if (charged) {
@@ -511,7 +516,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   for (auto d : dst) DA(*d, Nn);
   for (int k = 0; k < 9; ++k) DA(S.tmp[k], Nn);
   DA(S.tag, Nn); DA(S.info, Nn); DA(S.tmp_tag, Nn); DA(S.tmp_info, Nn); DA(S.slot_of_tag, Nn);
-  if (S.mixed) { DA(S.pfx, Nn); DA(S.vf, Nn); } else { DA(S.pd, Nn); DA(S.vd, Nn); }
+  if (S.mixed) { DA(S.pfx, Nn); DA(S.vf, Nn); DA(S.f4, Nn); } else { DA(S.pd, Nn); DA(S.vd, Nn); }
   DA(S.ref, Nn);
   DA(S.nn, Nn);
   DA(S.cell_of, Nn); DA(S.rank, Nn); DA(S.perm, Nn);
@@ -838,11 +843,11 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool cap
     }
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
     L += 1;
-    if (mask) { launch_bonded(S, C, st, mask, ef, acc); L += 1; }
+    if (mask) { launch_bonded(S, C, st, mask, ef, acc, true); L += 1; }
     if (ctx->kspace) {
-      launch_kspace(S, C, ctx->K, st, ef, acc);
-      launch_dipolar(S, C, ctx->K, st, ef, acc);
-      L += 6;
+      launch_kspace(S, C, ctx->K, st, ef, acc, true);
+      launch_dipolar(S, C, ctx->K, st, ef, acc, true);
+      L += 7;
     }
     if (k < n && !prof) {
       launch_integrate(S, C, st, 2, true, ef, acc);
@@ -1099,8 +1104,12 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
     mark(0);
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
     mark(1);
-    if (mask) { launch_bonded(S, C, st, mask, ef, acc); mark(2); }
-    if (ctx->kspace) { launch_kspace(S, C, ctx->K, st, ef, acc); launch_dipolar(S, C, ctx->K, st, ef, acc); mark(4); }
+    if (mask) { launch_bonded(S, C, st, mask, ef, acc, true); mark(2); }
+    if (ctx->kspace) {
+      launch_kspace(S, C, ctx->K, st, ef, acc, true);
+      launch_dipolar(S, C, ctx->K, st, ef, acc, true);
+      mark(4);
+    }
     launch_integrate(S, C, st, k < nsteps ? 2 : 1, true, ef, acc);
     mark(3);
     if (ef) { launch_record(acc, ctx->rec, st); mark(6); }

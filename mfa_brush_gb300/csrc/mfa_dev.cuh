@@ -91,6 +91,7 @@ struct RepDesc {
   long long s_time;
   double lz_half, v_ww, inv_n;
   double hist_inv_dz;
+  long long Lbits[2];   // bit patterns of Lx, Ly: for positive doubles, integer order = numeric order
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -137,14 +138,59 @@ __device__ __forceinline__ double pair_gauss_d(unsigned long long seed, long lon
 }
 
 // ---------------------------------------------------------------------------------------------
+// Conversions on the fast pipes.  On GB300 the conversion instructions (I2F, F2F, F2I) issue at
+// the FP64 rate, 2 per SM per clock against 128 FP32 operations, which made them the hidden
+// limiter of the pair kernel (three int->float per list entry) and of the integrator.  These
+// exact replacements use integer and FP32 arithmetic only.
+// ---------------------------------------------------------------------------------------------
+// int32 -> float, correctly rounded: high and low 16-bit halves through the 2^23 magic numbers,
+// recombined with one FFMA (hi*2^16 + lo is exact before the single rounding).
+__device__ __forceinline__ float i2f_fast(int d) {
+  const float hi = __int_as_float(0x4B400000 + (d >> 16)) - 12582912.0f;     // d>>16 in [-2^15, 2^15)
+  const float lo = __int_as_float(0x4B000000 | (d & 0xFFFF)) - 8388608.0f;   // [0, 2^16)
+  return fmaf(hi, 65536.0f, lo);
+}
+
+// float -> double, exact for normal numbers; zero and subnormals become signed zero.
+__device__ __forceinline__ double f2d_fast(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  const unsigned sgn = u & 0x80000000u;
+  unsigned hi = sgn | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+  unsigned lo = u << 29;
+  if (e == 0) { hi = sgn; lo = 0u; }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// double -> float, round to nearest even, for |d| inside the normal float range (smaller
+// magnitudes flush to signed zero; the values converted here are velocities and distances).
+__device__ __forceinline__ float d2f_fast(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sgn = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  unsigned mant = (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)(m & 0x1FFFFFFFull);
+  mant += (rem > 0x10000000u || (rem == 0x10000000u && (mant & 1u))) ? 1u : 0u;
+  const unsigned r = sgn | (((unsigned)e << 23) + mant);  // a mantissa carry bumps the exponent
+  return __uint_as_float(e <= 0 ? sgn : r);
+}
+
+// round(x) of a double with |x| < 2^51 to int64 with one FP64 add (2^52 + 2^51 magic).
+__device__ __forceinline__ long long d2ll_round_fast(double x) {
+  return __double_as_longlong(x + 6755399441055744.0) - 0x4338000000000000ll;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Fixed-point positions
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ int to_fx_periodic(double x, double s) {
   // x in [0, L] -> [0, 2^32) modulo 2^32
-  long long v = __double2ll_rn(x * s);
+  long long v = d2ll_round_fast(x * s);
   return (int)(unsigned int)(unsigned long long)v;
 }
-__device__ __forceinline__ int to_fx_z(double z, double s) { return (int)__double2ll_rn(z * s); }
+__device__ __forceinline__ int to_fx_z(double z, double s) { return (int)d2ll_round_fast(z * s); }
 __device__ __forceinline__ int fx_diff(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
 
 // Minimum image of the reference: d - L*int(2 d / L) (fluid_fluid.f90:111-112).

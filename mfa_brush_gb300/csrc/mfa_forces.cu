@@ -76,9 +76,9 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
     auto delta = [&](int j, real& dx, real& dy, real& dz) -> int {
       if constexpr (MIXED) {
         const int4 qj = __ldg(&s.pfx[j]);
-        dx = (float)fx_diff(qi.x, qj.x) * ux;
-        dy = (float)fx_diff(qi.y, qj.y) * uy;
-        dz = (float)fx_diff(qi.z, qj.z) * uz;
+        dx = i2f_fast(fx_diff(qi.x, qj.x)) * ux;
+        dy = i2f_fast(fx_diff(qi.y, qj.y)) * uy;
+        dz = i2f_fast(fx_diff(qi.z, qj.z)) * uz;
         return qj.w;
       } else {
         const dbl4 pj = s.pd[j];
@@ -93,21 +93,38 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
     // Without the split a warp runs the Philox/DPD body whenever any lane has an interacting
     // pair, i.e. on almost every list entry.
     constexpr int BATCH = 16;
+    constexpr int G = 4;  // list entries screened per group: their loads are all in flight at once
     int jl[BATCH];
     int k = 0;
+    auto screen = [&](int j) -> bool {
+      real dx, dy, dz;
+      const int wj = delta(j, dx, dy, dz);
+      const real r2raw = dx * dx + dy * dy + dz * dz;
+      const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
+      return r2raw < e.range2 || ((e.flags & PF_DPD_OWN) && r2raw < e.dpd_rc2) ||
+             ((e.flags & PF_COUL) && r2raw < coul_rc2);
+    };
     while (k < n) {
       int m = 0;
+      // groups of G independent entries (index loads first, then the position gathers)
+      while (k + G <= n && m <= BATCH - G) {
+        int jg[G];
+#pragma unroll
+        for (int u = 0; u < G; ++u) jg[u] = __ldg(nb + (size_t)(k + u) * s.Np);
+        bool hg[G];
+#pragma unroll
+        for (int u = 0; u < G; ++u) hg[u] = screen(jg[u]);
+#pragma unroll
+        for (int u = 0; u < G; ++u)
+          if (hg[u]) jl[m++] = jg[u];
+        k += G;
+      }
       while (k < n && m < BATCH) {
         const int j = __ldg(nb + (size_t)k * s.Np);
         ++k;
-        real dx, dy, dz;
-        const int wj = delta(j, dx, dy, dz);
-        const real r2raw = dx * dx + dy * dy + dz * dz;
-        const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
-        const bool hit = r2raw < e.range2 || ((e.flags & PF_DPD_OWN) && r2raw < e.dpd_rc2) ||
-                         ((e.flags & PF_COUL) && r2raw < coul_rc2);
-        if (hit) jl[m++] = j;
+        if (screen(j)) jl[m++] = j;
       }
+#pragma unroll 2
     for (int t = 0; t < m; ++t) {
       const int j = jl[t];
       real dx, dy, dz;
@@ -180,10 +197,12 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
         s.fy[i] += (double)fy;
         s.fz[i] += (double)fz;
       }
+    } else if constexpr (MIXED) {
+      s.f4[i] = make_float4(fx, fy, fz, 0.f);  // fused step: FP32 forces for the integrator
     } else {
-      s.fx[i] = (double)fx;
-      s.fy[i] = (double)fy;
-      s.fz[i] = (double)fz;
+      s.fx[i] = fx;
+      s.fy[i] = fy;
+      s.fz[i] = fz;
     }
   }
   if (EFLAG) {
@@ -227,9 +246,9 @@ template <bool MIXED>
 __device__ __forceinline__ void bead_delta(const BeadPos<MIXED>& a, const BeadPos<MIXED>& b, const RepDesc& R,
                                            real_t<MIXED>* d) {
   if constexpr (MIXED) {
-    d[0] = (float)fx_diff(a.q.x, b.q.x) * R.ufx_f[0];
-    d[1] = (float)fx_diff(a.q.y, b.q.y) * R.ufx_f[1];
-    d[2] = (float)fx_diff(a.q.z, b.q.z) * R.ufx_f[2];
+    d[0] = i2f_fast(fx_diff(a.q.x, b.q.x)) * R.ufx_f[0];
+    d[1] = i2f_fast(fx_diff(a.q.y, b.q.y)) * R.ufx_f[1];
+    d[2] = i2f_fast(fx_diff(a.q.z, b.q.z)) * R.ufx_f[2];
   } else {
     d[0] = mic_ref(a.x - b.x, R.L[0], R.invL[0]);
     d[1] = mic_ref(a.y - b.y, R.L[1], R.invL[1]);
@@ -312,7 +331,7 @@ __device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, cons
 }
 
 template <bool MIXED, bool EFLAG>
-__global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask, Acc acc) {
+__global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask, Acc acc, bool to_f4) {
   using real = real_t<MIXED>;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool inside = i < s.N;
@@ -429,9 +448,17 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
       F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
       if (EFLAG && m == 0) e_or += (real)0.5 * fm * da;
     }
-    s.fx[i] += (double)F[0];
-    s.fy[i] += (double)F[1];
-    s.fz[i] += (double)F[2];
+    if (MIXED && to_f4) {  // fused step: FP32 force array
+      float4 f = s.f4[i];
+      f.x += (float)F[0];
+      f.y += (float)F[1];
+      f.z += (float)F[2];
+      s.f4[i] = f;
+    } else {
+      s.fx[i] += (double)F[0];
+      s.fy[i] += (double)F[1];
+      s.fz[i] += (double)F[2];
+    }
   }
   if (EFLAG) {
     active = active && kind >= 0;
@@ -442,15 +469,16 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
   }
 }
 
-void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc) {
+void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc,
+                   bool fused) {
   if (!mask) return;
   int B = 128, g = (s.N + B - 1) / B;
   if (s.mixed) {
-    if (eflag) k_bonded<true, true><<<g, B, 0, st>>>(s, C, mask, acc);
-    else k_bonded<true, false><<<g, B, 0, st>>>(s, C, mask, acc);
+    if (eflag) k_bonded<true, true><<<g, B, 0, st>>>(s, C, mask, acc, fused);
+    else k_bonded<true, false><<<g, B, 0, st>>>(s, C, mask, acc, fused);
   } else {
-    if (eflag) k_bonded<false, true><<<g, B, 0, st>>>(s, C, mask, acc);
-    else k_bonded<false, false><<<g, B, 0, st>>>(s, C, mask, acc);
+    if (eflag) k_bonded<false, true><<<g, B, 0, st>>>(s, C, mask, acc, false);
+    else k_bonded<false, false><<<g, B, 0, st>>>(s, C, mask, acc, false);
   }
 }
 

@@ -92,9 +92,9 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       int4 q;
       store_views(s, i, R, x, y, z, vx, vy, vz, w, s.tag[i], q);
       const int4 q0 = s.ref[i];
-      const float dx = (float)fx_diff(q.x, q0.x) * R.ufx_f[0];
-      const float dy = (float)fx_diff(q.y, q0.y) * R.ufx_f[1];
-      const float dz = (float)fx_diff(q.z, q0.z) * R.ufx_f[2];
+      const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
+      const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
+      const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
       if (dx * dx + dy * dy + dz * dz > (float)C.skin_half2) *s.rebuild_flag = 1;
       if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(s.status, ST_NAN);
     }
@@ -119,14 +119,29 @@ __device__ __forceinline__ float wall93f(const SimConst& C, int t, float zl, flo
   return f;
 }
 
-// The fused step of the mixed-precision path: velocities of step n and positions of step n+1 in
-// one pass with the FP64 work cut to the accumulators (GB300 issues FP64 at a small fraction of
-// the FP32 rate).  Forces, the wall term, accelerations and the velocity increment are FP32; the
-// half-kick pair v(n-1/2) -> v(n) -> v(n+1/2) is one FP64 add of dt*a, and the drift is
-// r(n+1) = r(n) + dt v(n+1/2), identical in exact arithmetic to verlet_velocities followed by
-// verlet_positions.  Kinetic energy (energy steps) uses v(n) = v(n+1/2) - dt/2 a.
-template <bool EFLAG>
-__global__ void __launch_bounds__(256) k_fused_mixed(DevState s, SimConst C, Acc acc) {
+// x -> wrapped x of verlet_positions.f90:170-186 (`> L` then `< 0`), decided on the bit pattern:
+// for positive doubles integer order equals numeric order, so no FP64 compare is issued.
+__device__ __forceinline__ double wrap_bits(double x, double L, long long Lbits) {
+  const long long b = __double_as_longlong(x);
+  if (b < 0) return (b == (long long)0x8000000000000000ull) ? x : x + L;  // -0.0 stays
+  if (b > Lbits) return x - L;
+  return x;
+}
+
+// The integrator of the mixed-precision path with the FP64 work cut to the state accumulators
+// (GB300 issues FP64 and every conversion instruction at 2 per SM per clock, 1/64 of FP32):
+//   MODE 0  positions (verlet_positions): dv = dt/2 a(n-1); v += dv; r += dt v.
+//   MODE 1  velocities (verlet_velocities): a = F/m; v += dt/2 a; heads fixed; a and the total
+//           force are stored; kinetic energy.
+//   MODE 2  both at once: v(n-1/2) -> v(n+1/2) with one FP64 add of dt a(n), r += dt v(n+1/2),
+//           equal in exact arithmetic to MODE 1 followed by MODE 0; kinetic energy from
+//           v(n) = v(n+1/2) - dt/2 a.
+// r + dt v + dt^2/2 a is formed as r + dt (v + dt/2 a).  Forces, accelerations, wall and body
+// forces and velocity increments are FP32; r and v stay FP64.  FUSED reads the FP32 force array
+// of the fused step and adds the 9-3 walls and the body force; otherwise the FP64 force array of
+// the per-routine path is used as is.  Conversions use the integer forms of mfa_dev.cuh.
+template <int MODE, bool EFLAG, bool FUSED>
+__global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc acc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool inside = i < s.N;
   const int w = inside ? s.info[i] : 0;
@@ -136,66 +151,88 @@ __global__ void __launch_bounds__(256) k_fused_mixed(DevState s, SimConst C, Acc
   if (mob) {
     const RepDesc& R = s.reps[rep];
     const int t = info_type(w);
-    float Fx = (float)s.fx[i], Fy = (float)s.fy[i], Fz = (float)s.fz[i];
     double x = s.rx[i], y = s.ry[i], z = s.rz[i];
-    if (C.wall == 2) {
-      float e;
-      Fz += wall93f(C, t, (float)z, (float)(R.L[2] - z), e);
-      efw = e;
-    }
-    if (C.poiseuille && t != 0) {
-      Fx += C.mass_f[t] * C.cforce_f[0];
-      Fy += C.mass_f[t] * C.cforce_f[1];
-      Fz += C.mass_f[t] * C.cforce_f[2];
-    }
-    const float sc = C.dt_f * C.inv_mass_f[t];
-    float dvx = Fx * sc, dvy = Fy * sc, dvz = Fz * sc;
     double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
-    if (info_head(w)) {
-      vx = vy = vz = 0.;
-      dvx = dvy = dvz = 0.f;
+    float ax, ay, az;
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    if (MODE >= 1) {
+      if (FUSED) {
+        const float4 F4 = s.f4[i];
+        Fx = F4.x; Fy = F4.y; Fz = F4.z;
+        if (C.wall == 2) {
+          float e;
+          Fz += wall93f(C, t, d2f_fast(z), d2f_fast(R.L[2] - z), e);
+          efw = e;
+        }
+        if (C.poiseuille && t != 0) {
+          Fx += C.mass_f[t] * C.cforce_f[0];
+          Fy += C.mass_f[t] * C.cforce_f[1];
+          Fz += C.mass_f[t] * C.cforce_f[2];
+        }
+      } else {
+        Fx = d2f_fast(s.fx[i]); Fy = d2f_fast(s.fy[i]); Fz = d2f_fast(s.fz[i]);
+      }
+      const float im = C.inv_mass_f[t];
+      ax = Fx * im; ay = Fy * im; az = Fz * im;
+      if (info_head(w)) {
+        vx = vy = vz = 0.;
+        ax = ay = az = 0.f;
+        Fx = Fy = Fz = 0.f;
+      }
+    } else {
+      ax = d2f_fast(s.ax[i]); ay = d2f_fast(s.ay[i]); az = d2f_fast(s.az[i]);
     }
-    if (EFLAG) {
-      const float ux = (float)vx + 0.5f * dvx, uy = (float)vy + 0.5f * dvy, uz = (float)vz + 0.5f * dvz;
+    const float h = (MODE == 2) ? C.dt_f : 0.5f * C.dt_f;
+    const float dvx = h * ax, dvy = h * ay, dvz = h * az;
+    if (EFLAG && MODE >= 1) {
+      const float c = (MODE == 2) ? 0.5f : 1.0f;  // v(n) = v + dv/2 (MODE 2) or v + dv (MODE 1)
+      const float ux = d2f_fast(vx) + c * dvx, uy = d2f_fast(vy) + c * dvy, uz = d2f_fast(vz) + c * dvz;
       ke = 0.5f * C.mass_f[t] * (ux * ux + uy * uy + uz * uz);
     }
-    vx += (double)dvx;
-    vy += (double)dvy;
-    vz += (double)dvz;
-    x = fma(C.dt, vx, x);
-    y = fma(C.dt, vy, y);
-    z = fma(C.dt, vz, z);
-    if (x > R.L[0]) x -= R.L[0]; else if (x < 0.) x += R.L[0];
-    if (y > R.L[1]) y -= R.L[1]; else if (y < 0.) y += R.L[1];
-    s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
+    vx += f2d_fast(dvx);
+    vy += f2d_fast(dvy);
+    vz += f2d_fast(dvz);
     s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
-    int4 q;
-    q.x = to_fx_periodic(x, R.sfx[0]);
-    q.y = to_fx_periodic(y, R.sfx[1]);
-    q.z = to_fx_z(z, R.sfx[2]);
-    q.w = w;
-    s.pfx[i] = q;
-    s.vf[i] = make_float4((float)vx, (float)vy, (float)vz, __int_as_float(s.tag[i]));
-    const int4 q0 = s.ref[i];
-    const float dx = (float)fx_diff(q.x, q0.x) * R.ufx_f[0];
-    const float dy = (float)fx_diff(q.y, q0.y) * R.ufx_f[1];
-    const float dz = (float)fx_diff(q.z, q0.z) * R.ufx_f[2];
-    if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) *s.rebuild_flag = 1;
-    if (!(isfinite(z) && isfinite(x))) atomicOr(s.status, ST_NAN);
+    if (MODE == 1) {
+      s.ax[i] = f2d_fast(ax); s.ay[i] = f2d_fast(ay); s.az[i] = f2d_fast(az);
+      s.fx[i] = f2d_fast(Fx); s.fy[i] = f2d_fast(Fy); s.fz[i] = f2d_fast(Fz);
+    } else {
+      x = wrap_bits(fma(C.dt, vx, x), R.L[0], R.Lbits[0]);
+      y = wrap_bits(fma(C.dt, vy, y), R.L[1], R.Lbits[1]);
+      z = fma(C.dt, vz, z);
+      s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
+      int4 q;
+      q.x = to_fx_periodic(x, R.sfx[0]);
+      q.y = to_fx_periodic(y, R.sfx[1]);
+      q.z = to_fx_z(z, R.sfx[2]);
+      q.w = w;
+      s.pfx[i] = q;
+      s.vf[i] = make_float4(d2f_fast(vx), d2f_fast(vy), d2f_fast(vz), __int_as_float(s.tag[i]));
+      const int4 q0 = s.ref[i];
+      const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
+      const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
+      const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
+      if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) *s.rebuild_flag = 1;
+      const long long bx = __double_as_longlong(x), bz = __double_as_longlong(z);
+      if (((bx >> 52) & 0x7FF) == 0x7FF || ((bz >> 52) & 0x7FF) == 0x7FF) atomicOr(s.status, ST_NAN);
+    }
   }
-  if (i == 0) *s.steps_done += 1;
-  if (EFLAG) {
+  if (MODE >= 1 && i == 0) *s.steps_done += 1;
+  if (EFLAG && MODE >= 1) {
     add_obs(acc.col(O_TFLUID), rep, (double)ke, mob, acc.nrep);
-    if (C.wall == 2) add_obs(acc.col(O_VFW), rep, (double)efw, mob, acc.nrep);
+    if (FUSED && C.wall == 2) add_obs(acc.col(O_VFW), rep, (double)efw, mob, acc.nrep);
   }
 }
 
 template <int MODE>
 static void launch_mode(const DevState& s, const SimConst& C, cudaStream_t st, bool add_ext, bool eflag, Acc acc) {
   const int B = 256, g = (s.N + B - 1) / B;
-  if (MODE == 2 && add_ext && s.mixed) {
-    if (eflag) k_fused_mixed<true><<<g, B, 0, st>>>(s, C, acc);
-    else k_fused_mixed<false><<<g, B, 0, st>>>(s, C, acc);
+  if (s.mixed) {
+    if (MODE == 0) k_int_mixed<0, false, false><<<g, B, 0, st>>>(s, C, acc);
+    else if (add_ext && eflag) k_int_mixed<MODE, true, true><<<g, B, 0, st>>>(s, C, acc);
+    else if (add_ext) k_int_mixed<MODE, false, true><<<g, B, 0, st>>>(s, C, acc);
+    else if (eflag) k_int_mixed<MODE, true, false><<<g, B, 0, st>>>(s, C, acc);
+    else k_int_mixed<MODE, false, false><<<g, B, 0, st>>>(s, C, acc);
     return;
   }
   if (add_ext) {

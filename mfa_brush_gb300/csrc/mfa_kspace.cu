@@ -162,14 +162,37 @@ __global__ void __launch_bounds__(128) k_ks_force(DevState s, SimConst C, KSpace
     y = kd[kk * 6 + 1] * sgl - cy; t = fy + y; cy = (t - fy) - y; fy = t;
     y = kd[kk * 6 + 2] * sgl - cz; t = fz + y; cz = (t - fz) - y; fz = t;
   }
-  const int i = s.slot_of_tag[K.qtag[p]];
-  const double qf = -pi8 * C.charge[info_type(s.info[i])] * K.inv_V;
-  atomicAdd(&s.fx[i], qf * (double)fx);
-  atomicAdd(&s.fy[i], qf * (double)fy);
-  atomicAdd(&s.fz[i], qf * (double)fz);
+  double* o = K.fpart + ((size_t)blockIdx.y * K.nq + p) * 3;
+  o[0] = (double)fx;
+  o[1] = (double)fy;
+  o[2] = (double)fz;
 }
 
-void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc) {
+// F_i = -(8 pi q_i / V) * sum over k-chunks in a fixed order (deterministic), added to the FP64
+// force array or, in the fused mixed-precision step, to the FP32 one.
+__global__ void k_ks_force_sum(DevState s, SimConst C, KSpace K, double pi8, bool to_f4) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= K.nq) return;
+  double f[3] = {0., 0., 0.};
+  for (int c = 0; c < K.nkchunks; ++c)
+    for (int d = 0; d < 3; ++d) f[d] += K.fpart[((size_t)c * K.nq + p) * 3 + d];
+  const int i = s.slot_of_tag[K.qtag[p]];
+  const double qf = -pi8 * C.charge[info_type(s.info[i])] * K.inv_V;
+  if (to_f4) {
+    float4 g = s.f4[i];
+    g.x += (float)(qf * f[0]);
+    g.y += (float)(qf * f[1]);
+    g.z += (float)(qf * f[2]);
+    s.f4[i] = g;
+  } else {
+    s.fx[i] += qf * f[0];
+    s.fy[i] += qf * f[1];
+    s.fz[i] += qf * f[2];
+  }
+}
+
+void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
+                   bool fused) {
   if (K.nk == 0 || K.nq == 0) return;
   const double pi = (double)3.1415926536f;  // mfa_common.f90:315 (single-precision literal)
   int nt = K.nq * K.ncol;
@@ -187,11 +210,11 @@ void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaSt
   if (s.mixed) k_ks_rho<true><<<g1, 256, shm, st>>>(s, C, K, chunk);
   else k_ks_rho<false><<<g1, 256, shm, st>>>(s, C, K, chunk);
   k_ks_energy<<<1, 1024, 0, st>>>(K, 4. * pi, acc, eflag);
-  const int kchunk = 512;
-  dim3 g2((K.nq + 127) / 128, (K.nk + kchunk - 1) / kchunk);
-  size_t shm2 = kchunk * sizeof(int4) + kchunk * 6 * rsz;
-  if (s.mixed) k_ks_force<true><<<g2, 128, shm2, st>>>(s, C, K, kchunk, 8. * pi);
-  else k_ks_force<false><<<g2, 128, shm2, st>>>(s, C, K, kchunk, 8. * pi);
+  dim3 g2((K.nq + 127) / 128, K.nkchunks);
+  size_t shm2 = K.kchunk * sizeof(int4) + K.kchunk * 6 * rsz;
+  if (s.mixed) k_ks_force<true><<<g2, 128, shm2, st>>>(s, C, K, K.kchunk, 8. * pi);
+  else k_ks_force<false><<<g2, 128, shm2, st>>>(s, C, K, K.kchunk, 8. * pi);
+  k_ks_force_sum<<<(K.nq + 127) / 128, 128, 0, st>>>(s, C, K, 8. * pi, fused && s.mixed);
 }
 
 __global__ void __launch_bounds__(1024) k_ks_dipole(DevState s, SimConst C, KSpace K, double pi, Acc acc, bool eflag) {
@@ -214,18 +237,21 @@ __global__ void __launch_bounds__(1024) k_ks_dipole(DevState s, SimConst C, KSpa
   }
 }
 
-__global__ void k_ks_dipole_force(DevState s, SimConst C, KSpace K, double pi) {
+__global__ void k_ks_dipole_force(DevState s, SimConst C, KSpace K, double pi, bool to_f4) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= K.nq) return;
   int i = s.slot_of_tag[K.qtag[p]];
-  s.fz[i] -= 4. * pi * C.charge[info_type(s.info[i])] * K.mz[0] * K.inv_V;
+  const double f = -4. * pi * C.charge[info_type(s.info[i])] * K.mz[0] * K.inv_V;
+  if (to_f4) s.f4[i].z += (float)f;
+  else s.fz[i] += f;
 }
 
-void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc) {
+void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
+                    bool fused) {
   if (K.nq == 0) return;
   const double pi = (double)3.1415926536f;
   k_ks_dipole<<<1, 1024, 0, st>>>(s, C, K, pi, acc, eflag);
-  k_ks_dipole_force<<<(K.nq + 255) / 256, 256, 0, st>>>(s, C, K, pi);
+  k_ks_dipole_force<<<(K.nq + 255) / 256, 256, 0, st>>>(s, C, K, pi, fused && s.mixed);
 }
 
 }  // namespace mfa

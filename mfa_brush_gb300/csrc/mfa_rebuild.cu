@@ -292,16 +292,17 @@ __global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
           nseg = 2;
         }
         for (int g = 0; g < nseg; ++g) {
+          // unrolled so that several candidates' (consecutive) position loads are in flight
+#pragma unroll 4
           for (int j = sb[g]; j < se[g]; ++j) {
-            if (j == i) continue;
             int wj;
             bool hit;
             if (MIXED) {
               const int4 qj = s.pfx[j];
               wj = qj.w;
-              const float ddx = (float)fx_diff(qi.x, qj.x) * ux;
-              const float ddy = (float)fx_diff(qi.y, qj.y) * uy;
-              const float ddz = (float)fx_diff(qi.z, qj.z) * uz;
+              const float ddx = i2f_fast(fx_diff(qi.x, qj.x)) * ux;
+              const float ddy = i2f_fast(fx_diff(qi.y, qj.y)) * uy;
+              const float ddz = i2f_fast(fx_diff(qi.z, qj.z)) * uz;
               hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2f[ti * MAXT + info_type(wj)];
             } else {
               wj = s.info[j];
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
               const double ddz = z - s.rz[j];
               hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2d[ti * MAXT + info_type(wj)];
             }
-            if (hit) {
+            if (hit && j != i) {
               if (cnt < cap) mine[cnt] = j;
               ++cnt;
             }

@@ -17,6 +17,8 @@ struct DevState {
   double* tmp[9];
   int *tmp_tag, *tmp_info;
   int* slot_of_tag;
+  // FP32 force of the fused mixed-precision step (pair + bonded + k-space), read by the integrator
+  float4* f4;
   // pair-kernel views
   int4* pfx;
   float4* vf;
@@ -56,7 +58,8 @@ constexpr int NL_CAP_MAX = 420;
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag,
                  Acc acc, int block);
 // bonded terms: mask bit 1 FENE, 2 brush bending, 4 melt bending, 8 orientation
-void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc);
+void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc,
+                   bool fused = false);
 // implicit 9-3 walls (fluid_wall 2) and constant body force (constant_force 1)
 void launch_wall(const DevState& s, const SimConst& C, cudaStream_t st, bool eflag, Acc acc);
 void launch_const_force(const DevState& s, const SimConst& C, cudaStream_t st);
@@ -95,10 +98,15 @@ struct KSpace {
   double cx, cy, cz;    // dk/(2 pi) per axis
   double inv_V, lz_half;
   double* mz;           // [1] dipole moment M_z
+  double* fpart;        // [kchunks][nq][3] per-k-chunk force partials, summed in a fixed order
+  int kchunk, nkchunks;
   int rep;
 };
-void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc);
-void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc);
+// fused: the mixed-precision fused step adds into the FP32 force array, otherwise into FP64
+void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
+                   bool fused = false);
+void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
+                    bool fused = false);
 
 // implicit 9-3 walls (fluid_wall.f90:93-121): returns F_z, e = energy of both walls
 __device__ __forceinline__ double wall93(const SimConst& C, int t, double z, double D, double& e) {

@@ -91,6 +91,25 @@ def test_fused_step_matches_drop_ins(gpu, try_deck):
     assert g2.step_index() == s.s_time + 7
 
 
+def test_try_steps_mixed(gpu, try_deck, oracle_mod):
+    """Ten fused mixed-precision steps against ten FP64 oracle steps (dt = 2e-4): positions within
+    1e-8 sigma, velocities within 1e-5 relative to their RMS, energies within 1e-5."""
+    inp, p, s, a_type, r0, v, a = try_deck
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, a, "mixed")
+    g.step(10)
+    o.step(10, 1, 0)
+    r, vv, aa, f = g.state()
+    ro, vo, ao, fo = o.state()
+    L = np.array(list(s.boundary))
+    d = r - ro
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < 1e-8
+    assert np.abs(vv - vo).max() < 1e-5 * np.sqrt(np.mean(vo ** 2))
+    eg, eo = g.energies()[0], o.energies()
+    for k in ("v_fluid_fluid", "v_intra_molec", "v_bend", "v_or", "v_fluid_wall", "t_fluid"):
+        assert rel(eg[k], eo[k]) < 1e-5, k
+
+
 @pytest.mark.parametrize("l_box", [1, 2])
 def test_reference_cell_list_bit_exact(gpu, try_deck, oracle_mod, l_box):
     """get_cell on the reference's own grid (make_binning with r_cut_max): identical cells."""
