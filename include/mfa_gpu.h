@@ -297,7 +297,9 @@ int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_
 int mfa_event_record(mfa_ctx* ctx, int32_t slot);
 int mfa_event_elapsed(mfa_ctx* ctx, int32_t slot_a, int32_t slot_b, float* ms);
 /* Runs nsteps un-graphed steps with events around each kernel family and returns the mean
-   device ms per launch and the launch count per family (names from mfa_kernel_name).        */
+   device ms per launch and the launch count per family (names from mfa_kernel_name).  Every
+   timed step rebuilds the cell sort and the lists, so the "rebuild" family is the cost of one
+   rebuild; mfa_step rebuilds only when the displacement test fires (mfa_rebuild_count).      */
 #define MFA_NKFAM 8
 int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* launches);
 const char* mfa_kernel_name(int32_t fam);

@@ -424,6 +424,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
         }
         e.flags = fl;
         e.rlist2 = rc > 0. ? (rc + skin) * (rc + skin) : 0.;
+        e.screen2 = rc * rc;
         if (rc > 0.) rl_max = std::max(rl_max, rc + skin);
       }
       td[k] = e;
@@ -431,6 +432,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       g.range2 = (float)e.range2; g.eps4 = (float)e.eps4; g.sig2 = (float)e.sig2; g.shift = (float)e.shift;
       g.inv_rc = (float)e.inv_rc; g.rlist2 = (float)e.rlist2; g.dpd_rc2 = (float)e.dpd_rc2;
       g.inv_dpd_rc = (float)e.inv_dpd_rc; g.qq = (float)e.qq; g.flags = e.flags;
+      g.screen2 = (float)(e.screen2 * 1.0002);
+      g.rlist2 = (float)(e.rlist2 * 1.0002);
     }
   if (rl_max <= 0.) rl_max = 1.0 + skin;
   ctx->rl_max = rl_max;
@@ -451,10 +454,11 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       R.sfx[d] = (d < 2) ? 4294967296.0 / s.boundary[d] : 1073741824.0 / s.boundary[d];
       R.ufx[d] = 1. / R.sfx[d];
       R.ufx_f[d] = (float)R.ufx[d];
-      int nc = (int)std::floor(s.boundary[d] / rl_max);
+      // list cells of at least half the list cut-off: the 5x5x5 stencil covers every neighbour
+      int nc = (int)std::floor(s.boundary[d] / (0.5 * rl_max));
       if (nc < 1) nc = 1;
-      if (d < 2 && nc < 3)
-        return fail(ctx, MFA_ERR_UNSUPPORTED, "box shorter than 3 list cells (3*(r_cut_max+skin)) in x or y");
+      if (d < 2 && nc < 5)
+        return fail(ctx, MFA_ERR_UNSUPPORTED, "box shorter than 2.5*(r_cut_max+skin) in x or y");
       R.nc[d] = nc;
       R.inv_lc[d] = (double)nc / s.boundary[d];
     }
@@ -1099,7 +1103,9 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
   mark(7);
   for (int k = 1; k <= nsteps; ++k) {
     const bool ef = (k == nsteps);
-    launch_rebuild(S, st, false);
+    // a rebuild on every step: the "rebuild" family is then the cost of one rebuild (the
+    // fused step runs it only on steps whose displacement test fires)
+    launch_rebuild(S, st, true);
     k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
     mark(0);
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);

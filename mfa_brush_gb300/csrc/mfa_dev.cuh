@@ -50,8 +50,17 @@ struct PairEntry {
   T rlist2;                             // (cut-off + skin)^2 for the neighbour list
   T dpd_rc2, inv_dpd_rc;                // own DPD cut-off (DPD_CUT_OFF)
   T qq;                                 // charge product (real-space Ewald)
+  T screen2;                            // largest interaction cut-off^2 (x 1.0002 in FP32): the
+                                        // pair kernel's screening threshold
   int flags;
 };
+
+// Coarse int32 -> float for screening only: the difference is shifted right by `sh` bits and
+// converted with one magic add (exact for |d >> sh| < 2^22); the result times 2^sh units is off
+// by at most 2^sh units, covered by the margin of PairEntry::screen2.
+__device__ __forceinline__ float i2f_coarse(int d, int sh) {
+  return __int_as_float(0x4B400000 + (d >> sh)) - 12582912.0f;
+}
 
 // Scalars shared by every replica (passed by value).
 struct SimConst {

@@ -29,7 +29,7 @@ __device__ __forceinline__ double r2min_of(const SimConst& C, long long step) {
 }
 
 template <bool MIXED, bool EFLAG>
-__global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accumulate, Acc acc) {
+__global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc) {
   using real = real_t<MIXED>;
   __shared__ PairEntry<real> tab[NPAIR];
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
@@ -96,13 +96,21 @@ __global__ void __launch_bounds__(128) k_pair(DevState s, SimConst C, bool accum
     constexpr int G = 4;  // list entries screened per group: their loads are all in flight at once
     int jl[BATCH];
     int k = 0;
+    // screening against the largest cut-off of the type pair; MIXED uses the coarse conversion
+    // (512 fixed-point units of resolution, inside the 2e-4 margin of screen2)
+    const float cx = ux * 512.f, cy = uy * 512.f, cz = uz * 512.f;
     auto screen = [&](int j) -> bool {
-      real dx, dy, dz;
-      const int wj = delta(j, dx, dy, dz);
-      const real r2raw = dx * dx + dy * dy + dz * dz;
-      const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
-      return r2raw < e.range2 || ((e.flags & PF_DPD_OWN) && r2raw < e.dpd_rc2) ||
-             ((e.flags & PF_COUL) && r2raw < coul_rc2);
+      if constexpr (MIXED) {
+        const int4 qj = __ldg(&s.pfx[j]);
+        const float dx = i2f_coarse(fx_diff(qi.x, qj.x), 9) * cx;
+        const float dy = i2f_coarse(fx_diff(qi.y, qj.y), 9) * cy;
+        const float dz = i2f_coarse(fx_diff(qi.z, qj.z), 9) * cz;
+        return dx * dx + dy * dy + dz * dz < tab[ti * MAXT + info_type(qj.w)].screen2;
+      } else {
+        real dx, dy, dz;
+        const int wj = delta(j, dx, dy, dz);
+        return dx * dx + dy * dy + dz * dz < tab[ti * MAXT + info_type(wj)].screen2;
+      }
     };
     while (k < n) {
       int m = 0;

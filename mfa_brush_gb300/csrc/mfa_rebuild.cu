@@ -261,35 +261,29 @@ __global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
       x = s.rx[i]; y = s.ry[i]; z = s.rz[i];
       cell_coords(R, x, y, z, ix, iy, iz);
     }
-    const float ux = R.ufx_f[0], uy = R.ufx_f[1], uz = R.ufx_f[2];
+    // coarse conversion (512 fixed-point units); rl2f carries a 2e-4 margin
+    const float ux = R.ufx_f[0] * 512.f, uy = R.ufx_f[1] * 512.f, uz = R.ufx_f[2] * 512.f;
     const int nx = R.nc[0];
-    const int xl = (ix == 0) ? nx - 1 : ix - 1, xr = (ix == nx - 1) ? 0 : ix + 1;
-    for (int dz = -1; dz <= 1; ++dz) {
+    // x-runs of the 5-cell row ix-2..ix+2: one contiguous slot range, or two when it wraps
+    int xa0, xb0, xa1 = 0, xb1 = -1;
+    if (ix - 2 < 0) { xa0 = 0; xb0 = ix + 2; xa1 = nx + ix - 2; xb1 = nx - 1; }
+    else if (ix + 2 >= nx) { xa0 = ix - 2; xb0 = nx - 1; xa1 = 0; xb1 = ix + 2 - nx; }
+    else { xa0 = ix - 2; xb0 = ix + 2; }
+    const int nseg = (xb1 >= xa1) ? 2 : 1;
+    for (int dz = -2; dz <= 2; ++dz) {
       const int cz = iz + dz;
       if (cz < 0 || cz >= R.nc[2]) continue;
-      for (int dy = -1; dy <= 1; ++dy) {
+      for (int dy = -2; dy <= 2; ++dy) {
         int cy = iy + dy;
         cy += (cy < 0) ? R.nc[1] : 0;
         cy -= (cy >= R.nc[1]) ? R.nc[1] : 0;
         const int row = R.cell_off + (cz * R.nc[1] + cy) * nx;
-        // segments of the row: [xl..xr] without wrap, else {xl} + [ix..xr] or [xl..ix] + {xr}
-        int sb[2], se[2], nseg;
-        if (xl < xr) {
-          sb[0] = s.cell_start[row + xl];
-          se[0] = s.cell_start[row + xr] + s.cell_count[row + xr];
-          nseg = 1;
-        } else if (ix == 0) {
-          sb[0] = s.cell_start[row + ix];
-          se[0] = s.cell_start[row + xr] + s.cell_count[row + xr];
-          sb[1] = s.cell_start[row + xl];
-          se[1] = sb[1] + s.cell_count[row + xl];
-          nseg = 2;
-        } else {
-          sb[0] = s.cell_start[row + xl];
-          se[0] = s.cell_start[row + ix] + s.cell_count[row + ix];
-          sb[1] = s.cell_start[row + xr];
-          se[1] = sb[1] + s.cell_count[row + xr];
-          nseg = 2;
+        int sb[2], se[2];
+        sb[0] = s.cell_start[row + xa0];
+        se[0] = s.cell_start[row + xb0] + s.cell_count[row + xb0];
+        if (nseg == 2) {
+          sb[1] = s.cell_start[row + xa1];
+          se[1] = s.cell_start[row + xb1] + s.cell_count[row + xb1];
         }
         for (int g = 0; g < nseg; ++g) {
           // unrolled so that several candidates' (consecutive) position loads are in flight
@@ -300,9 +294,9 @@ __global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
             if (MIXED) {
               const int4 qj = s.pfx[j];
               wj = qj.w;
-              const float ddx = i2f_fast(fx_diff(qi.x, qj.x)) * ux;
-              const float ddy = i2f_fast(fx_diff(qi.y, qj.y)) * uy;
-              const float ddz = i2f_fast(fx_diff(qi.z, qj.z)) * uz;
+              const float ddx = i2f_coarse(fx_diff(qi.x, qj.x), 9) * ux;
+              const float ddy = i2f_coarse(fx_diff(qi.y, qj.y), 9) * uy;
+              const float ddz = i2f_coarse(fx_diff(qi.z, qj.z), 9) * uz;
               hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2f[ti * MAXT + info_type(wj)];
             } else {
               wj = s.info[j];
