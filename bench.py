@@ -150,7 +150,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
-    ap.add_argument("--skin", type=float, default=0.3)
+    ap.add_argument("--skin", type=float, default=0.5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)

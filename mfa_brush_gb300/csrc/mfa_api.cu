@@ -461,6 +461,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
         return fail(ctx, MFA_ERR_UNSUPPORTED, "box shorter than 2.5*(r_cut_max+skin) in x or y");
       R.nc[d] = nc;
       R.inv_lc[d] = (double)nc / s.boundary[d];
+      R.lc_f[d] = (float)(s.boundary[d] / nc);
+      R.cpu_f[d] = (float)(512. * nc / ((d < 2) ? 4294967296.0 : 1073741824.0));
     }
     R.ncell = R.nc[0] * R.nc[1] * R.nc[2];
     R.cell_off = cell_off;

@@ -92,6 +92,8 @@ struct RepDesc {
   double ufx[3];        // sigma per fixed-point unit
   float ufx_f[3];
   double inv_lc[3];     // neighbour-list grid
+  float lc_f[3];        // list cell edge in sigma
+  float cpu_f[3];       // list cells per 512 fixed-point units
   int nc[3];
   int cell_off, ncell;
   int p0, n_part, n_mon_tot;

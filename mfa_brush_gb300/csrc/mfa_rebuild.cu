@@ -219,26 +219,35 @@ __global__ void k_copyback(DevState s, bool force) {
 }
 
 // Full Verlet list: every mobile particle lists all j (mobile or wall) with r^2 < (rc_ij+skin)^2.
-// One thread per particle.  The 27 surrounding cells are walked as 9 x-rows: the three cells of a
-// row are consecutive in the sorted order unless the row wraps in x, so a row is one contiguous
-// slot range (two when it wraps).  Each thread stages its list in shared memory (row stride
+// One thread per particle.  Cells are at least half the list cut-off wide, and the 5x5x5 cells
+// around a particle are walked as 25 x-rows: the cells of a row are consecutive in the sorted
+// order unless the row wraps in x, so a row is one contiguous slot range (two when it wraps).
+// Rows whose y/z distance from the particle exceeds the largest list cut-off of its type are
+// skipped, and each kept row is trimmed in x to the cells within that cut-off, which removes
+// about half of the candidates.  Each thread stages its list in shared memory (row stride
 // cap|1 keeps the banks distinct) and the block writes the list out row by row: the k-th
 // neighbours of 128 consecutive particles are 128 consecutive ints of nbr, so every store is
 // coalesced (scattered 4-byte stores into the column-major list cost read-modify-writes in HBM).
 constexpr int NL_BLOCK = 128;
 
 template <bool MIXED>
-__global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
+__global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
   extern __shared__ int nl_sh[];
   __shared__ float rl2f[NPAIR];
   __shared__ double rl2d[NPAIR];
+  __shared__ float rlmax[MAXT];
   __shared__ int blk_max;
   const int cap = s.nbr_cap, pitch = cap | 1;
   int* mine = nl_sh + threadIdx.x * pitch;
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
     rl2d[k] = s.tabd[k].rlist2;
     rl2f[k] = s.tabf ? s.tabf[k].rlist2 : 0.f;
+  }
+  if (threadIdx.x < MAXT) {  // largest list cut-off of each type, with the culling margin
+    double m = 0.;
+    for (int t = 0; t < MAXT; ++t) m = fmax(m, s.tabd[threadIdx.x * MAXT + t].rlist2);
+    rlmax[threadIdx.x] = (float)m * 1.0004f;
   }
   if (threadIdx.x == 0) blk_max = 0;
   __syncthreads();
@@ -264,26 +273,54 @@ __global__ void __launch_bounds__(NL_BLOCK) k_nlist(DevState s, bool force) {
     // coarse conversion (512 fixed-point units); rl2f carries a 2e-4 margin
     const float ux = R.ufx_f[0] * 512.f, uy = R.ufx_f[1] * 512.f, uz = R.ufx_f[2] * 512.f;
     const int nx = R.nc[0];
-    // x-runs of the 5-cell row ix-2..ix+2: one contiguous slot range, or two when it wraps
-    int xa0, xb0, xa1 = 0, xb1 = -1;
-    if (ix - 2 < 0) { xa0 = 0; xb0 = ix + 2; xa1 = nx + ix - 2; xb1 = nx - 1; }
-    else if (ix + 2 >= nx) { xa0 = ix - 2; xb0 = nx - 1; xa1 = 0; xb1 = ix + 2 - nx; }
-    else { xa0 = ix - 2; xb0 = ix + 2; }
-    const int nseg = (xb1 >= xa1) ? 2 : 1;
+    // Row culling and x trimming: a cell is skipped when its distance from the particle, taken
+    // from the cell edges, is beyond the largest list cut-off of the particle's type times 1.0004
+    // (the candidate test below has a 1.0002 margin; the coarse position is off by < 1e-5 sigma).
+    // (no FP64 and no conversion instructions here: both run on the slow FP64 pipe)
+    float px, py, pz;  // position in cell units
+    if (MIXED) {
+      px = (__int_as_float(0x4B000000 | ((unsigned)qi.x >> 9)) - 8388608.0f) * R.cpu_f[0];
+      py = (__int_as_float(0x4B000000 | ((unsigned)qi.y >> 9)) - 8388608.0f) * R.cpu_f[1];
+      pz = i2f_coarse(qi.z, 9) * R.cpu_f[2];
+    } else {
+      px = (float)(x * R.inv_lc[0]);
+      py = (float)(y * R.inv_lc[1]);
+      pz = (float)(z * R.inv_lc[2]);
+    }
+    const float lx = R.lc_f[0], ly = R.lc_f[1], lz = R.lc_f[2];
+    const float rl2max = rlmax[ti];
+    auto fl = [](int v) { return i2f_coarse(v, 0); };  // exact for small integers
+    auto gap2 = [](float d, float l) {  // squared gap of d cell widths (0 when the particle is past the edge)
+      d = fmaxf(d, 0.f) * l;
+      return d * d;
+    };
+    const float gxp1 = gap2(fl(ix + 1) - px, lx), gxp2 = gap2(fl(ix + 2) - px, lx);
+    const float gxm1 = gap2(px - fl(ix), lx), gxm2 = gap2(px - fl(ix - 1), lx);
     for (int dz = -2; dz <= 2; ++dz) {
       const int cz = iz + dz;
       if (cz < 0 || cz >= R.nc[2]) continue;
+      const float rz2 = rl2max - ((dz > 0) ? gap2(fl(cz) - pz, lz) : (dz < 0 ? gap2(pz - fl(cz + 1), lz) : 0.f));
       for (int dy = -2; dy <= 2; ++dy) {
         int cy = iy + dy;
+        const float rem2 = rz2 - ((dy > 0) ? gap2(fl(cy) - py, ly) : (dy < 0 ? gap2(py - fl(cy + 1), ly) : 0.f));
+        if (rem2 <= 0.f) continue;  // the whole row is beyond the list cut-off
+        const int xa = ix - (gxm1 < rem2) - (gxm2 < rem2), xb = ix + (gxp1 < rem2) + (gxp2 < rem2);
         cy += (cy < 0) ? R.nc[1] : 0;
         cy -= (cy >= R.nc[1]) ? R.nc[1] : 0;
         const int row = R.cell_off + (cz * R.nc[1] + cy) * nx;
+        // x-runs of cells xa..xb: one contiguous slot range, or two when the row wraps; the
+        // scan has one entry past the last cell, so cell_start[c + 1] ends cell c
+        int xa0, xb0, xa1 = 0, xb1 = -1;
+        if (xa < 0) { xa0 = 0; xb0 = xb; xa1 = nx + xa; xb1 = nx - 1; }
+        else if (xb >= nx) { xa0 = xa; xb0 = nx - 1; xa1 = 0; xb1 = xb - nx; }
+        else { xa0 = xa; xb0 = xb; }
+        const int nseg = (xb1 >= xa1) ? 2 : 1;
         int sb[2], se[2];
         sb[0] = s.cell_start[row + xa0];
-        se[0] = s.cell_start[row + xb0] + s.cell_count[row + xb0];
+        se[0] = s.cell_start[row + xb0 + 1];
         if (nseg == 2) {
           sb[1] = s.cell_start[row + xa1];
-          se[1] = s.cell_start[row + xb1] + s.cell_count[row + xb1];
+          se[1] = s.cell_start[row + xb1 + 1];
         }
         for (int g = 0; g < nseg; ++g) {
           // unrolled so that several candidates' (consecutive) position loads are in flight
@@ -336,12 +373,14 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   const int B = 256;
   int gN = (s.N + B - 1) / B;
   int gC = (s.ncell_tot + B - 1) / B;
-  int nb = (s.ncell_tot + 1023) / 1024;
-  k_zero_counts<<<min(gC, 4096), B, 0, st>>>(s.ncell_tot, s.cell_count, s.rebuild_flag, force);
+  // counts and scan run one entry past the last cell, so that cell_start[c + 1] ends every cell c
+  const int nc1 = s.ncell_tot + 1;
+  int nb = (nc1 + 1023) / 1024;
+  k_zero_counts<<<min((nc1 + B - 1) / B, 4096), B, 0, st>>>(nc1, s.cell_count, s.rebuild_flag, force);
   k_bin<<<gN, B, 0, st>>>(s, force);
-  k_scan_local<<<nb, 1024, 0, st>>>(s.ncell_tot, s.cell_count, s.cell_start, s.scan_blk, s.rebuild_flag, force);
+  k_scan_local<<<nb, 1024, 0, st>>>(nc1, s.cell_count, s.cell_start, s.scan_blk, s.rebuild_flag, force);
   k_scan_blocks<<<1, 1024, 0, st>>>(nb, s.scan_blk, s.rebuild_flag, force);
-  k_scan_add<<<nb, 1024, 0, st>>>(s.ncell_tot, s.cell_start, s.scan_blk, s.rebuild_flag, force);
+  k_scan_add<<<nb, 1024, 0, st>>>(nc1, s.cell_start, s.scan_blk, s.rebuild_flag, force);
   k_place<<<gN, B, 0, st>>>(s, force);
   k_sort_cells<<<gC, B, 0, st>>>(s, force);
   k_permute<<<gN, B, 0, st>>>(s, force);
