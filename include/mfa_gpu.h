@@ -291,6 +291,14 @@ int mfa_cell_neigh_list(const int32_t* n_cells, int32_t n_nei, int32_t* out);
 /* All interacting pairs (r^2 < range_2, or inside the DPD cut-off where DPD applies) of
    replica rep as 0-based caller-order index pairs i<j; *n = count (may exceed cap).          */
 int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n);
+/* No counterpart in the reference.  mfa_pair_list that takes no device memory from the
+   allocator: for callers that cannot allocate device memory at the point of the call (a host
+   program that has handed the device's memory to another component or pool).  The pairs are
+   staged in a fixed device array of MFA_PAIR_LIST_STATIC_MAX pairs; cap above that returns
+   MFA_ERR_CAPACITY.  The first call on a device looks the array up (make it before any stream
+   capture); calls that overlap on one device share the array and race.                      */
+#define MFA_PAIR_LIST_STATIC_MAX 262144
+int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n);
 
 /* ---- timing ---------------------------------------------------------------------------- */
 /* Records CUDA event `slot` (0..15) on the context stream / elapsed ms between two slots. */

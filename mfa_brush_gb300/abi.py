@@ -148,6 +148,7 @@ SIGNATURES = {
     "mfa_cell_list": (i32, [vp, i32, i32, ip, ip, i32, ip]),
     "mfa_cell_neigh_list": (i32, [ip, i32, ip]),
     "mfa_pair_list": (i32, [vp, i32, ip, i64, P(i64)]),
+    "mfa_pair_list_static": (i32, [vp, i32, ip, i64, P(i64)]),
     "mfa_event_record": (i32, [vp, i32]),
     "mfa_event_elapsed": (i32, [vp, i32, i32, P(C.c_float)]),
     "mfa_kernel_times": (i32, [vp, i32, P(C.c_float), ip]),

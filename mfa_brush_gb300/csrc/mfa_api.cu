@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -1063,6 +1064,61 @@ int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_
   CK(cudaFreeAsync(dp, ctx->st));
   CK(cudaFreeAsync(dc, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
+  return MFA_OK;
+}
+
+// ---- mfa_pair_list without device allocation -----------------------------------------------
+// Same result as mfa_pair_list, staged in file-scope device arrays instead of memory taken from
+// the allocator: MFA_PAIR_LIST_STATIC_MAX pairs and one counter.  Their device addresses are
+// looked up once per device, on the first call made with that device (the lookup may load this
+// module, so the first call must come before any stream capture).  Every call shares the same
+// scratch: two calls that overlap on one device race.
+static __device__ __align__(256) int g_static_pairs[2 * MFA_PAIR_LIST_STATIC_MAX];
+static __device__ __align__(256) unsigned long long g_static_count;
+
+namespace {
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+int* g_static_pairs_at[kStaticMaxDevices] = {};
+unsigned long long* g_static_count_at[kStaticMaxDevices] = {};
+}  // namespace
+
+int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n) {
+  if (!ctx || rep < 0 || rep >= ctx->nrep || !n || cap < 0) return MFA_ERR_ARG;
+  if (cap > MFA_PAIR_LIST_STATIC_MAX)
+    return fail(ctx, MFA_ERR_CAPACITY,
+                "cap above MFA_PAIR_LIST_STATIC_MAX (" + std::to_string(MFA_PAIR_LIST_STATIC_MAX) +
+                    " pairs): use mfa_pair_list");
+  const int dev = ctx->device;
+  if (dev < 0 || dev >= kStaticMaxDevices) return fail(ctx, MFA_ERR_ARG, "device index out of range");
+  CK(cudaSetDevice(dev));
+  int* dp = nullptr;
+  unsigned long long* dc = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_pairs_at[dev]) {
+      void* a = nullptr;
+      void* b = nullptr;
+      CK(cudaGetSymbolAddress(&a, g_static_pairs));
+      CK(cudaGetSymbolAddress(&b, g_static_count));
+      g_static_pairs_at[dev] = static_cast<int*>(a);
+      g_static_count_at[dev] = static_cast<unsigned long long*>(b);
+    }
+    dp = g_static_pairs_at[dev];
+    dc = g_static_count_at[dev];
+  }
+  CK(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), ctx->st));  // the pair counter starts at zero
+  launch_pair_list(ctx->S, ctx->C, ctx->st, rep, dp, cap, dc);
+  ctx->launches += 1;
+  unsigned long long hc = 0;
+  CK(cudaMemcpyAsync(&hc, dc, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  *n = (int64_t)hc;
+  if (pairs && cap > 0) {
+    CK(cudaMemcpyAsync(pairs, dp, sizeof(int) * 2 * std::min<int64_t>(cap, (int64_t)hc), cudaMemcpyDeviceToHost,
+                       ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
   return MFA_OK;
 }
 
