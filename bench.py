@@ -32,9 +32,23 @@ sys.path.insert(0, ROOT)
 METRIC = "atom-steps/s on 1 GB300: batched FP32-force vs plain FP64 (force rel err<=1e-5)"
 UNIT = "atom-steps/s"
 CHUNK = 10
-# algorithmic bytes per particle of the pair kernel (mixed): int4 position + float4 velocity in,
-# three FP64 force components out
-PAIR_BYTES = {"mixed": 16 + 16 + 24, "fp64": 32 + 32 + 24}
+# algorithmic bytes per particle of the pair kernel: mixed -- int4 fixed-point position and float4
+# velocity in, float4 force out; fp64 -- double4 position and velocity in, three doubles out (the
+# neighbour list itself, 4 B per entry, is not counted)
+PAIR_BYTES = {"mixed": 16 + 16 + 16, "fp64": 32 + 32 + 24}
+
+
+def profiled_traffic(precision, n_atoms):
+    """DRAM bytes of one pair-kernel launch, scaled to n_atoms from the committed ncu summary
+    (`traffic_bytes_per_particle:` line of profiles/k_pair_<precision>_brush_replicas.md)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "k_pair_%s_brush_replicas.md" % precision)) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_particle:"):
+                    return float(ln.split(":")[1]) * n_atoms
+    except OSError:
+        pass
+    return None
 
 
 def peaks():
@@ -111,6 +125,27 @@ def cpu_sample(reps, p, steps, warmup, threads):
     return tot_n / tot_t, tot_n, tot_t
 
 
+def plain_fp64(reps, p, skin, device, every=16, steps=100, warmup=20):
+    """The plain FP64 step on replicas run one at a time (every `every`-th replica of the set):
+    atom-steps/s over the sample, each replica timed with CUDA events on its own stream."""
+    from mfa_brush_gb300 import md
+    tot_n, tot_t, picked = 0, 0.0, 0
+    for (s, a_type, r0, v) in reps[::every]:
+        g = md.MdSystem(p, s, a_type, r0, v, precision="fp64", device=device, skin=skin)
+        for _ in range(warmup // CHUNK):
+            g.step(CHUNK)
+        g.synchronize()
+        g.event_record(0)
+        for _ in range(steps // CHUNK):
+            g.step(CHUNK)
+        g.event_record(1)
+        tot_t += g.event_elapsed(0, 1) / 1000.0
+        tot_n += s.n_part * steps
+        picked += 1
+        g.close()
+    return tot_n / tot_t, picked, tot_n // steps
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -149,6 +184,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
     ap.add_argument("--skin", type=float, default=0.5)
     args = ap.parse_args()
@@ -234,11 +270,19 @@ def main():
             "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None, "kernel": "k_pair (mixed)",
+                         "frac": achieved / hbm, "traffic": profiled_traffic(args.precision, n_atoms),
+                         "kernel": "k_pair (%s)" % args.precision,
                          "peak_kind": peak_kind},
             "clocks": clocks}
     if e2e is not None:
         line["e2e"] = e2e
+    if rank == 0 and not args.no_fp64:
+        # spec comparison: the same kind of replicas advanced one at a time in plain FP64
+        fv, fk, fn = plain_fp64(reps, p, args.skin, local)
+        line["plain_fp64_one_at_a_time"] = {
+            "value": fv, "unit": UNIT, "replicas": fk, "particles": int(fn), "steps": 100,
+            "sample": "every 16th replica of the set, each alone in its own FP64 context, 10-step graphs",
+            "speedup_of_value": value / world / fv}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         sample, n = [], 0
