@@ -198,6 +198,8 @@ def main():
     if world > 1:
         import torch
         import torch.distributed as dist
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
         r = run_reference(args, rank, world)
@@ -205,10 +207,13 @@ def main():
             dist.destroy_process_group()
         return r
 
-    from mfa_brush_gb300 import build, md
+    from mfa_brush_gb300 import build, md, shard
     build.build()
-    p, reps = make_workload(args.seed + 7919 * rank, args.replicas)
+    # weak scaling: a global set of replicas x world replicas, split by atom count; rank r
+    # generates and runs only its share (the whole set when world == 1)
     from mfa_brush_gb300 import configs
+    p = configs.wca_params(gamma=5.0, kT=1.0, dt=0.005)
+    rep_idx, reps = shard.rank_replicas(args.replicas, args.seed, rank, world)
     systems, a_type, r0, v = configs.concat(reps)
     n_atoms = int(sum(s.n_part for s in systems))
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin)
@@ -239,12 +244,14 @@ def main():
     launches = g.launch_count() - l0
     rebuilds = g.rebuild_count() - rb0
     t = ms / 1000.0
-    if dist is not None:
-        import torch
-        tt = torch.tensor([t], dtype=torch.float64, device="cuda:%d" % local if torch.cuda.is_available() else "cpu")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = n_atoms * world * args.steps / t
+    # the slowest rank's time; the atom count and per-replica energies of every rank (the one
+    # end-of-run gather: E/N of each replica of the global set, in global order, on rank 0)
+    dev = "cuda:%d" % local
+    t = shard.max_over_ranks(t, dist, dev)
+    e_rows = [[e["e_total"] * e["inv_n"], float(s.n_part)] for e, s in zip(g.energies(), systems)]
+    e_all = shard.gather_per_replica(e_rows, rep_idx, args.replicas * world, dist)
+    n_all = int(e_all[:, 1].sum()) if e_all is not None else n_atoms * world
+    value = n_all * args.steps / t
 
     # per-kernel device times (un-graphed, events around each kernel family)
     kt = g.kernel_times(args.kernel_steps)
@@ -255,14 +262,17 @@ def main():
     # end-to-end through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(g, n_atoms, args, world, dist)
+        e2e = run_e2e(g, n_atoms, n_all, args, dist)
 
+    if e_all is not None and not np.all(np.isfinite(e_all[:, 0])):
+        raise RuntimeError("non-finite replica energy after the timed steps")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded brush channels)",
             "config": {"workload": "256 uneven brush-channel replicas, WCA+FENE+DPD, batched",
-                       "replicas": len(systems) * world, "particles_per_gpu": n_atoms,
+                       "replicas": args.replicas * world, "particles_per_gpu": n_atoms,
+                       "particles_total": n_all, "seed": args.seed,
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
@@ -303,7 +313,7 @@ def main():
     return 0
 
 
-def run_e2e(g, n_atoms, args, world, dist):
+def run_e2e(g, n_atoms, n_all, args, dist):
     import torch
     from mfa_brush_gb300 import abi
     shape = (n_atoms, 3)
@@ -328,13 +338,11 @@ def run_e2e(g, n_atoms, args, world, dist):
         abi.check(lib.mfa_sync_to_host(g.ctx, dp(hr), dp(hv), dp(ha), None), g.ctx)  # D2H
         abi.check(lib.mfa_get_energies(g.ctx, e), g.ctx)
     t = time.perf_counter() - t0
-    if dist is not None:
-        tt = torch.tensor([t], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    from mfa_brush_gb300 import shard
+    t = shard.max_over_ranks(t, dist, "cuda:%d" % torch.cuda.current_device() if torch.cuda.is_available() else "cpu")
     steps = chunks * CHUNK
     bytes_state = 3 * 3 * 8 * n_atoms
-    return {"value": n_atoms * world * steps / t, "unit": UNIT,
+    return {"value": n_all * steps / t, "unit": UNIT,
             "h2d_bytes_per_step": bytes_state // CHUNK,
             "d2h_bytes_per_step": (bytes_state + g.nrep * 104) // CHUNK,
             "steps": steps, "pattern": "per 10-step chunk: r,v,a H2D (mfa_set_state) + mfa_step(10) + "

@@ -238,12 +238,14 @@ def draw_replica_shapes(n_rep, seed, rho=0.8, max_brush_frac=0.7):
     return out
 
 
-def replicas(n_rep=256, seed=2024, rho=0.8, shapes=None):
+def replicas(n_rep=256, seed=2024, rho=0.8, shapes=None, indices=None):
     """The batched workload: list of (System, a_type, r0, v), one per replica.  A lattice walk
-    that traps itself is regrown from the next sub-seed (deterministic for a given seed)."""
+    that traps itself is regrown from the next sub-seed (deterministic for a given seed).
+    `indices` builds only those replicas of the set (each seeded by its index in the set)."""
     shapes = shapes or draw_replica_shapes(n_rep, seed, rho)
     reps = []
-    for k, (sg, N, D, L) in enumerate(shapes):
+    for k in (range(len(shapes)) if indices is None else indices):
+        sg, N, D, L = shapes[k]
         for attempt in range(50):
             try:
                 reps.append(brush_channel(L, D, sg, N, rho=rho, seed=(seed * 100003 + k) * 64 + attempt))
