@@ -50,9 +50,12 @@ def _lattice(L, D, n_sites_min, z_lo=Z_LO):
 
 
 def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=None, kT=1.0,
-                  solvent_type=3, melt_type=3, max_fill=0.97):
+                  solvent_type=3, melt_type=3, max_fill=0.97, z_lo=Z_LO, wall_spacing=0.0, wall_type=4):
     """One replica: returns (abi.System, a_type[n], r0[n,3], v[n,3]).  Types are the reference's:
-    1 head, 2 brush bead, 3 melt/solvent."""
+    1 head, 2 brush bead, 3 melt/solvent.  wall_spacing > 0 appends explicit wall beads (type
+    wall_type, at rest) on a square lattice of that spacing at z = 0 and z = D, after the mobile
+    particles as in the reference (init_system.f90:172-187; gen_wall.f90 uses two beads per
+    lattice cell, this generator one)."""
     rng = np.random.default_rng(seed)
     n_chain = 2 * int(round(sigma_g * L * L))
     n_brush = n_chain * n_mon
@@ -61,7 +64,7 @@ def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=No
         n_chain_d = max(0, (n_total - n_brush) // n_mon_d)
     n_melt = n_chain_d * n_mon_d
     n = n_brush + n_melt
-    nx, nz, ax, az = _lattice(L, D, int(np.ceil((n - n_chain) / max_fill)))
+    nx, nz, ax, az = _lattice(L, D, int(np.ceil((n - n_chain) / max_fill)), z_lo)
     occ = np.zeros((nx, nx, nz), bool)
     # the first and last layer hold the brush heads only; no other bead may enter them
     occ[:, :, 0] = True
@@ -170,7 +173,7 @@ def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=No
     r0 = np.empty((n, 3))
     r0[:, 0] = (sites[:, 0] + 0.5) * ax
     r0[:, 1] = (sites[:, 1] + 0.5) * ax
-    r0[:, 2] = Z_LO + sites[:, 2] * az
+    r0[:, 2] = z_lo + sites[:, 2] * az
     a_type = np.full(n, solvent_type if n_mon_d == 1 else melt_type, np.int32)
     if n_chain:
         a_type[:n_brush] = 2
@@ -178,27 +181,41 @@ def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=No
     v = rng.normal(0.0, np.sqrt(kT), size=(n, 3))
     if n_chain:
         v[0:n_brush:n_mon] = 0.0
+    n_mob = n
+    if wall_spacing > 0:
+        m = max(1, int(round(L / wall_spacing)))
+        g = np.arange(m) * (L / m)
+        gx, gy = np.meshgrid(g, g, indexing="ij")
+        layer = np.stack([gx.ravel(), gy.ravel(), np.zeros(m * m)], 1)
+        top = layer.copy()
+        top[:, 2] = D
+        r0 = np.concatenate([r0, layer, top])
+        a_type = np.concatenate([a_type, np.full(2 * m * m, wall_type, np.int32)])
+        v = np.concatenate([v, np.zeros((2 * m * m, 3))])
+        n = len(r0)
     s = abi.System()
     s.boundary[0] = s.boundary[1] = L
     s.boundary[2] = D
     s.n_mon, s.n_chain = n_mon, n_chain
     s.n_mon_d, s.n_chain_d = n_mon_d, n_chain_d
     s.n_mon_e = s.n_chain_e = 0
-    s.n_mon_tot = s.n_part = n
+    s.n_mon_tot = n_mob
+    s.n_part = n
     s.s_time = 1
     s.seed = int(rng.integers(1, 2**63 - 1))
     return s, a_type, r0, v
 
 
 def wca_inputs(gamma=5.0, kT=1.0, dt=0.005, a_w=-3.2, sigma_w=1.0, k_chain=30.0, r_chain=1.5,
-               bending=False, k_bend=0.0, thermostat=0):
+               bending=False, k_bend=0.0, thermostat=0, wall=2, dpd_cut_off=0.0):
     """abi.Inputs of the WCA + FENE + DPD brush model expressed with the reference's own switches:
-    SYSTEM 0, WALL 2 (repulsive 9-3 walls, A_w < 0), SOLVENT 1 (every pair cut at 2^(1/6) sigma),
-    DPD inside the LJ cut-off with gamma = friction(1)."""
+    SYSTEM 0, WALL 2 (repulsive 9-3 walls, A_w < 0) or WALL 1 (explicit wall beads, type 4),
+    SOLVENT 1 (every pair cut at 2^(1/6) sigma), DPD inside the LJ cut-off (dpd_cut_off 0) or with
+    its own cut-off (DPD_CUT_OFF), gamma = friction(1)."""
     inp = abi.Inputs()
     f = inp.flags
-    f.system, f.symmetry, f.wall, f.solvent = 0, 0, 2, 1
-    f.thermostat, f.dpd_weight, f.dpd_cut_off = thermostat, 0, 0.0
+    f.system, f.symmetry, f.wall, f.solvent = 0, 0, wall, 1
+    f.thermostat, f.dpd_weight, f.dpd_cut_off = thermostat, 0, dpd_cut_off
     f.bending = 1 if bending else 0
     f.bin_type, f.l_box = 2, 1
     inp.dt, inp.temp = dt, kT
@@ -264,6 +281,14 @@ def concat(reps):
     r0 = np.concatenate([r[2] for r in reps])
     v = np.concatenate([r[3] for r in reps])
     return systems, a_type, r0, v
+
+
+def explicit_wall_channel(seed=1, L=20.0, D=20.0):
+    """The plain-FP64 reference-scale case: L x L x D channel with explicit wall beads on a 1 sigma
+    square lattice at z = 0 and z = D, grafting density 0.1 per wall (40 chains of 30 beads per
+    wall at L = 20), solvent to total density 0.8; bead layers start 1 sigma from the walls.
+    Use with wca_params(wall=1, dpd_cut_off=1.0)."""
+    return brush_channel(L, D, 0.1, 30, rho=0.8, seed=seed, z_lo=1.0, wall_spacing=1.0)
 
 
 def small_channel(seed=1):

@@ -35,6 +35,7 @@ struct mfa_ctx {
   double* prof = nullptr;
   long long n_obs = 0;
   std::vector<double> v_coul_self, v_ww;
+  std::vector<double> v_ff_walls;  // LJ energy of the fixed wall beads among themselves (WALL 1)
   KSpace K;
   bool kspace = false;
   unsigned* h_status = nullptr;  // pinned
@@ -177,8 +178,7 @@ void fill_energies(const mfa_ctx* ctx, const double* acc, int rep, mfa_energies*
   auto A = [&](int slot) { return acc[(size_t)slot * R + rep]; };
   std::memset(e, 0, sizeof *e);
   e->step = ctx->sys[rep].s_time + ctx->host_steps;
-  e->v_fluid_fluid = A(O_VFF);
-  if (ctx->P.flags.bin_type == 1) e->v_fluid_fluid *= 1.0;  // full-list sums are already single-counted
+  e->v_fluid_fluid = A(O_VFF) + ctx->v_ff_walls[rep];
   e->v_fluid_wall = A(O_VFW);
   e->v_wall_wall = ctx->v_ww[rep];
   e->v_intra_molec = A(O_VINTRA);
@@ -442,6 +442,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   ctx->hreps.resize(n_rep);
   ctx->v_coul_self.assign(n_rep, 0.);
   ctx->v_ww.assign(n_rep, 0.);
+  ctx->v_ff_walls.assign(n_rep, 0.);
   int cell_off = 0, p0 = 0;
   double dens_max = 0.;
   for (int r = 0; r < n_rep; ++r) {
@@ -490,6 +491,26 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     std::memcpy(&R.Lbits[1], &R.L[1], 8);
     p0 += s.n_part;
     dens_max = std::max(dens_max, (double)s.n_part / (s.boundary[0] * s.boundary[1] * D));
+    if (F.wall == 1) {
+      // Explicit walls: the reference's Verlet list holds every particle, wall beads included
+      // (binning.f90:25,56), so v_fluid_fluid also sums the wall-wall pairs (fluid_fluid.f90:61).
+      // The wall beads never move: that part is a constant, summed here once.
+      double vw = 0.;
+      for (int i = s.n_mon_tot; i < s.n_part; ++i)
+        for (int j = i + 1; j < s.n_part; ++j) {
+          const double* ri = r0 + 3 * (size_t)(R.p0 + i);
+          const double* rj = r0 + 3 * (size_t)(R.p0 + j);
+          double d[3] = {ri[0] - rj[0], ri[1] - rj[1], ri[2] - rj[2]};
+          for (int c = 0; c < 2; ++c) d[c] -= s.boundary[c] * std::nearbyint(d[c] / s.boundary[c]);
+          const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          const PairEntry<double>& e = td[(a_type[R.p0 + i] - 1) * MAXT + (a_type[R.p0 + j] - 1)];
+          if (r2 < e.range2) {
+            const double s2 = e.sig2 / r2, s6 = s2 * s2 * s2;
+            vw += e.eps4 * ((s6 * s6 - s6) - e.shift);
+          }
+        }
+      ctx->v_ff_walls[r] = vw;
+    }
     if (charged) {
       double vs = 0.;
       for (int t = 0; t < s.n_mon_tot; ++t) vs -= p->charge[a_type[R.p0 + t] - 1] * p->charge[a_type[R.p0 + t] - 1];
@@ -715,6 +736,8 @@ int mfa_fluid_fluid(mfa_ctx* ctx, double* v_ff, double* v_coul) {
   ctx->last_source = 2;
   if ((r = read_call_slot(ctx, O_VFF, v_ff, 0.))) return r;
   if ((r = read_call_slot(ctx, O_VCOUL, v_coul, ctx->C.charged ? 1. : 0.))) return r;
+  if (v_ff)
+    for (int k = 0; k < ctx->nrep; ++k) v_ff[k] += ctx->v_ff_walls[k];
   return MFA_OK;
 }
 

@@ -150,7 +150,8 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
         const real s6 = s2 * s2 * s2;
         const real s12 = s6 * s6;
         fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
-        if (EFLAG) e_lj += (real)0.5 * e.eps4 * ((s12 - s6) - e.shift);
+        // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
+        if (EFLAG) e_lj += (info_mobile(wj) ? (real)0.5 : (real)1) * e.eps4 * ((s12 - s6) - e.shift);
       }
       const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
       if (dpd) {
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
           const real r = sqrt(rc2), ir = (real)1 / r;
           const real qq = e.qq;
           const real ec = erfc((real)C.sqrt_alpha * r);
-          if (EFLAG) e_c += (real)0.5 * qq * ec * ir;
+          if (EFLAG) e_c += (info_mobile(wj) ? (real)0.5 : (real)1) * qq * ec * ir;
           fs += (qq * (real)C.sqrt_alpha * (real)C.inv_sqrt_pi * (real)2 * exp(-(real)C.alpha_c * rc2) * ir +
                  qq * ec * ir * ir) * ir;
         }

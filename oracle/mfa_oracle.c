@@ -18,6 +18,9 @@
  *   - DPD with its own cut-off reuses a stale 1/r in the reference for pairs outside the LJ
  *     range (fluid_fluid.f90:217-258 calls dpd_forces with inv_sqrt_r_2 from the last LJ pair);
  *     here 1/r of the current pair is used.
+ *   - Explicit walls (WALL 1): wall beads are in the cell list, as in the BIN_TYPE 0 Verlet list
+ *     (binning.f90:25,56); under BIN_TYPE 2 the reference lists mobile particles only and its
+ *     wall beads would not interact at all.
  *   - Reference defects with a compat bit (MFA_COMPAT_*): 1/pi for 1/sqrt(pi) in ewald_real,
  *     force on i only, Coulomb only inside the LJ cut-off.
  *
@@ -387,8 +390,11 @@ int orc_make_cell_list(orc_sys* o, int l_box) {
   o->part_in_cell = (int*)calloc((size_t)o->nct + 1, sizeof(int));
   o->cell_neigh_ls = (int*)malloc((size_t)o->nct * o->n_nei * sizeof(int));
   for (int i = 1; i <= o->n; ++i) o->r_nei[i] = o->l_nei[i] = 0;
-  /* the list covers the mobile particles only (init_config.f90:270) */
-  for (int i = 1; i <= o->nm; ++i) {
+  /* The linked-cell list covers the mobile particles only (init_config.f90:270), so under
+     BIN_TYPE 2 explicit wall beads never interact.  With explicit walls (WALL 1) the list takes
+     every particle, walls included, as the BIN_TYPE 0 Verlet list does (binning.f90:25,56). */
+  const int n_listed = (o->p.flags.wall == 1) ? o->n : o->nm;
+  for (int i = 1; i <= n_listed; ++i) {
     int pc = get_cell(o, &o->r0[3 * (i - 1)]);
     if (o->part_in_cell[pc] == 0) {
       o->part_in_cell[pc] = i;

@@ -74,6 +74,42 @@ def test_try_md_steps_fp64(gpu, try_deck, oracle_mod):
         assert rel(eg[k], eo[k]) < 1e-8, k
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_explicit_walls_fluid_fluid(gpu, oracle_mod, precision):
+    """WALL 1 (explicit wall beads on a 1 sigma lattice, DPD with its own 1 sigma cut-off): pair
+    forces on the mobile particles and the LJ energy, wall-wall pairs included."""
+    p = configs.wca_params(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    s, a_type, r0, v = configs.explicit_wall_channel(seed=3)
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, None, precision)
+    g.zero_force()
+    vff, _ = g.fluid_fluid()
+    o.zero_force()
+    o.fluid_fluid()
+    m = s.n_mon_tot
+    assert rel(vff[0], o.energies()["v_fluid_fluid"]) < TOL_E[precision]
+    assert_force_parity(g.state()[3][:m], o.state()[3][:m], precision)
+
+
+def test_explicit_walls_md_steps_fp64(gpu, oracle_mod):
+    """Five md_main iterations with explicit walls through the drop-ins vs the oracle."""
+    p = configs.wca_params(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    s, a_type, r0, v = configs.explicit_wall_channel(seed=4)
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, None, "fp64")
+    for _ in range(5):
+        eg = g.md_step()[0]
+    o.step(5, 1, 0)
+    r, vv, aa, f = g.state()
+    ro, vo, ao, fo = o.state()
+    L = np.array(list(s.boundary))
+    d = r - ro
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < 1e-9
+    assert np.abs(vv - vo).max() < 1e-7 * max(1.0, np.abs(vo).max())
+    eo = o.energies()
+    for k in ("v_fluid_fluid", "v_intra_molec", "t_fluid"):
+        assert rel(eg[k], eo[k]) < 1e-8, k
+
+
 def test_fused_step_matches_drop_ins(gpu, try_deck):
     """mfa_step(n) (graph-captured, fused integrator) reproduces n per-routine md_main steps."""
     inp, p, s, a_type, r0, v, a = try_deck

@@ -84,3 +84,16 @@ def test_pair_gauss_is_symmetric_and_normal(oracle_mod):
     g = np.array([oracle_mod.pair_gauss(7, 11, i, i + 1 + (i % 13)) for i in range(20000)])
     assert oracle_mod.pair_gauss(7, 11, 3, 9) == oracle_mod.pair_gauss(7, 11, 9, 3)
     assert abs(g.mean()) < 0.03 and abs(g.std() - 1) < 0.03
+
+
+def test_product_tables_equal_oracle_explicit_walls(oracle_mod):
+    """WALL 1 + DPD_CUT_OFF: the product's table derivation equals the oracle's."""
+    from mfa_brush_gb300 import configs, md
+    inp = configs.wca_inputs(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    p, _ = md.derive(inp)
+    po, _ = oracle_mod.derive_params(inp)
+    assert p.n_type == po.n_type == 4
+    for name in ("range_2", "inv_range_2", "e_shift", "epsil", "sigma", "sigma_2"):
+        assert np.array_equal(p.table(name), po.table(name)), name
+    for f in ("r_cut_max", "r_cut_dpd_2", "sig", "friction1", "skin"):
+        assert getattr(p, f) == getattr(po, f), f

@@ -117,3 +117,17 @@ def test_dpd_thermostat_temperature(oracle_mod):
     n_free = s.n_mon_tot - s.n_chain
     kT = 2 * np.mean(ts) / (3 * n_free)
     assert abs(kT - 1.0) < 0.06, kT
+
+
+def test_explicit_walls_cell_traversal_matches_n2(oracle_mod):
+    """WALL 1: wall beads are in the cell list (BIN_TYPE 0 semantics), so the cell traversal sums
+    the same LJ energy as the O(N^2) check over every particle, walls included."""
+    from mfa_brush_gb300 import configs
+    p = configs.wca_params(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    s, a_type, r0, v = configs.explicit_wall_channel(seed=3, L=10.0, D=10.0)
+    assert s.n_part > s.n_mon_tot
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    o.zero_force()
+    o.fluid_fluid()
+    e_cell, e_n2 = o.energies()["v_fluid_fluid"], o.check_fluid_fluid()
+    assert abs(e_cell - e_n2) <= 1e-12 * max(1.0, abs(e_n2))
