@@ -871,9 +871,10 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool cap
       k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
       L += 11;
     }
-    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
+    // mixed: bonded terms inside the pair kernel; FP64: their own kernel
+    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
     L += 1;
-    if (mask) { launch_bonded(S, C, st, mask, ef, acc, true); L += 1; }
+    if (mask && !S.mixed) { launch_bonded(S, C, st, mask, ef, acc, true); L += 1; }
     if (ctx->kspace) {
       launch_kspace(S, C, ctx->K, st, ef, acc, true);
       launch_dipolar(S, C, ctx->K, st, ef, acc, true);
@@ -1189,9 +1190,9 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
     launch_rebuild(S, st, true);
     k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
     mark(0);
-    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size);
+    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
     mark(1);
-    if (mask) { launch_bonded(S, C, st, mask, ef, acc, true); mark(2); }
+    if (mask && !S.mixed) { launch_bonded(S, C, st, mask, ef, acc, true); mark(2); }
     if (ctx->kspace) {
       launch_kspace(S, C, ctx->K, st, ef, acc, true);
       launch_dipolar(S, C, ctx->K, st, ef, acc, true);

@@ -28,8 +28,267 @@ __device__ __forceinline__ double r2min_of(const SimConst& C, long long step) {
   return (r_time < C.r2min_time) ? (1. - r_time / C.r2min_time) * C.r2min_init : 0.;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Bonded terms
+// ---------------------------------------------------------------------------------------------
+template <bool MIXED>
+struct BeadPos;
+template <>
+struct BeadPos<true> {
+  int4 q;
+  __device__ void load(const DevState& s, int slot) { q = __ldg(&s.pfx[slot]); }
+};
+template <>
+struct BeadPos<false> {
+  double x, y, z;
+  __device__ void load(const DevState& s, int slot) { x = s.rx[slot]; y = s.ry[slot]; z = s.rz[slot]; }
+};
+
+// a - b with the x,y minimum image
+template <bool MIXED>
+__device__ __forceinline__ void bead_delta(const BeadPos<MIXED>& a, const BeadPos<MIXED>& b, const RepDesc& R,
+                                           real_t<MIXED>* d) {
+  if constexpr (MIXED) {
+    d[0] = i2f_fast(fx_diff(a.q.x, b.q.x)) * R.ufx_f[0];
+    d[1] = i2f_fast(fx_diff(a.q.y, b.q.y)) * R.ufx_f[1];
+    d[2] = i2f_fast(fx_diff(a.q.z, b.q.z)) * R.ufx_f[2];
+  } else {
+    d[0] = mic_ref(a.x - b.x, R.L[0], R.invL[0]);
+    d[1] = mic_ref(a.y - b.y, R.L[1], R.invL[1]);
+    d[2] = a.z - b.z;
+  }
+}
+
+// One angle term of bending.f90:47-109 with r_prev = r_c - r_{c-1}, r_next = r_{c+1} - r_c.
+// fa acts on c-1, fc on c+1 (c gets -fa-fc).  MIXED computes the angle as atan2(|p x n|, p.n),
+// which keeps FP32 accurate for the nearly straight chains that stiff brushes produce.
+template <bool MIXED>
+__device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, const SimConst& C, real_t<MIXED> kb,
+                          real_t<MIXED> aeq, real_t<MIXED>* fa, real_t<MIXED>* fc, real_t<MIXED>& e) {
+  using real = real_t<MIXED>;
+  real dot = 0, rp2 = 0, rn2 = 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dot += rn[j] * rp[j];
+    rp2 += rp[j] * rp[j];
+    rn2 += rn[j] * rn[j];
+  }
+  real dn[3], dp[3], dn2 = 0, dp2 = 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dn[j] = rp[j] * rn2 - rn[j] * dot;
+    dp[j] = -rn[j] * rp2 + rp[j] * dot;
+    dn2 += dn[j] * dn[j];
+    dp2 += dp[j] * dp[j];
+  }
+  const real small = (real)C.bend_small;
+  const real srp = sqrt(rp2), srn = sqrt(rn2);
+  if (dn2 < small) {
+    real u[3], nu = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
+    nu = sqrt(nu);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dn[j] = (nu != 0) ? u[j] / nu / srn : (real)0;
+  } else {
+    const real sc = (real)1 / sqrt(dn2 * rn2);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dn[j] *= sc;
+  }
+  if (dp2 < small) {
+    real u[3], nu = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
+    nu = sqrt(nu);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dp[j] = (nu != 0) ? u[j] / nu / srp : (real)0;
+  } else {
+    const real sc = (real)1 / sqrt(dp2 * rp2);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dp[j] *= sc;
+  }
+  real alpha;
+  if constexpr (MIXED) {
+    real cx = rp[1] * rn[2] - rp[2] * rn[1];
+    real cy = rp[2] * rn[0] - rp[0] * rn[2];
+    real cz = rp[0] * rn[1] - rp[1] * rn[0];
+    alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
+  } else {
+    real ca = dot / sqrt(rp2 * rn2);
+    alpha = (ca >= 1.0) ? aeq : acos(ca);  // bending.f90:93-98 guard: delta_alpha = 0
+  }
+  real fm;
+  if (C.bend_form == 1) {
+    fm = kb * sin(alpha);
+    e = kb * ((real)1 - cos(alpha));
+  } else {
+    real da = alpha - aeq;
+    fm = kb * da;
+    e = (real)0.5 * fm * da;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    fa[j] = fm * dp[j];
+    fc[j] = fm * dn[j];
+  }
+}
+
+// Bonded force on the mobile particle i (owner computes, see k_bonded); adds to F[3] and, for the
+// terms that i owns, to e[4] = {FENE, brush bending, melt bending, orientation}.  Returns false
+// when i is in no chain of two or more beads.
 template <bool MIXED, bool EFLAG>
-__global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc) {
+__device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, int mask, int i, int w,
+                                          real_t<MIXED>* F, real_t<MIXED>* e4) {
+  using real = real_t<MIXED>;
+  const RepDesc& R = s.reps[info_rep(w)];
+  int kind = -1, m = 0, n = 0;
+  const int t = __ldg(&s.tag[i]);
+  const int lt = t - R.p0;
+  if (lt < R.part_init_d) {
+    kind = 0; n = R.n_mon; m = lt % n;
+  } else if (lt < R.part_init_e) {
+    kind = 1; n = R.n_mon_d; m = (lt - R.part_init_d) % n;
+  } else if (lt < R.n_mon_tot) {
+    kind = 2; n = R.n_mon_e; m = (lt - R.part_init_e) % n;
+  }
+  if (kind < 0 || n < 2) return false;
+  const int t0 = t - m;
+  {
+    const bool do_fene = mask & 1;
+    const bool do_bend = (kind == 0 && (mask & 2)) || (kind == 1 && (mask & 4));
+    const bool do_or = kind == 0 && (mask & 8) && m <= 1;
+    const int lo = max(0, m - ((do_bend) ? 2 : 1)), hi = min(n - 1, m + ((do_bend) ? 2 : 1));
+    BeadPos<MIXED> P[5];  // beads m-2 .. m+2 (fixed slots, so the array stays in registers)
+#pragma unroll
+    for (int u = 0; u < 5; ++u) {
+      const int b = m - 2 + u;
+      if (b >= lo && b <= hi) P[u].load(s, __ldg(&s.slot_of_tag[t0 + b]));
+    }
+    if (do_fene) {
+      const real kc = (real)C.k_chain, ir2 = (real)C.inv_r_chain_2, xm = (real)C.fene_xmax;
+      if (m > 0) {  // bond (m-1, m): this bead is the second partner
+        real d[3];
+        bead_delta<MIXED>(P[1], P[2], R, d);
+        real x = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * ir2;
+        x = x < xm ? x : xm;
+        real fac = kc / ((real)1 - x) * ir2;
+        F[0] += fac * d[0]; F[1] += fac * d[1]; F[2] += fac * d[2];
+      }
+      if (m < n - 1) {  // bond (m, m+1): first partner; energy counted here
+        real d[3];
+        bead_delta<MIXED>(P[2], P[3], R, d);
+        real x = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * ir2;
+        x = x < xm ? x : xm;
+        real fac = kc / ((real)1 - x) * ir2;
+        F[0] -= fac * d[0]; F[1] -= fac * d[1]; F[2] -= fac * d[2];
+        if (EFLAG) e4[0] += kc * ((real)-0.5 * log((real)1 - x));
+      }
+    }
+    if (do_bend) {
+      const real kb = (real)C.k_bend, aeq = (real)C.alpha_eq;
+#pragma unroll
+      for (int u = 1; u <= 3; ++u) {  // the angle centred on bead c = m - 2 + u
+        const int c = m - 2 + u;
+        if (c < 1 || c > n - 2) continue;
+        real rp[3], rn[3], fa[3], fc[3], e;
+        bead_delta<MIXED>(P[u], P[u - 1], R, rp);
+        bead_delta<MIXED>(P[u + 1], P[u], R, rn);
+        bend_term<MIXED>(rp, rn, C, kb, aeq, fa, fc, e);
+        if (u == 3) { F[0] += fa[0]; F[1] += fa[1]; F[2] += fa[2]; }
+        else if (u == 2) {
+          F[0] -= fa[0] + fc[0]; F[1] -= fa[1] + fc[1]; F[2] -= fa[2] + fc[2];
+          if (EFLAG) { if (kind == 0) e4[1] += e; else e4[2] += e; }
+        } else { F[0] += fc[0]; F[1] += fc[1]; F[2] += fc[2]; }
+      }
+    }
+    if (do_or) {
+      // orientation.f90:35-88: ghost bond head -> head -/+ z, against bond 1
+      const BeadPos<MIXED> H = (m == 0) ? P[2] : P[1];   // the head
+      const BeadPos<MIXED> B1 = (m == 0) ? P[3] : P[2];  // bead 1 of the chain
+      real rp[3], rn[3];
+      bead_delta<MIXED>(B1, H, R, rn);
+      double hz;
+      if constexpr (MIXED) hz = (double)H.q.z * R.ufx[2]; else hz = H.z;
+      if constexpr (MIXED) {
+        rp[0] = 0; rp[1] = 0; rp[2] = (hz > R.L[2] / 2) ? -1.f : 1.f;
+      } else {
+        double g = (hz > R.L[2] / 2) ? hz + 1.0 : hz - 1.0;
+        rp[0] = 0; rp[1] = 0; rp[2] = hz - g;
+      }
+      real dot = 0, rp2 = 0, rn2 = 0, dn[3], dn2 = 0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { dot += rn[j] * rp[j]; rp2 += rp[j] * rp[j]; rn2 += rn[j] * rn[j]; }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { dn[j] = rp[j] * rn2 - rn[j] * dot; dn2 += dn[j] * dn[j]; }
+      const real srp = sqrt(rp2), srn = sqrt(rn2);
+      if (dn2 < (real)C.bend_small) {
+        real u[3], nu = 0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
+        nu = sqrt(nu);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) dn[j] = (nu != 0) ? u[j] / nu / srn : (real)0;
+      } else {
+        const real sc = (real)1 / sqrt(dn2 * rn2);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) dn[j] *= sc;
+      }
+      real alpha;
+      if constexpr (MIXED) {
+        real cx = rp[1] * rn[2] - rp[2] * rn[1];
+        real cy = rp[2] * rn[0] - rp[0] * rn[2];
+        real cz = rp[0] * rn[1] - rp[1] * rn[0];
+        alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
+      } else {
+        real ca = dot / sqrt(rp2 * rn2);
+        alpha = (ca >= 1.0) ? 0. : acos(ca);
+      }
+      const real da = alpha - (real)C.alpha_or;
+      const real fm = (real)C.k_or * da;
+      const real sgn = (m == 0) ? (real)-1 : (real)1;
+      F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
+      if (EFLAG && m == 0) e4[3] += (real)0.5 * fm * da;
+    }
+  }
+  return true;
+}
+
+template <bool MIXED, bool EFLAG>
+__global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask, Acc acc, bool to_f4) {
+  using real = real_t<MIXED>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool inside = i < s.N;
+  const int w = inside ? __ldg(&s.info[i]) : 0;
+  const int rep = info_rep(w);
+  real F[3] = {0, 0, 0};
+  real e4[4] = {0, 0, 0, 0};
+  const bool has = inside && info_mobile(w) && bonded_of<MIXED, EFLAG>(s, C, mask, i, w, F, e4);
+  if (has) {
+    if (MIXED && to_f4) {  // fused step: FP32 force array
+      float4 f = s.f4[i];
+      f.x += (float)F[0];
+      f.y += (float)F[1];
+      f.z += (float)F[2];
+      s.f4[i] = f;
+    } else {
+      s.fx[i] += (double)F[0];
+      s.fy[i] += (double)F[1];
+      s.fz[i] += (double)F[2];
+    }
+  }
+  if (EFLAG) {
+    if (mask & 1) add_obs(acc.col(O_VINTRA), rep, (double)e4[0], has, acc.nrep);
+    if (mask & 2) add_obs(acc.col(O_VBEND), rep, (double)e4[1], has, acc.nrep);
+    if (mask & 4) add_obs(acc.col(O_VBENDM), rep, (double)e4[2], has, acc.nrep);
+    if (mask & 8) add_obs(acc.col(O_VOR), rep, (double)e4[3], has, acc.nrep);
+  }
+}
+
+// BONDED (fused mixed step only): the particle's bonded force (bonded_of) is added before the
+// FP32 force is stored, which saves the bonded kernel's launch and its read-modify-write of f4.
+template <bool MIXED, bool EFLAG, bool BONDED = false>
+__global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc,
+                                                             int bmask = 0) {
   using real = real_t<MIXED>;
   __shared__ PairEntry<real> tab[NPAIR];
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
@@ -199,6 +458,17 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
     }
     }
   }
+  real eb[4] = {0, 0, 0, 0};
+  bool hb = false;
+  if constexpr (BONDED) {
+    if (active) {
+      real fb[3] = {0, 0, 0};
+      hb = bonded_of<MIXED, EFLAG>(s, C, bmask, i, w, fb, eb);
+      fx += fb[0];
+      fy += fb[1];
+      fz += fb[2];
+    }
+  }
   if (inside) {
     if (accumulate) {
       if (active) {
@@ -217,264 +487,29 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
   if (EFLAG) {
     add_obs(acc.col(O_VFF), rep, (double)e_lj, active, acc.nrep);
     if (C.charged) add_obs(acc.col(O_VCOUL), rep, (double)e_c, active, acc.nrep);
+    if constexpr (BONDED) {
+      if (bmask & 1) add_obs(acc.col(O_VINTRA), rep, (double)eb[0], hb, acc.nrep);
+      if (bmask & 2) add_obs(acc.col(O_VBEND), rep, (double)eb[1], hb, acc.nrep);
+      if (bmask & 4) add_obs(acc.col(O_VBENDM), rep, (double)eb[2], hb, acc.nrep);
+      if (bmask & 8) add_obs(acc.col(O_VOR), rep, (double)eb[3], hb, acc.nrep);
+    }
   }
 }
 
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag, Acc acc,
-                 int block) {
+                 int block, int bonded_mask) {
   (void)block;
   int B = 128;
   int g = (s.N + B - 1) / B;
-  if (s.mixed) {
+  if (s.mixed && !accumulate && bonded_mask) {
+    if (eflag) k_pair<true, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+    else k_pair<true, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+  } else if (s.mixed) {
     if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
     else k_pair<true, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
   } else {
     if (eflag) k_pair<false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
     else k_pair<false, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
-  }
-}
-
-// ---------------------------------------------------------------------------------------------
-// Bonded terms
-// ---------------------------------------------------------------------------------------------
-template <bool MIXED>
-struct BeadPos;
-template <>
-struct BeadPos<true> {
-  int4 q;
-  __device__ void load(const DevState& s, int slot) { q = __ldg(&s.pfx[slot]); }
-};
-template <>
-struct BeadPos<false> {
-  double x, y, z;
-  __device__ void load(const DevState& s, int slot) { x = s.rx[slot]; y = s.ry[slot]; z = s.rz[slot]; }
-};
-
-// a - b with the x,y minimum image
-template <bool MIXED>
-__device__ __forceinline__ void bead_delta(const BeadPos<MIXED>& a, const BeadPos<MIXED>& b, const RepDesc& R,
-                                           real_t<MIXED>* d) {
-  if constexpr (MIXED) {
-    d[0] = i2f_fast(fx_diff(a.q.x, b.q.x)) * R.ufx_f[0];
-    d[1] = i2f_fast(fx_diff(a.q.y, b.q.y)) * R.ufx_f[1];
-    d[2] = i2f_fast(fx_diff(a.q.z, b.q.z)) * R.ufx_f[2];
-  } else {
-    d[0] = mic_ref(a.x - b.x, R.L[0], R.invL[0]);
-    d[1] = mic_ref(a.y - b.y, R.L[1], R.invL[1]);
-    d[2] = a.z - b.z;
-  }
-}
-
-// One angle term of bending.f90:47-109 with r_prev = r_c - r_{c-1}, r_next = r_{c+1} - r_c.
-// fa acts on c-1, fc on c+1 (c gets -fa-fc).  MIXED computes the angle as atan2(|p x n|, p.n),
-// which keeps FP32 accurate for the nearly straight chains that stiff brushes produce.
-template <bool MIXED>
-__device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, const SimConst& C, real_t<MIXED> kb,
-                          real_t<MIXED> aeq, real_t<MIXED>* fa, real_t<MIXED>* fc, real_t<MIXED>& e) {
-  using real = real_t<MIXED>;
-  real dot = 0, rp2 = 0, rn2 = 0;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    dot += rn[j] * rp[j];
-    rp2 += rp[j] * rp[j];
-    rn2 += rn[j] * rn[j];
-  }
-  real dn[3], dp[3], dn2 = 0, dp2 = 0;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    dn[j] = rp[j] * rn2 - rn[j] * dot;
-    dp[j] = -rn[j] * rp2 + rp[j] * dot;
-    dn2 += dn[j] * dn[j];
-    dp2 += dp[j] * dp[j];
-  }
-  const real small = (real)C.bend_small;
-  const real srp = sqrt(rp2), srn = sqrt(rn2);
-  if (dn2 < small) {
-    real u[3], nu = 0;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
-    nu = sqrt(nu);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) dn[j] = (nu != 0) ? u[j] / nu / srn : (real)0;
-  } else {
-    const real sc = (real)1 / sqrt(dn2 * rn2);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) dn[j] *= sc;
-  }
-  if (dp2 < small) {
-    real u[3], nu = 0;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
-    nu = sqrt(nu);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) dp[j] = (nu != 0) ? u[j] / nu / srp : (real)0;
-  } else {
-    const real sc = (real)1 / sqrt(dp2 * rp2);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) dp[j] *= sc;
-  }
-  real alpha;
-  if constexpr (MIXED) {
-    real cx = rp[1] * rn[2] - rp[2] * rn[1];
-    real cy = rp[2] * rn[0] - rp[0] * rn[2];
-    real cz = rp[0] * rn[1] - rp[1] * rn[0];
-    alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
-  } else {
-    real ca = dot / sqrt(rp2 * rn2);
-    alpha = (ca >= 1.0) ? aeq : acos(ca);  // bending.f90:93-98 guard: delta_alpha = 0
-  }
-  real fm;
-  if (C.bend_form == 1) {
-    fm = kb * sin(alpha);
-    e = kb * ((real)1 - cos(alpha));
-  } else {
-    real da = alpha - aeq;
-    fm = kb * da;
-    e = (real)0.5 * fm * da;
-  }
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    fa[j] = fm * dp[j];
-    fc[j] = fm * dn[j];
-  }
-}
-
-template <bool MIXED, bool EFLAG>
-__global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask, Acc acc, bool to_f4) {
-  using real = real_t<MIXED>;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool inside = i < s.N;
-  const int w = inside ? __ldg(&s.info[i]) : 0;
-  bool active = inside && info_mobile(w);
-  const int rep = info_rep(w);
-  real F[3] = {0, 0, 0};
-  real e_fene = 0, e_bend = 0, e_bendm = 0, e_or = 0;
-  int kind = -1, m = 0, n = 0, t0 = 0;
-  const RepDesc* Rp = nullptr;
-  if (active) {
-    Rp = &s.reps[rep];
-    const RepDesc& R = *Rp;
-    int t = __ldg(&s.tag[i]);
-    int lt = t - R.p0;
-    if (lt < R.part_init_d) {
-      kind = 0; n = R.n_mon; m = lt % n;
-    } else if (lt < R.part_init_e) {
-      kind = 1; n = R.n_mon_d; m = (lt - R.part_init_d) % n;
-    } else if (lt < R.n_mon_tot) {
-      kind = 2; n = R.n_mon_e; m = (lt - R.part_init_e) % n;
-    }
-    t0 = t - m;
-    if (n < 2) kind = -1;
-  }
-  if (kind >= 0) {
-    const RepDesc& R = *Rp;
-    const bool do_fene = mask & 1;
-    const bool do_bend = (kind == 0 && (mask & 2)) || (kind == 1 && (mask & 4));
-    const bool do_or = kind == 0 && (mask & 8) && m <= 1;
-    const int lo = max(0, m - ((do_bend) ? 2 : 1)), hi = min(n - 1, m + ((do_bend) ? 2 : 1));
-    BeadPos<MIXED> P[5];  // beads m-2 .. m+2
-    for (int b = lo; b <= hi; ++b) P[b - m + 2].load(s, __ldg(&s.slot_of_tag[t0 + b]));
-    if (do_fene) {
-      const real kc = (real)C.k_chain, ir2 = (real)C.inv_r_chain_2, xm = (real)C.fene_xmax;
-      if (m > 0) {  // bond (m-1, m): this bead is the second partner
-        real d[3];
-        bead_delta<MIXED>(P[1], P[2], R, d);
-        real x = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * ir2;
-        x = x < xm ? x : xm;
-        real fac = kc / ((real)1 - x) * ir2;
-        F[0] += fac * d[0]; F[1] += fac * d[1]; F[2] += fac * d[2];
-      }
-      if (m < n - 1) {  // bond (m, m+1): first partner; energy counted here
-        real d[3];
-        bead_delta<MIXED>(P[2], P[3], R, d);
-        real x = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * ir2;
-        x = x < xm ? x : xm;
-        real fac = kc / ((real)1 - x) * ir2;
-        F[0] -= fac * d[0]; F[1] -= fac * d[1]; F[2] -= fac * d[2];
-        if (EFLAG) e_fene += kc * ((real)-0.5 * log((real)1 - x));
-      }
-    }
-    if (do_bend) {
-      const real kb = (real)C.k_bend, aeq = (real)C.alpha_eq;
-      for (int c = m - 1; c <= m + 1; ++c) {
-        if (c < 1 || c > n - 2) continue;
-        real rp[3], rn[3], fa[3], fc[3], e;
-        bead_delta<MIXED>(P[c - m + 2], P[c - 1 - m + 2], R, rp);
-        bead_delta<MIXED>(P[c + 1 - m + 2], P[c - m + 2], R, rn);
-        bend_term<MIXED>(rp, rn, C, kb, aeq, fa, fc, e);
-        if (c == m + 1) { F[0] += fa[0]; F[1] += fa[1]; F[2] += fa[2]; }
-        else if (c == m) {
-          F[0] -= fa[0] + fc[0]; F[1] -= fa[1] + fc[1]; F[2] -= fa[2] + fc[2];
-          if (EFLAG) { if (kind == 0) e_bend += e; else e_bendm += e; }
-        } else { F[0] += fc[0]; F[1] += fc[1]; F[2] += fc[2]; }
-      }
-    }
-    if (do_or) {
-      // orientation.f90:35-88: ghost bond head -> head -/+ z, against bond 1
-      const BeadPos<MIXED>& H = P[2 - m];
-      const BeadPos<MIXED>& B1 = P[3 - m];
-      real rp[3], rn[3];
-      bead_delta<MIXED>(B1, H, R, rn);
-      double hz;
-      if constexpr (MIXED) hz = (double)H.q.z * R.ufx[2]; else hz = H.z;
-      if constexpr (MIXED) {
-        rp[0] = 0; rp[1] = 0; rp[2] = (hz > R.L[2] / 2) ? -1.f : 1.f;
-      } else {
-        double g = (hz > R.L[2] / 2) ? hz + 1.0 : hz - 1.0;
-        rp[0] = 0; rp[1] = 0; rp[2] = hz - g;
-      }
-      real dot = 0, rp2 = 0, rn2 = 0, dn[3], dn2 = 0;
-#pragma unroll
-      for (int j = 0; j < 3; ++j) { dot += rn[j] * rp[j]; rp2 += rp[j] * rp[j]; rn2 += rn[j] * rn[j]; }
-#pragma unroll
-      for (int j = 0; j < 3; ++j) { dn[j] = rp[j] * rn2 - rn[j] * dot; dn2 += dn[j] * dn[j]; }
-      const real srp = sqrt(rp2), srn = sqrt(rn2);
-      if (dn2 < (real)C.bend_small) {
-        real u[3], nu = 0;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
-        nu = sqrt(nu);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) dn[j] = (nu != 0) ? u[j] / nu / srn : (real)0;
-      } else {
-        const real sc = (real)1 / sqrt(dn2 * rn2);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) dn[j] *= sc;
-      }
-      real alpha;
-      if constexpr (MIXED) {
-        real cx = rp[1] * rn[2] - rp[2] * rn[1];
-        real cy = rp[2] * rn[0] - rp[0] * rn[2];
-        real cz = rp[0] * rn[1] - rp[1] * rn[0];
-        alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
-      } else {
-        real ca = dot / sqrt(rp2 * rn2);
-        alpha = (ca >= 1.0) ? 0. : acos(ca);
-      }
-      const real da = alpha - (real)C.alpha_or;
-      const real fm = (real)C.k_or * da;
-      const real sgn = (m == 0) ? (real)-1 : (real)1;
-      F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
-      if (EFLAG && m == 0) e_or += (real)0.5 * fm * da;
-    }
-    if (MIXED && to_f4) {  // fused step: FP32 force array
-      float4 f = s.f4[i];
-      f.x += (float)F[0];
-      f.y += (float)F[1];
-      f.z += (float)F[2];
-      s.f4[i] = f;
-    } else {
-      s.fx[i] += (double)F[0];
-      s.fy[i] += (double)F[1];
-      s.fz[i] += (double)F[2];
-    }
-  }
-  if (EFLAG) {
-    active = active && kind >= 0;
-    if (mask & 1) add_obs(acc.col(O_VINTRA), rep, (double)e_fene, active, acc.nrep);
-    if (mask & 2) add_obs(acc.col(O_VBEND), rep, (double)e_bend, active, acc.nrep);
-    if (mask & 4) add_obs(acc.col(O_VBENDM), rep, (double)e_bendm, active, acc.nrep);
-    if (mask & 8) add_obs(acc.col(O_VOR), rep, (double)e_or, active, acc.nrep);
   }
 }
 

@@ -54,9 +54,11 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force);
 size_t nlist_smem(int cap);
 constexpr int NL_CAP_MAX = 420;
 // ---- forces ------------------------------------------------------------------------------------
-// pair forces (fluid_fluid); accumulate = add into f, else overwrite; eflag = energies into acc
+// pair forces (fluid_fluid); accumulate = add into f, else overwrite; eflag = energies into acc;
+// bonded_mask != 0 in the fused mixed step (overwrite into f4) adds the bonded terms in the same
+// kernel (the caller then skips launch_bonded)
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag,
-                 Acc acc, int block);
+                 Acc acc, int block, int bonded_mask = 0);
 // bonded terms: mask bit 1 FENE, 2 brush bending, 4 melt bending, 8 orientation
 void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc,
                    bool fused = false);
