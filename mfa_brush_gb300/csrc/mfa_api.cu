@@ -438,6 +438,18 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     }
   if (rl_max <= 0.) rl_max = 1.0 + skin;
   ctx->rl_max = rl_max;
+  {  // uniform cut-offs: every nonzero list cut-off of the present types equal (and the screens)
+    double lo = 1e300, hi = 0., slo = 1e300, shi = 0.;
+    for (int i = 0; i < p->n_type; ++i)
+      for (int j = 0; j < p->n_type; ++j) {
+        const PairEntry<double>& e = td[i * MAXT + j];
+        if (e.rlist2 > 0.) { lo = std::min(lo, e.rlist2); hi = std::max(hi, e.rlist2); }
+        if (e.screen2 > 0.) { slo = std::min(slo, e.screen2); shi = std::max(shi, e.screen2); }
+      }
+    const bool uni = hi > 0. && hi == lo && shi == slo;
+    C.rl2_uni_f = uni ? (float)(hi * 1.0002) : 0.f;
+    C.scr2_uni_f = uni ? (float)(shi * 1.0002) : 0.f;
+  }
   // ---- replicas -------------------------------------------------------------------------------
   ctx->hreps.resize(n_rep);
   ctx->v_coul_self.assign(n_rep, 0.);
@@ -569,6 +581,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   S.reps = ctx->dreps;
   S.tabf = ctx->dtabf;
   S.tabd = ctx->dtabd;
+  S.rl2_uni = S.mixed ? C.rl2_uni_f : 0.f;
   // neighbour capacity: 2x the mean count of the densest replica + 32, at least 48
   int cap = ctx->opt.nbr_capacity;
   if (cap <= 0) {

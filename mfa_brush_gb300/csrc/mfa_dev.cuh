@@ -83,6 +83,11 @@ struct SimConst {
   // FP32 copies for the mixed-precision integrator
   float dt_f, skin_half2_f, a_w_f;
   float mass_f[MAXT], inv_mass_f[MAXT], sigma_wall_f[MAXT], a_wall_f[MAXT], cforce_f[3];
+  // When every interacting type pair has the same list and screening cut-offs (a single WCA or
+  // LJ range), the list builder and the pair screening compare against these instead of a table
+  // lookup; pairs whose own cut-off is 0 (head-head) are then listed too and dropped later.
+  // 0 = cut-offs differ.
+  float rl2_uni_f, scr2_uni_f;
 };
 
 // Per replica (device array, read through the L1).

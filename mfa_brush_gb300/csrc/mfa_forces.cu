@@ -286,7 +286,8 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
 
 // BONDED (fused mixed step only): the particle's bonded force (bonded_of) is added before the
 // FP32 force is stored, which saves the bonded kernel's launch and its read-modify-write of f4.
-template <bool MIXED, bool EFLAG, bool BONDED = false>
+// UNI (mixed only): one screening cut-off for every type pair (SimConst::scr2_uni_f).
+template <bool MIXED, bool EFLAG, bool BONDED = false, bool UNI = false>
 __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc,
                                                              int bmask = 0) {
   using real = real_t<MIXED>;
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
         const float dx = i2f_coarse(fx_diff(qi.x, qj.x), 9) * cx;
         const float dy = i2f_coarse(fx_diff(qi.y, qj.y), 9) * cy;
         const float dz = i2f_coarse(fx_diff(qi.z, qj.z), 9) * cz;
-        return dx * dx + dy * dy + dz * dz < tab[ti * MAXT + info_type(qj.w)].screen2;
+        return dx * dx + dy * dy + dz * dz < (UNI ? C.scr2_uni_f : tab[ti * MAXT + info_type(qj.w)].screen2);
       } else {
         real dx, dy, dz;
         const int wj = delta(j, dx, dy, dz);
@@ -501,12 +502,23 @@ void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool acc
   (void)block;
   int B = 128;
   int g = (s.N + B - 1) / B;
+  const bool uni = C.scr2_uni_f > 0.f;
   if (s.mixed && !accumulate && bonded_mask) {
-    if (eflag) k_pair<true, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
-    else k_pair<true, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+    if (uni) {
+      if (eflag) k_pair<true, true, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+      else k_pair<true, false, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+    } else {
+      if (eflag) k_pair<true, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+      else k_pair<true, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+    }
   } else if (s.mixed) {
-    if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
-    else k_pair<true, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
+    if (uni) {
+      if (eflag) k_pair<true, true, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
+      else k_pair<true, false, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
+    } else {
+      if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
+      else k_pair<true, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
+    }
   } else {
     if (eflag) k_pair<false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
     else k_pair<false, false><<<g, B, 0, st>>>(s, C, accumulate, acc);

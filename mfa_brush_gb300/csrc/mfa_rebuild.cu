@@ -41,26 +41,37 @@ __global__ void k_bin(DevState s, bool force) {
   if (i >= s.N) return;
   int w = s.info[i];
   const RepDesc& R = s.reps[info_rep(w)];
-  double x = s.rx[i], y = s.ry[i], z = s.rz[i];
-  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
-    atomicOr(s.status, ST_NAN);
-    x = y = z = 0.;
-  }
-  double lz = 1. / R.inv_lc[2];
-  if (z < -lz || z > R.L[2] + lz) atomicOr(s.status, ST_OUT_OF_BOX);
+  const double lz = 1. / R.inv_lc[2];
   int ix, iy, iz;
   if (s.mixed) {  // the list builder's integer formula on the fixed-point view
+    // (x, y need no check: the fixed-point view wraps them; the integrator flags NaN)
+    const double z = s.rz[i];
+    if (!(z >= -lz && z <= R.L[2] + lz)) atomicOr(s.status, isnan(z) ? ST_NAN : ST_OUT_OF_BOX);
     const int4 q = s.pfx[i];
     ix = (int)(((unsigned long long)(unsigned)q.x * (unsigned)R.nc[0]) >> 32);
     iy = (int)(((unsigned long long)(unsigned)q.y * (unsigned)R.nc[1]) >> 32);
     iz = (int)(((long long)q.z * R.nc[2]) >> 30);
     iz = min(max(iz, 0), R.nc[2] - 1);
   } else {
+    double x = s.rx[i], y = s.ry[i], z = s.rz[i];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+      atomicOr(s.status, ST_NAN);
+      x = y = z = 0.;
+    }
+    if (z < -lz || z > R.L[2] + lz) atomicOr(s.status, ST_OUT_OF_BOX);
     cell_coords(R, x, y, z, ix, iy, iz);
   }
-  int c = R.cell_off + (iz * R.nc[1] + iy) * R.nc[0] + ix;
+  const int c = R.cell_off + (iz * R.nc[1] + iy) * R.nc[0] + ix;
   s.cell_of[i] = c;
-  s.rank[i] = atomicAdd(&s.cell_count[c], 1);
+  // Particles are still nearly sorted by cell, so neighbouring lanes share cells: the lanes of one
+  // cell take consecutive ranks from a single atomicAdd (k_sort_cells orders each cell by tag
+  // afterwards, so the order of the ranks does not matter).
+  const unsigned grp = __match_any_sync(__activemask(), c);
+  const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&s.cell_count[c], __popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  s.rank[i] = base + __popc(grp & ((1u << lane) - 1u));
 }
 
 // exclusive scan, 1024 elements per block
@@ -230,7 +241,7 @@ __global__ void k_copyback(DevState s, bool force) {
 // coalesced (scattered 4-byte stores into the column-major list cost read-modify-writes in HBM).
 constexpr int NL_BLOCK = 128;
 
-template <bool MIXED>
+template <bool MIXED, bool UNI>
 __global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
   extern __shared__ int nl_sh[];
@@ -289,6 +300,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
     }
     const float lx = R.lc_f[0], ly = R.lc_f[1], lz = R.lc_f[2];
     const float rl2max = rlmax[ti];
+    const float rl_uni = s.rl2_uni;  // UNI: one list cut-off for every pair (2e-4 margin included)
     auto fl = [](int v) { return i2f_coarse(v, 0); };  // exact for small integers
     auto gap2 = [](float d, float l) {  // squared gap of d cell widths (0 when the particle is past the edge)
       d = fmaxf(d, 0.f) * l;
@@ -334,7 +346,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
               const float ddx = i2f_coarse(fx_diff(qi.x, qj.x), 9) * ux;
               const float ddy = i2f_coarse(fx_diff(qi.y, qj.y), 9) * uy;
               const float ddz = i2f_coarse(fx_diff(qi.z, qj.z), 9) * uz;
-              hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2f[ti * MAXT + info_type(wj)];
+              hit = ddx * ddx + ddy * ddy + ddz * ddz < (UNI ? rl_uni : rl2f[ti * MAXT + info_type(wj)]);
             } else {
               wj = s.info[j];
               const double ddx = mic_ref(x - s.rx[j], R.L[0], R.invL[0]);
@@ -386,17 +398,15 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   k_permute<<<gN, B, 0, st>>>(s, force);
   k_copyback<<<gN, B, 0, st>>>(s, force);
   const size_t shm = nlist_smem(s.nbr_cap);
-  static size_t shm_set[2] = {48 * 1024, 48 * 1024};
-  if (shm > shm_set[s.mixed]) {  // above 48 KB of dynamic shared memory needs an opt-in
-    if (s.mixed) cudaFuncSetAttribute(k_nlist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    else cudaFuncSetAttribute(k_nlist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    shm_set[s.mixed] = shm;
+  static size_t shm_set[3] = {48 * 1024, 48 * 1024, 48 * 1024};
+  const int var = s.mixed ? (s.rl2_uni > 0.f ? 2 : 1) : 0;
+  auto kern = var == 2 ? k_nlist<true, true> : var == 1 ? k_nlist<true, false> : k_nlist<false, false>;
+  if (shm > shm_set[var]) {  // above 48 KB of dynamic shared memory needs an opt-in
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    shm_set[var] = shm;
   }
   const int gl = (s.N + NL_BLOCK - 1) / NL_BLOCK;
-  if (s.mixed)
-    k_nlist<true><<<gl, NL_BLOCK, shm, st>>>(s, force);
-  else
-    k_nlist<false><<<gl, NL_BLOCK, shm, st>>>(s, force);
+  kern<<<gl, NL_BLOCK, shm, st>>>(s, force);
 }
 
 // ---------------------------------------------------------------------------------------------

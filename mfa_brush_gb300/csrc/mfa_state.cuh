@@ -32,6 +32,7 @@ struct DevState {
   int *cell_of, *rank, *perm, *cell_count, *cell_start, *scan_blk;
   int ncell_tot;
   // control words
+  float rl2_uni;  // SimConst::rl2_uni_f (0: per-pair list cut-offs)
   int* rebuild_flag;
   unsigned* status;
   long long* steps_done;

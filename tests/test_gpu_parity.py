@@ -174,6 +174,27 @@ def test_interacting_pairs_identical(gpu, try_deck, oracle_mod):
     assert len(pg) == len(sg) and sg == so
 
 
+def test_wca_channel_fused_mixed_vs_oracle(gpu, oracle_mod):
+    """The bench model (WCA + FENE + DPD, single cut-off, so the list builder and the pair
+    screening take their uniform-cut-off form, and the bonded terms run inside the pair kernel):
+    10 fused mixed steps against 10 FP64 oracle steps with the same noise."""
+    p = configs.wca_params(gamma=5.0)
+    s, a_type, r0, v = configs.brush_channel(16.0, 14.0, 0.2, 25, seed=21)
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, None, "mixed")
+    g.step(10)
+    o.step(10, 1, 0)
+    r, vv, aa, f = g.state()
+    ro, vo, ao, fo = o.state()
+    L = np.array(list(s.boundary))
+    d = r - ro
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < 1e-7
+    assert np.abs(vv - vo).max() < 1e-4 * np.sqrt(np.mean(vo ** 2))
+    eg, eo = g.energies()[0], o.energies()
+    for k in ("v_fluid_fluid", "v_intra_molec", "v_fluid_wall", "t_fluid"):
+        assert rel(eg[k], eo[k]) < 1e-5, k
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_batched_replicas_equal_single(gpu, precision):
     """A replica inside a batch gets bit-identical forces to the same replica run alone."""
