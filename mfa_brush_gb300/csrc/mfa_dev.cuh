@@ -140,8 +140,11 @@ __device__ __forceinline__ void pair_uniform_bits(unsigned long long seed, long 
 __device__ __forceinline__ float pair_gauss_f(unsigned long long seed, long long step, int ta, int tb) {
   uint32_t b1, b2;
   pair_uniform_bits(seed, step, ta, tb, b1, b2);
-  float u1 = ((float)b1 + 0.5f) * (1.0f / 8388608.0f);
-  float u2 = (float)b2 * (1.0f / 8388608.0f);
+  // b1, b2 < 2^23: 2^23 + b is exact in FP32, so the subtraction converts without an I2F
+  const float f1 = __uint_as_float(0x4B000000u | b1) - 8388608.0f;
+  const float f2 = __uint_as_float(0x4B000000u | b2) - 8388608.0f;
+  float u1 = (f1 + 0.5f) * (1.0f / 8388608.0f);
+  float u2 = f2 * (1.0f / 8388608.0f);
   return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
 }
 

@@ -1,0 +1,146 @@
+"""GPU parity on the configuration families beyond the try deck, through the C ABI against the
+oracle: melt chains in a brush with cosine bending on every chain (the large melt-in-brush
+case), the Poiseuille body force with fixed heads (the two-liquid channel case), and the NVE
+energy drift of the mixed-precision step against the FP64 oracle over 10^4 steps.
+
+Tolerances as in test_gpu_parity.py; the drift criterion is the one the mixed mode is built to:
+its energy drift within 2x of the FP64 oracle's (with a floor at the FP64 round-off level)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import assert_force_parity
+from mfa_brush_gb300 import abi, configs, md
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(x, y):
+    return abs(x - y) / max(abs(y), 1e-300)
+
+
+def melt_brush_inputs(try_deck):
+    """The try deck's switches (SOLVENT 3, brush in good solvent, DPD in the LJ range) with
+    cosine bending k_b = 2 on the brush and on the melt chains."""
+    inp = abi.Inputs.from_buffer_copy(try_deck[0])
+    f = inp.flags
+    f.bending, f.bending_melt, f.orientation = 1, 1, 0
+    f.dpd_cut_off, f.force_switch_on, f.profiles = 0.0, 0, 0
+    inp.bend_form, inp.k_bend = 1, 2.0
+    inp.dt = 0.002
+    return inp
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_melt_in_brush_cosine_bending(gpu, try_deck, oracle_mod, precision):
+    inp = melt_brush_inputs(try_deck)
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(14.0, 12.0, 0.15, 16, rho=0.85, n_mon_d=10, seed=7, max_fill=0.75)
+    assert s.n_chain_d > 0 and p.bend_form == 1
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    tol_e = 1e-10 if precision == "fp64" else 1e-5
+    # each routine's energy; the forces summed over the four routines, as md_main sums them.
+    # (A bending force alone on a nearly straight chain is ~sin(angle) small and its FP32
+    # direction carries a relative error ~1e-7/angle; only max|dF|/F_rms is asked of it.)
+    g.zero_force()
+    o.zero_force()
+    for routine, key in (("fluid_fluid", "v_fluid_fluid"), ("intra_molec", "v_intra_molec"),
+                         ("bending", "v_bend"), ("bending_melt", "v_bend_melt")):
+        f0, fo0 = g.state()[3], o.state()[3]
+        e = getattr(g, routine)()
+        e = e[0] if isinstance(e, tuple) else e
+        getattr(o, routine)()
+        assert rel(e[0], o.energies()[key]) < tol_e, routine
+        df, dfo = g.state()[3] - f0, o.state()[3] - fo0
+        rms = np.sqrt(np.mean(np.sum(dfo ** 2, axis=1)))
+        assert np.linalg.norm(df - dfo, axis=1).max() <= (1e-9 if precision == "fp64" else 1e-5) * rms, routine
+    assert_force_parity(g.state()[3], o.state()[3], precision)
+
+
+def test_melt_in_brush_fused_mixed_steps(gpu, try_deck, oracle_mod):
+    inp = melt_brush_inputs(try_deck)
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(14.0, 12.0, 0.15, 16, rho=0.85, n_mon_d=10, seed=8, max_fill=0.75)
+    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    g.step(10)
+    o.step(10, 1, 0)
+    r, vv, _, _ = g.state()
+    ro, vo, _, _ = o.state()
+    L = np.array(list(s.boundary))
+    d = r - ro
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < 1e-7
+    assert np.abs(vv - vo).max() < 1e-4 * np.sqrt(np.mean(vo ** 2))
+    eg, eo = g.energies()[0], o.energies()
+    for k in ("v_fluid_fluid", "v_intra_molec", "v_bend", "v_bend_melt", "t_fluid"):
+        assert rel(eg[k], eo[k]) < 1e-5, k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_poiseuille_body_force_and_fixed_heads(gpu, try_deck, oracle_mod, precision):
+    """POISEUILLE: m g on every non-head bead (constant_force.f90:17-21) and heads held at rest
+    (verlet_velocities.f90:115-120); five md_main steps through the drop-ins (FP64) or the fused
+    step (mixed) against the oracle."""
+    inp = abi.Inputs.from_buffer_copy(try_deck[0])
+    inp.flags.poiseuille = 1
+    inp.const_force[0], inp.const_force[1], inp.const_force[2] = 0.05, 0.0, 0.0
+    p, s = md.derive(inp)
+    _, _, _, a_type, r0, v, a = try_deck
+    g = md.MdSystem(p, s, a_type, r0, v, a, precision=precision)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v, a)
+    if precision == "fp64":
+        for _ in range(5):
+            g.md_step()
+    else:
+        g.step(5)
+    o.step(5, 1, 0)
+    r, vv, _, _ = g.state()
+    ro, vo, _, _ = o.state()
+    L = np.array(list(s.boundary))
+    d = r - ro
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < (1e-9 if precision == "fp64" else 1e-7)
+    heads = np.flatnonzero(a_type == 1)
+    assert np.abs(vv[heads]).max() == 0.0
+    tol = 1e-7 if precision == "fp64" else 1e-4
+    assert np.abs(vv - vo).max() < tol * max(1.0, np.sqrt(np.mean(vo ** 2)))
+
+
+def _energy_series(run, n_steps, every):
+    e = []
+    for _ in range(n_steps // every):
+        e.append(run(every))
+    return np.array(e)
+
+
+def test_nve_drift_mixed_within_2x_fp64_oracle(gpu, oracle_mod):
+    """10^4 NVE steps (no thermostat) of a WCA brush channel: the mixed-precision total-energy
+    drift (slope of a linear fit, per particle per step) stays within 2x of the FP64 oracle's."""
+    p = configs.wca_params(gamma=0.0, thermostat=1, dt=0.005)
+    s, a_type, r0, v = configs.brush_channel(12.0, 10.0, 0.15, 12, seed=31, kT=0.5)
+    n, every = 10000, 500
+    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+
+    def run_g(k):
+        g.step(k)
+        return g.energies()[0]["e_total"]
+
+    threads = max(1, os.cpu_count() or 1)
+
+    def run_o(k):
+        o.step(k, threads, 0)
+        e = o.energies()
+        return e["v_fluid_fluid"] + e["v_fluid_wall"] + e["v_wall_wall"] + e["v_intra_molec"] + e["t_fluid"]
+
+    eg = _energy_series(run_g, n, every)
+    eo = _energy_series(run_o, n, every)
+    t = np.arange(1, len(eg) + 1) * every
+    slope_g = abs(np.polyfit(t, eg, 1)[0]) / s.n_mon_tot
+    slope_o = abs(np.polyfit(t, eo, 1)[0]) / s.n_mon_tot
+    print("NVE drift per particle per step: mixed %.3e  fp64 oracle %.3e" % (slope_g, slope_o))
+    assert np.all(np.isfinite(eg))
+    assert slope_g <= 2.0 * max(slope_o, 1e-9)
