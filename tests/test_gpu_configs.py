@@ -144,3 +144,42 @@ def test_nve_drift_mixed_within_2x_fp64_oracle(gpu, oracle_mod):
     print("NVE drift per particle per step: mixed %.3e  fp64 oracle %.3e" % (slope_g, slope_o))
     assert np.all(np.isfinite(eg))
     assert slope_g <= 2.0 * max(slope_o, 1e-9)
+
+
+def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod):
+    """The charged-brush case at its full size: 40 x 40 x 30 channel, grafting density 0.1, N = 40,
+    slab Ewald with alpha = 0.9 (alpha_c = 0.81), real-space cut-off 3, |k| <= 12 (2 pi / L) with
+    the reference's k-set rule (8071 vectors), dipolar correction.  The line charge of "every
+    10th bead -1" is spread as -0.1 per brush bead, neutralised by the solvent.  Prints the
+    k-space energy and force errors of the FP64 and the mixed (Kahan-compensated FP32) paths
+    against the FP64 oracle; the mixed path must meet the 1e-5 force criterion."""
+    s, a_type, r0, v = configs.brush_channel(40.0, 30.0, 0.1, 40, rho=0.7, seed=41)
+    n_brush = int(np.sum(a_type == 2))
+    n_solv = int(np.sum(a_type == 3))
+    inp = configs.wca_inputs(gamma=1.0, thermostat=0)
+    inp.flags.system = 3
+    inp.charge[1] = -0.1
+    inp.charge[2] = 0.1 * n_brush / n_solv
+    inp.alpha_c = 0.81
+    inp.n_kmax = 12
+    inp.rc_coul = 3.0
+    p, _ = md.derive(inp)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    o.ewald_init()
+    o.zero_force()
+    uko = o.ewald_k()
+    fko = o.state()[3]
+    rms = np.sqrt(np.mean(np.sum(fko ** 2, axis=1)))
+    out = {}
+    for precision in ("fp64", "mixed"):
+        g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+        g.zero_force()
+        uk = g.ewald_k()[0]
+        fk = g.state()[3]
+        a, b = (np.linalg.norm(fk - fko, axis=1).max() / rms, None)
+        out[precision] = (rel(uk, uko), a)
+        g.close()
+    print("k-space vs FP64 oracle (N=%d, rel energy error, max|dF|/F_rms): fp64 %.2e %.2e  mixed %.2e %.2e"
+          % (s.n_mon_tot, *out["fp64"], *out["mixed"]))
+    assert out["fp64"][0] < 1e-10 and out["fp64"][1] < 1e-9
+    assert out["mixed"][0] < 1e-5 and out["mixed"][1] < 1e-5
