@@ -291,6 +291,42 @@ def explicit_wall_channel(seed=1, L=20.0, D=20.0):
     return brush_channel(L, D, 0.1, 30, rho=0.8, seed=seed, z_lo=1.0, wall_spacing=1.0)
 
 
+def two_liquid_channel(L=20.0, D=16.0, sigma_g=0.15, n_mon=12, rho=0.8, seed=1):
+    """Brush channel whose free liquid is split into layered halves: liquid A (type 3, melt
+    chains of one bead) below D/2 and liquid B (type 4, particle-4 chains of one bead) above,
+    ordered brush, A, B as the reference orders its molecules (init_system.f90:172-187).
+    Use with two_liquid_inputs()."""
+    s, a_type, r0, v = brush_channel(L, D, sigma_g, n_mon, rho=rho, seed=seed)
+    n_brush = s.n_mon * s.n_chain
+    free = np.arange(n_brush, s.n_mon_tot)
+    a_idx = free[r0[free, 2] < D / 2]
+    b_idx = free[r0[free, 2] >= D / 2]
+    order = np.concatenate([np.arange(n_brush), a_idx, b_idx])
+    a_type, r0, v = a_type[order].copy(), r0[order].copy(), v[order].copy()
+    a_type[n_brush + len(a_idx):] = 4
+    s.n_mon_d, s.n_chain_d = 1, len(a_idx)
+    s.n_mon_e, s.n_chain_e = 1, len(b_idx)
+    return s, a_type, r0, v
+
+
+def two_liquid_inputs(gamma=5.0, kT=1.0, dt=0.005, eps_ab=0.5, f_x=0.01):
+    """abi.Inputs of the two-liquid Poiseuille channel in the reference's switches: PARTICLE_4
+    (liquid B), SOLVENT 3 with INTER4 4 (every pair cut at 2 * 2^(1/6) sigma), the brush in good
+    solvent (WCA among brush beads), eps_AB between the liquids, WALL 2, POISEUILLE with the body
+    force f_x, DPD in the LJ range, z-profiles on."""
+    inp = wca_inputs(gamma=gamma, kT=kT, dt=dt)
+    f = inp.flags
+    f.solvent, f.particle_4, f.brush_in_good_sv = 3, 1, 1
+    f.poiseuille, f.profiles = 1, 1
+    inp.inter4 = 4
+    # SOLVENT >= 2 takes the brush-liquid and A-B sigmas from system_input (non-additive)
+    inp.delta_sig[0] = inp.delta_sig[1] = inp.delta_sig[2] = 1.0
+    inp.a_w4, inp.sigma_w4 = inp.a_w, inp.sigma_w
+    inp.epsil[2 * abi.MAXT + 3] = inp.epsil[3 * abi.MAXT + 2] = eps_ab
+    inp.const_force[0] = f_x
+    return inp
+
+
 def small_channel(seed=1):
     """20x20x20 channel, 40 chains of 30 beads per wall (grafting density 0.1), solvent to 0.8."""
     return brush_channel(20.0, 20.0, 0.1, 30, rho=0.8, seed=seed)

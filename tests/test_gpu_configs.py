@@ -183,3 +183,46 @@ def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod):
           % (s.n_mon_tot, *out["fp64"], *out["mixed"]))
     assert out["fp64"][0] < 1e-10 and out["fp64"][1] < 1e-9
     assert out["mixed"][0] < 1e-5 and out["mixed"][1] < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_two_liquid_poiseuille_channel(gpu, oracle_mod, precision):
+    """The two-liquid Poiseuille family: liquids A (type 3) and B (type 4, PARTICLE_4) in layered
+    halves, eps_AB = 0.5, every liquid pair cut at 2 * 2^(1/6), brush WCA, body force f_x on every
+    non-head bead, z-profiles of three species.  Pair + wall + body forces against the oracle,
+    then six steps with profiles (drop-ins in FP64, the fused graph step in mixed)."""
+    inp = configs.two_liquid_inputs(f_x=0.05)
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.two_liquid_channel(seed=3)
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision, profile_from_step=0)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    g.zero_force()
+    vff = g.fluid_fluid()[0][0]
+    vfw = g.fluid_wall(2)[0]
+    g.constant_force(1)
+    o.zero_force()
+    o.fluid_fluid()
+    o.fluid_wall()
+    o.constant_force()
+    eo = o.energies()
+    tol_e = 1e-10 if precision == "fp64" else 1e-5
+    assert rel(vff, eo["v_fluid_fluid"]) < tol_e and rel(vfw, eo["v_fluid_wall"]) < 1e-10
+    assert_force_parity(g.state()[3], o.state()[3], precision)
+    g.reset_profiles()
+    if precision == "fp64":
+        for _ in range(6):
+            g.md_step(profiles=True)
+    else:
+        g.step(6)
+    o.step(6, 1, 1)
+    dg, vg, v2g, ng = g.profiles(0)
+    do, vo, v2o, no = o.profiles()
+    assert ng == no == 6
+    assert dg.reshape(-1, 3).sum(0)[1:].tolist() == do.reshape(-1, 3).sum(0)[1:].tolist()  # A, B counts
+    if precision == "fp64":
+        assert np.array_equal(dg, do)
+        assert np.abs(vg - vo).max() < 1e-9 and np.abs(v2g - v2o).max() < 1e-9
+    else:
+        # a bead within ~1e-7 sigma of a bin edge may land in the neighbouring bin
+        assert np.abs(dg - do).sum() <= 8
+        assert np.abs(vg.sum(0) - vo.sum(0)).max() < 1e-3 * max(1.0, np.abs(vo).sum())
