@@ -405,7 +405,9 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
       real fs = 0;  // force factor along d = r_i - r_j
       if (in_lj) {
         r2 = r2raw < r2min ? r2min : r2raw;
-        const real inv_r2 = (real)1 / r2;
+        // MIXED: the hardware reciprocal (2 ulp) instead of the IEEE division sequence
+        real inv_r2;
+        if constexpr (MIXED) inv_r2 = __fdividef(1.f, r2); else inv_r2 = (real)1 / r2;
         const real s2 = e.sig2 * inv_r2;
         const real s6 = s2 * s2 * s2;
         const real s12 = s6 * s6;
@@ -426,8 +428,14 @@ __global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimCons
           vjx = v4.x; vjy = v4.y; vjz = v4.z;
           tag_j = (int)__double_as_longlong(v4.w) - p0;
         }
-        const real r = sqrt(r2);
-        const real ir = (real)1 / r;
+        real r, ir;
+        if constexpr (MIXED) {  // one hardware reciprocal square root (2 ulp)
+          ir = rsqrtf(r2);
+          r = r2 * ir;
+        } else {
+          r = sqrt(r2);
+          ir = (real)1 / r;
+        }
         real wr, wd;
         if (C.dpd_weight1) {
           wr = wd = 1;
