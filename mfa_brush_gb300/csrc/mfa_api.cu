@@ -991,8 +991,9 @@ int mfa_set_state(mfa_ctx* ctx, const double* r0, const double* v, const double*
   if (v) { CK(cudaMallocAsync(&dv, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(dv, v, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
   if (a) { CK(cudaMallocAsync(&da, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(da, a, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
   launch_scatter_state(ctx->S, ctx->st, dr, dv, da);
-  launch_init_views(ctx->S, ctx->st);
-  rebuild(ctx, true);
+  // the lists stay valid unless some particle moved more than skin/2 from the last rebuild
+  launch_refresh_views(ctx->S, ctx->C, ctx->st);
+  rebuild(ctx, false);
   if (dr) CK(cudaFreeAsync(dr, ctx->st));
   if (dv) CK(cudaFreeAsync(dv, ctx->st));
   if (da) CK(cudaFreeAsync(da, ctx->st));

@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
 // FP32 force is stored, which saves the bonded kernel's launch and its read-modify-write of f4.
 // UNI (mixed only): one screening cut-off for every type pair (SimConst::scr2_uni_f).
 template <bool MIXED, bool EFLAG, bool BONDED = false, bool UNI = false>
-__global__ void __launch_bounds__(128, MIXED ? 8 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc,
+__global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc,
                                                              int bmask = 0) {
   using real = real_t<MIXED>;
   __shared__ PairEntry<real> tab[NPAIR];

@@ -382,4 +382,25 @@ void launch_init_views(const DevState& s, cudaStream_t st) {
   k_init_views<<<(s.N + 255) / 256, 256, 0, st>>>(s);
 }
 
+// After a host update of the state (mfa_set_state): the views from the new r, v, and the skin
+// test against the positions of the last rebuild, so that the lists are rebuilt only when some
+// particle now sits more than skin/2 from where the lists were made.
+__global__ void k_refresh_views(DevState s, float skin_half2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  int w = s.info[i];
+  const RepDesc& R = s.reps[info_rep(w)];
+  int4 q;
+  store_views(s, i, R, s.rx[i], s.ry[i], s.rz[i], s.vx[i], s.vy[i], s.vz[i], w, s.tag[i], q);
+  const int4 q0 = s.ref[i];
+  const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
+  const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
+  const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
+  if (info_mobile(w) && dx * dx + dy * dy + dz * dz > skin_half2) *s.rebuild_flag = 1;
+}
+
+void launch_refresh_views(const DevState& s, const SimConst& C, cudaStream_t st) {
+  k_refresh_views<<<(s.N + 255) / 256, 256, 0, st>>>(s, C.skin_half2_f);
+}
+
 }  // namespace mfa

@@ -79,6 +79,8 @@ void launch_scatter_state(const DevState& s, cudaStream_t st, const double* r, c
                           const double* a);
 void launch_gather_state(const DevState& s, cudaStream_t st, double* r, double* v, double* a, double* f);
 void launch_init_views(const DevState& s, cudaStream_t st);
+// views from the current r, v plus the skin test against the last rebuild (sets rebuild_flag)
+void launch_refresh_views(const DevState& s, const SimConst& C, cudaStream_t st);
 // ---- parity exports ----------------------------------------------------------------------------
 void launch_ref_cells(const DevState& s, cudaStream_t st, int rep, const double* inv_l, const int* nc,
                       int* cell_of_tag, int* counts);
