@@ -48,6 +48,7 @@ struct mfa_ctx {
   cudaEvent_t ev[16];
   long long launches = 0;
   std::vector<void*> allocs;
+  double* stage = nullptr;  // 4 x 3N doubles for host <-> device state movement, made on first use
   std::string err;
   double rl_max = 0.;
 };
@@ -958,13 +959,20 @@ int mfa_get_step(mfa_ctx* ctx, int64_t* step) {
 }
 
 // ---- data movement --------------------------------------------------------------------------
+// The context's staging buffer for state movement (caller layout, 4 arrays of 3N doubles).
+static int staging(mfa_ctx* ctx, double** out) {
+  if (!ctx->stage) RET(dalloc(ctx, &ctx->stage, 12 * (size_t)ctx->N));
+  *out = ctx->stage;
+  return MFA_OK;
+}
+
 int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* force) {
   if (!ctx) return MFA_ERR_ARG;
   size_t n3 = 3 * (size_t)ctx->N;
   double* buf = nullptr;
   int nb = (r0 != nullptr) + (v != nullptr) + (a != nullptr) + (force != nullptr);
   if (nb == 0) return mfa_synchronize(ctx);
-  CK(cudaMallocAsync(&buf, n3 * 8 * nb, ctx->st));
+  RET(staging(ctx, &buf));
   double* p = buf;
   double *dr = r0 ? p : nullptr;
   if (r0) p += n3;
@@ -978,7 +986,6 @@ int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* for
   if (v) CK(cudaMemcpyAsync(v, dv, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
   if (a) CK(cudaMemcpyAsync(a, da, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
   if (force) CK(cudaMemcpyAsync(force, df, n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
-  CK(cudaFreeAsync(buf, ctx->st));
   RET(post_status(ctx));
   return check_status(ctx);
 }
@@ -986,17 +993,16 @@ int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* for
 int mfa_set_state(mfa_ctx* ctx, const double* r0, const double* v, const double* a) {
   if (!ctx) return MFA_ERR_ARG;
   size_t n3 = 3 * (size_t)ctx->N;
-  double *dr = nullptr, *dv = nullptr, *da = nullptr;
-  if (r0) { CK(cudaMallocAsync(&dr, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(dr, r0, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
-  if (v) { CK(cudaMallocAsync(&dv, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(dv, v, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
-  if (a) { CK(cudaMallocAsync(&da, n3 * 8, ctx->st)); CK(cudaMemcpyAsync(da, a, n3 * 8, cudaMemcpyHostToDevice, ctx->st)); }
+  double* buf = nullptr;
+  RET(staging(ctx, &buf));
+  double *dr = r0 ? buf : nullptr, *dv = v ? buf + n3 : nullptr, *da = a ? buf + 2 * n3 : nullptr;
+  if (r0) CK(cudaMemcpyAsync(dr, r0, n3 * 8, cudaMemcpyHostToDevice, ctx->st));
+  if (v) CK(cudaMemcpyAsync(dv, v, n3 * 8, cudaMemcpyHostToDevice, ctx->st));
+  if (a) CK(cudaMemcpyAsync(da, a, n3 * 8, cudaMemcpyHostToDevice, ctx->st));
   launch_scatter_state(ctx->S, ctx->st, dr, dv, da);
   // the lists stay valid unless some particle moved more than skin/2 from the last rebuild
   launch_refresh_views(ctx->S, ctx->C, ctx->st);
   rebuild(ctx, false);
-  if (dr) CK(cudaFreeAsync(dr, ctx->st));
-  if (dv) CK(cudaFreeAsync(dv, ctx->st));
-  if (da) CK(cudaFreeAsync(da, ctx->st));
   return mfa_synchronize(ctx);
 }
 
