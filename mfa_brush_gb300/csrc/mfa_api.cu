@@ -388,6 +388,11 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     C.a_wall_f[t] = (float)C.a_wall[t];
   }
   for (int d = 0; d < 3; ++d) C.cforce_f[d] = (float)C.const_force[d];
+  C.sig_f = (float)C.sig; C.gamma_f = (float)C.gamma; C.coul_rc2_f = (float)C.coul_rc2;
+  C.sqrt_alpha_f = (float)C.sqrt_alpha; C.inv_sqrt_pi_f = (float)C.inv_sqrt_pi; C.alpha_c_f = (float)C.alpha_c;
+  C.k_chain_f = (float)C.k_chain; C.inv_r_chain_2_f = (float)C.inv_r_chain_2; C.fene_xmax_f = (float)C.fene_xmax;
+  C.k_bend_f = (float)C.k_bend; C.alpha_eq_f = (float)C.alpha_eq; C.k_or_f = (float)C.k_or;
+  C.alpha_or_f = (float)C.alpha_or; C.bend_small_f = (float)C.bend_small;
   if (C.hist_dim > MFA_HIST_DIM_MAX) return fail(ctx, MFA_ERR_CAPACITY, "hist_dim exceeds MFA_HIST_DIM_MAX");
   // ---- pair tables ----------------------------------------------------------------------------
   std::vector<PairEntry<float>> tf(NPAIR);

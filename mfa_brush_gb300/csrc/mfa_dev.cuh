@@ -88,6 +88,10 @@ struct SimConst {
   // lookup; pairs whose own cut-off is 0 (head-head) are then listed too and dropped later.
   // 0 = cut-offs differ.
   float rl2_uni_f, scr2_uni_f;
+  // FP32 copies of the pair and bond constants: a double -> float conversion issues on the FP64
+  // pipe, so the mixed kernels read these instead of converting per thread
+  float sig_f, gamma_f, coul_rc2_f, sqrt_alpha_f, inv_sqrt_pi_f, alpha_c_f;
+  float k_chain_f, inv_r_chain_2_f, fene_xmax_f, k_bend_f, alpha_eq_f, k_or_f, alpha_or_f, bend_small_f;
 };
 
 // Per replica (device array, read through the L1).

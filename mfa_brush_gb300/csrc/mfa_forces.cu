@@ -22,6 +22,12 @@ namespace mfa {
 template <bool MIXED>
 using real_t = typename std::conditional<MIXED, float, double>::type;
 
+// A constant in the kernel's precision: the FP32 copy for MIXED, the double otherwise.
+template <bool MIXED>
+__device__ __forceinline__ real_t<MIXED> cst(double d, float f) {
+  if constexpr (MIXED) return f; else return d;
+}
+
 __device__ __forceinline__ double r2min_of(const SimConst& C, long long step) {
   if (!C.force_switch_on) return 0.;
   double r_time = (double)step * C.dt;
@@ -81,7 +87,7 @@ __device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, cons
     dn2 += dn[j] * dn[j];
     dp2 += dp[j] * dp[j];
   }
-  const real small = (real)C.bend_small;
+  const real small = cst<MIXED>(C.bend_small, C.bend_small_f);
   const real srp = sqrt(rp2), srn = sqrt(rn2);
   if (dn2 < small) {
     real u[3], nu = 0;
@@ -165,7 +171,8 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
       if (b >= lo && b <= hi) P[u].load(s, __ldg(&s.slot_of_tag[t0 + b]));
     }
     if (do_fene) {
-      const real kc = (real)C.k_chain, ir2 = (real)C.inv_r_chain_2, xm = (real)C.fene_xmax;
+      const real kc = cst<MIXED>(C.k_chain, C.k_chain_f), ir2 = cst<MIXED>(C.inv_r_chain_2, C.inv_r_chain_2_f),
+                 xm = cst<MIXED>(C.fene_xmax, C.fene_xmax_f);
       if (m > 0) {  // bond (m-1, m): this bead is the second partner
         real d[3];
         bead_delta<MIXED>(P[1], P[2], R, d);
@@ -185,7 +192,7 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
       }
     }
     if (do_bend) {
-      const real kb = (real)C.k_bend, aeq = (real)C.alpha_eq;
+      const real kb = cst<MIXED>(C.k_bend, C.k_bend_f), aeq = cst<MIXED>(C.alpha_eq, C.alpha_eq_f);
 #pragma unroll
       for (int u = 1; u <= 3; ++u) {  // the angle centred on bead c = m - 2 + u
         const int c = m - 2 + u;
@@ -221,7 +228,7 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
 #pragma unroll
       for (int j = 0; j < 3; ++j) { dn[j] = rp[j] * rn2 - rn[j] * dot; dn2 += dn[j] * dn[j]; }
       const real srp = sqrt(rp2), srn = sqrt(rn2);
-      if (dn2 < (real)C.bend_small) {
+      if (dn2 < cst<MIXED>(C.bend_small, C.bend_small_f)) {
         real u[3], nu = 0;
 #pragma unroll
         for (int j = 0; j < 3; ++j) { u[j] = rp[j] / srp - rn[j] / srn; nu += u[j] * u[j]; }
@@ -243,8 +250,8 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
         real ca = dot / sqrt(rp2 * rn2);
         alpha = (ca >= 1.0) ? 0. : acos(ca);
       }
-      const real da = alpha - (real)C.alpha_or;
-      const real fm = (real)C.k_or * da;
+      const real da = alpha - cst<MIXED>(C.alpha_or, C.alpha_or_f);
+      const real fm = cst<MIXED>(C.k_or, C.k_or_f) * da;
       const real sgn = (m == 0) ? (real)-1 : (real)1;
       F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
       if (EFLAG && m == 0) e4[3] += (real)0.5 * fm * da;
@@ -306,10 +313,10 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
   if (active) {
     const RepDesc& R = s.reps[rep];
     const long long step = R.s_time + *s.steps_done;
-    const real r2min = (real)r2min_of(C, step);
+    const real r2min = C.force_switch_on ? (real)r2min_of(C, step) : (real)0;
     const int ti = info_type(w);
     const int n = __ldg(&s.nn[i]);
-    const real sig = (real)C.sig, gam = (real)C.gamma;
+    const real sig = cst<MIXED>(C.sig, C.sig_f), gam = cst<MIXED>(C.gamma, C.gamma_f);
     const int p0 = R.p0;
     // own position / velocity
     int4 qi;
@@ -332,7 +339,7 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
     const double L0 = R.L[0], L1 = R.L[1], iL0 = R.invL[0], iL1 = R.invL[1];
     const unsigned long long seed = R.seed;
     const int* __restrict__ nb = s.nbr + i;
-    const real coul_rc2 = (real)C.coul_rc2;
+    const real coul_rc2 = cst<MIXED>(C.coul_rc2, C.coul_rc2_f);
     auto delta = [&](int j, real& dx, real& dy, real& dz) -> int {
       if constexpr (MIXED) {
         const int4 qj = __ldg(&s.pfx[j]);
@@ -455,9 +462,10 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
           const real rc2 = in_lj ? r2 : r2raw;
           const real r = sqrt(rc2), ir = (real)1 / r;
           const real qq = e.qq;
-          const real ec = erfc((real)C.sqrt_alpha * r);
+          const real sqa = cst<MIXED>(C.sqrt_alpha, C.sqrt_alpha_f);
+          const real ec = erfc(sqa * r);
           if (EFLAG) e_c += (info_mobile(wj) ? (real)0.5 : (real)1) * qq * ec * ir;
-          fs += (qq * (real)C.sqrt_alpha * (real)C.inv_sqrt_pi * (real)2 * exp(-(real)C.alpha_c * rc2) * ir +
+          fs += (qq * sqa * cst<MIXED>(C.inv_sqrt_pi, C.inv_sqrt_pi_f) * (real)2 * exp(-cst<MIXED>(C.alpha_c, C.alpha_c_f) * rc2) * ir +
                  qq * ec * ir * ir) * ir;
         }
       }

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
       const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
       const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
-      if (dx * dx + dy * dy + dz * dz > (float)C.skin_half2) *s.rebuild_flag = 1;
+      if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) *s.rebuild_flag = 1;
       if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(s.status, ST_NAN);
     }
   }
