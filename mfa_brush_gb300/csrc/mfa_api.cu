@@ -483,6 +483,10 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       R.inv_lc[d] = (double)nc / s.boundary[d];
       R.lc_f[d] = (float)(s.boundary[d] / nc);
       R.cpu_f[d] = (float)(512. * nc / ((d < 2) ? 4294967296.0 : 1073741824.0));
+      if (d == 2) {
+        R.zlim_f[0] = (float)(-s.boundary[2] / nc);
+        R.zlim_f[1] = (float)(s.boundary[2] + s.boundary[2] / nc);
+      }
     }
     R.ncell = R.nc[0] * R.nc[1] * R.nc[2];
     R.cell_off = cell_off;

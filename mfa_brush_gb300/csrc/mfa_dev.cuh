@@ -103,6 +103,7 @@ struct RepDesc {
   double inv_lc[3];     // neighbour-list grid
   float lc_f[3];        // list cell edge in sigma
   float cpu_f[3];       // list cells per 512 fixed-point units
+  float zlim_f[2];      // -l_cell, D + l_cell: a particle outside is out of the channel
   int nc[3];
   int cell_off, ncell;
   int p0, n_part, n_mon_tot;

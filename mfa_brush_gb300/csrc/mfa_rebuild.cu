@@ -41,18 +41,22 @@ __global__ void k_bin(DevState s, bool force) {
   if (i >= s.N) return;
   int w = s.info[i];
   const RepDesc& R = s.reps[info_rep(w)];
-  const double lz = 1. / R.inv_lc[2];
   int ix, iy, iz;
   if (s.mixed) {  // the list builder's integer formula on the fixed-point view
-    // (x, y need no check: the fixed-point view wraps them; the integrator flags NaN)
-    const double z = s.rz[i];
-    if (!(z >= -lz && z <= R.L[2] + lz)) atomicOr(s.status, isnan(z) ? ST_NAN : ST_OUT_OF_BOX);
+    // (x, y need no check: the fixed-point view wraps them; the integrator flags NaN); the z
+    // check in FP32, as FP64 compares and the cell-height division issue on the FP64 pipe
+    const double zd = s.rz[i];
+    const float z = d2f_fast(zd);
+    if (!(z >= R.zlim_f[0] && z <= R.zlim_f[1]))  // also false for NaN
+      atomicOr(s.status, (__double_as_longlong(zd) & 0x7FF0000000000000ll) == 0x7FF0000000000000ll ? ST_NAN
+                                                                                                : ST_OUT_OF_BOX);
     const int4 q = s.pfx[i];
     ix = (int)(((unsigned long long)(unsigned)q.x * (unsigned)R.nc[0]) >> 32);
     iy = (int)(((unsigned long long)(unsigned)q.y * (unsigned)R.nc[1]) >> 32);
     iz = (int)(((long long)q.z * R.nc[2]) >> 30);
     iz = min(max(iz, 0), R.nc[2] - 1);
   } else {
+    const double lz = 1. / R.inv_lc[2];
     double x = s.rx[i], y = s.ry[i], z = s.rz[i];
     if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
       atomicOr(s.status, ST_NAN);
@@ -190,7 +194,8 @@ __global__ void k_permute(DevState s, bool force) {
   s.tmp_info[i] = s.info[o];
 }
 
-__device__ __forceinline__ void write_views(const DevState& s, int i, const RepDesc& R, double x, double y, double z,
+// Writes the pair-kernel views of slot i and returns the fixed-point position (w in q.w).
+__device__ __forceinline__ int4 write_views(const DevState& s, int i, const RepDesc& R, double x, double y, double z,
                                             double vx, double vy, double vz, int w, int t) {
   int4 q;
   q.x = to_fx_periodic(x, R.sfx[0]);
@@ -199,11 +204,12 @@ __device__ __forceinline__ void write_views(const DevState& s, int i, const RepD
   q.w = w;
   if (s.mixed) {
     s.pfx[i] = q;
-    s.vf[i] = make_float4((float)vx, (float)vy, (float)vz, __int_as_float(t));
+    s.vf[i] = make_float4(d2f_fast(vx), d2f_fast(vy), d2f_fast(vz), __int_as_float(t));
   } else {
     s.pd[i] = mk_dbl4(x, y, z, __longlong_as_double((long long)w));
     s.vd[i] = mk_dbl4(vx, vy, vz, __longlong_as_double((long long)t));
   }
+  return q;
 }
 
 __global__ void k_copyback(DevState s, bool force) {
@@ -220,11 +226,7 @@ __global__ void k_copyback(DevState s, bool force) {
   s.info[i] = w;
   s.slot_of_tag[t] = i;
   const RepDesc& R = s.reps[info_rep(w)];
-  write_views(s, i, R, x, y, z, vx, vy, vz, w, t);
-  int4 q;
-  q.x = to_fx_periodic(x, R.sfx[0]);
-  q.y = to_fx_periodic(y, R.sfx[1]);
-  q.z = to_fx_z(z, R.sfx[2]);
+  int4 q = write_views(s, i, R, x, y, z, vx, vy, vz, w, t);
   q.w = 0;
   s.ref[i] = q;
 }
