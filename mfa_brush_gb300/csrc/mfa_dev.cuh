@@ -205,20 +205,29 @@ __device__ __forceinline__ float d2f_fast(double d) {
   return __uint_as_float(e <= 0 ? sgn : r);
 }
 
-// round(x) of a double with |x| < 2^51 to int64 with one FP64 add (2^52 + 2^51 magic).
-__device__ __forceinline__ long long d2ll_round_fast(double x) {
-  return __double_as_longlong(x + 6755399441055744.0) - 0x4338000000000000ll;
-}
-
 // ---------------------------------------------------------------------------------------------
 // Fixed-point positions
 // ---------------------------------------------------------------------------------------------
+// Nearest integer (ties away from zero) of d, for |d| < 2^62, from the bit pattern: one FP64
+// multiply forms d, the rounding is integer work (an FP64 magic-number add would be a second
+// operation on the slow FP64 pipe).
+__device__ __forceinline__ long long round_bits(double d) {
+  const long long b = __double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const int sh = 1075 - e;                        // fractional bits of the 53-bit mantissa
+  const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  unsigned long long r;
+  if (sh <= 0) r = m << (-sh);                    // already an integer (|d| >= 2^52)
+  else if (sh > 53) r = 0;                        // |d| < 1/2
+  else r = (m + (1ull << (sh - 1))) >> sh;
+  return (b < 0) ? -(long long)r : (long long)r;
+}
+
 __device__ __forceinline__ int to_fx_periodic(double x, double s) {
   // x in [0, L] -> [0, 2^32) modulo 2^32
-  long long v = d2ll_round_fast(x * s);
-  return (int)(unsigned int)(unsigned long long)v;
+  return (int)(unsigned int)(unsigned long long)round_bits(x * s);
 }
-__device__ __forceinline__ int to_fx_z(double z, double s) { return (int)d2ll_round_fast(z * s); }
+__device__ __forceinline__ int to_fx_z(double z, double s) { return (int)round_bits(z * s); }
 __device__ __forceinline__ int fx_diff(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
 
 // Minimum image of the reference: d - L*int(2 d / L) (fluid_fluid.f90:111-112).

@@ -121,11 +121,12 @@ __device__ __forceinline__ float wall93f(const SimConst& C, int t, float zl, flo
 
 // x -> wrapped x of verlet_positions.f90:170-186 (`> L` then `< 0`), decided on the bit pattern:
 // for positive doubles integer order equals numeric order, so no FP64 compare is issued.
+// The shift is chosen by integer selects, so one FP64 add is issued, not one per direction.
 __device__ __forceinline__ double wrap_bits(double x, double L, long long Lbits) {
   const long long b = __double_as_longlong(x);
-  if (b < 0) return (b == (long long)0x8000000000000000ull) ? x : x + L;  // -0.0 stays
-  if (b > Lbits) return x - L;
-  return x;
+  const long long lb = __double_as_longlong(L), nlb = lb ^ (long long)0x8000000000000000ull;
+  const long long ob = (b < 0 && b != (long long)0x8000000000000000ull) ? lb : (b > Lbits ? nlb : 0ll);
+  return x + __longlong_as_double(ob);  // x + 0 keeps x (and -0.0 + 0 = +0, a zero all the same)
 }
 
 // The integrator of the mixed-precision path with the FP64 work cut to the state accumulators
