@@ -237,22 +237,27 @@ __global__ void k_copyback(DevState s, bool force) {
 // order unless the row wraps in x, so a row is one contiguous slot range (two when it wraps).
 // Rows whose y/z distance from the particle exceeds the largest list cut-off of its type are
 // skipped, and each kept row is trimmed in x to the cells within that cut-off, which removes
-// about half of the candidates.  Each thread stages its list in shared memory (row stride
-// cap|1 keeps the banks distinct) and the block writes the list out row by row: the k-th
-// neighbours of 128 consecutive particles are 128 consecutive ints of nbr, so every store is
+// about half of the candidates.  Each thread stages its first NL_STAGE entries in shared memory
+// (row stride NL_STAGE|1 keeps the banks distinct) and the block writes them out row by row: the
+// k-th neighbours of 128 consecutive particles are 128 consecutive ints of nbr, so every store is
 // coalesced (scattered 4-byte stores into the column-major list cost read-modify-writes in HBM).
+// The fixed staging size keeps the shared memory (17 KB per block) independent of the list
+// capacity, so eight blocks fit on an SM.
 constexpr int NL_BLOCK = 128;
+// entries per particle staged in shared memory (the first NL_STAGE rows of the list are written
+// coalesced; a particle with more neighbours writes the rest straight to the list)
+constexpr int NL_STAGE = 32;
 
 template <bool MIXED, bool UNI>
-__global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
+__global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
-  extern __shared__ int nl_sh[];
+  __shared__ int nl_sh[NL_BLOCK * (NL_STAGE | 1)];
   __shared__ float rl2f[NPAIR];
   __shared__ double rl2d[NPAIR];
   __shared__ float rlmax[MAXT];
   __shared__ int blk_max;
-  const int cap = s.nbr_cap, pitch = cap | 1;
-  int* mine = nl_sh + threadIdx.x * pitch;
+  const int cap = s.nbr_cap;
+  int* mine = nl_sh + threadIdx.x * (NL_STAGE | 1);
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
     rl2d[k] = s.tabd[k].rlist2;
     rl2f[k] = s.tabf ? s.tabf[k].rlist2 : 0.f;
@@ -357,7 +362,8 @@ __global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
               hit = ddx * ddx + ddy * ddy + ddz * ddz < rl2d[ti * MAXT + info_type(wj)];
             }
             if (hit && j != i) {
-              if (cnt < cap) mine[cnt] = j;
+              if (cnt < NL_STAGE) mine[cnt] = j;
+              else if (cnt < cap) s.nbr[(size_t)cnt * s.Np + i] = j;  // rare: past the staged rows
               ++cnt;
             }
           }
@@ -371,7 +377,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
   }
   atomicMax(&blk_max, cnt);
   __syncthreads();
-  const int mx = blk_max;
+  const int mx = min(blk_max, NL_STAGE);
   if (i < s.N) {
     for (int k = 0; k < mx; ++k)
       if (k < cnt) s.nbr[(size_t)k * s.Np + i] = mine[k];
@@ -379,7 +385,6 @@ __global__ void __launch_bounds__(NL_BLOCK, 6) k_nlist(DevState s, bool force) {
   }
 }
 
-size_t nlist_smem(int cap) { return (size_t)NL_BLOCK * (size_t)(cap | 1) * sizeof(int); }
 
 __global__ void k_clear_flag(int* flag) { *flag = 0; }
 
@@ -399,16 +404,10 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   k_sort_cells<<<gC, B, 0, st>>>(s, force);
   k_permute<<<gN, B, 0, st>>>(s, force);
   k_copyback<<<gN, B, 0, st>>>(s, force);
-  const size_t shm = nlist_smem(s.nbr_cap);
-  static size_t shm_set[3] = {48 * 1024, 48 * 1024, 48 * 1024};
   const int var = s.mixed ? (s.rl2_uni > 0.f ? 2 : 1) : 0;
   auto kern = var == 2 ? k_nlist<true, true> : var == 1 ? k_nlist<true, false> : k_nlist<false, false>;
-  if (shm > shm_set[var]) {  // above 48 KB of dynamic shared memory needs an opt-in
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    shm_set[var] = shm;
-  }
   const int gl = (s.N + NL_BLOCK - 1) / NL_BLOCK;
-  kern<<<gl, NL_BLOCK, shm, st>>>(s, force);
+  kern<<<gl, NL_BLOCK, 0, st>>>(s, force);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -51,8 +51,7 @@ struct Acc {
 
 // ---- rebuild (cell sort + neighbour list); `force` runs it even when the flag is clear -------
 void launch_rebuild(const DevState& s, cudaStream_t st, bool force);
-// shared memory of the list builder for a capacity; capacities above NL_CAP_MAX are refused
-size_t nlist_smem(int cap);
+// largest neighbour-list capacity (entries per particle) a context may grow to
 constexpr int NL_CAP_MAX = 420;
 // ---- forces ------------------------------------------------------------------------------------
 // pair forces (fluid_fluid); accumulate = add into f, else overwrite; eflag = energies into acc;
