@@ -186,7 +186,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
-    ap.add_argument("--skin", type=float, default=0.5)
+    ap.add_argument("--skin", type=float, default=0.6)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
