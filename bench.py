@@ -186,7 +186,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
-    ap.add_argument("--skin", type=float, default=0.6)
+    ap.add_argument("--skin", default="auto",
+                    help="list skin in sigma, or 'auto': timed on 32 of the replicas at 0.4-0.7")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
@@ -216,6 +217,14 @@ def main():
     rep_idx, reps = shard.rank_replicas(args.replicas, args.seed, rank, world)
     systems, a_type, r0, v = configs.concat(reps)
     n_atoms = int(sum(s.n_part for s in systems))
+    tuned = None
+    if args.skin == "auto":
+        from mfa_brush_gb300 import tune
+        best, rates = tune.tune_skin(p, reps, precision=args.precision, device=local)
+        tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
+                 "unit": "G atom-steps/s on 32 replicas"}
+        args.skin = best
+    args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin)
 
     def barrier():
@@ -274,6 +283,7 @@ def main():
                        "replicas": args.replicas * world, "particles_per_gpu": n_atoms,
                        "particles_total": n_all, "seed": args.seed,
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
+                       "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
             "gpu_launches": int(launches + 10 * rebuilds),
@@ -293,6 +303,19 @@ def main():
             "value": fv, "unit": UNIT, "replicas": fk, "particles": int(fn), "steps": 100,
             "sample": "every 16th replica of the set, each alone in its own FP64 context, 10-step graphs",
             "speedup_of_value": value / world / fv}
+        # the same batch in the plain FP64 mode (precision alone, batching held fixed)
+        gd = md.MdSystem(p, systems, a_type, r0, v, precision="fp64", device=local, skin=args.skin)
+        for _ in range(2):
+            gd.step(CHUNK)
+        gd.synchronize()
+        gd.event_record(0)
+        for _ in range(10):
+            gd.step(CHUNK)
+        gd.event_record(1)
+        bv = n_atoms * 10 * CHUNK / (gd.event_elapsed(0, 1) / 1000.0)
+        gd.close()
+        line["batched_fp64"] = {"value": bv, "unit": UNIT, "steps": 10 * CHUNK,
+                                "speedup_of_value": value / world / bv}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         sample, n = [], 0

@@ -1,0 +1,42 @@
+"""Autotuning of the neighbour-list skin.
+
+The skin trades the list rebuild (sort + list build, whose frequency falls as the skin grows) for
+the pair kernel (whose lists lengthen with it).  The best value depends on the density, the
+temperature, the time step and the replica mix, so it is measured: the fused step is timed at
+each candidate skin on a sample of the replicas, over enough steps to include several rebuilds.
+"""
+import numpy as np
+
+from . import configs, md
+
+
+def sample_replicas(reps, n_sample):
+    """Every k-th replica, so that the sample spans the size distribution of the set."""
+    if len(reps) <= n_sample:
+        return list(reps)
+    idx = np.linspace(0, len(reps) - 1, n_sample).round().astype(int)
+    return [reps[k] for k in sorted(set(idx.tolist()))]
+
+
+def tune_skin(params, reps, candidates=(0.4, 0.5, 0.6, 0.7), n_sample=32, steps=80, warmup=20,
+              precision="mixed", device=0, chunk=10):
+    """Times mfa_step on a sample of `reps` (list of (System, a_type, r0, v)) at each candidate
+    skin; returns (best skin, {skin: atom-steps/s})."""
+    sample = sample_replicas(reps, n_sample)
+    systems, a_type, r0, v = configs.concat(sample)
+    n_atoms = int(sum(s.n_part for s in systems))
+    rates = {}
+    for skin in candidates:
+        g = md.MdSystem(params, systems, a_type, r0, v, precision=precision, device=device, skin=skin)
+        for _ in range(max(1, warmup // chunk)):
+            g.step(chunk)
+        g.synchronize()
+        g.event_record(0)
+        for _ in range(max(1, steps // chunk)):
+            g.step(chunk)
+        g.event_record(1)
+        ms = g.event_elapsed(0, 1)
+        g.close()
+        rates[float(skin)] = n_atoms * max(1, steps // chunk) * chunk / (ms / 1000.0)
+    best = max(rates, key=rates.get)
+    return best, rates

@@ -114,3 +114,11 @@ def test_small_channel_is_well_formed():
     keep[s.n_mon - 1 :: s.n_mon] = False
     bl = np.linalg.norm(d[keep], axis=1)
     assert bl.max() < 1.5 and bl.min() > 0.9
+
+
+def test_skin_tuner_sample_spans_the_set():
+    from mfa_brush_gb300 import tune
+    reps = list(range(256))
+    s = tune.sample_replicas(reps, 32)
+    assert len(s) == 32 and s[0] == 0 and s[-1] == 255 and s == sorted(s)
+    assert tune.sample_replicas(reps[:5], 32) == reps[:5]
