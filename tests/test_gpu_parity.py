@@ -284,3 +284,40 @@ def test_deterministic_and_momentum(gpu):
     g.fluid_fluid()
     f = g.state()[3]
     assert np.abs(f.sum(0)).max() < 1e-5 * np.abs(f).sum()
+
+
+def test_state_round_trip_pinned_and_pageable(gpu):
+    """mfa_set_state reads page-locked arrays directly and pageable ones through the staging
+    buffer; mfa_sync_to_host fills both kinds alike.  Both give the same state, and a round trip
+    of an unchanged state is exact and needs no list rebuild."""
+    torch = pytest.importorskip("torch")
+    from mfa_brush_gb300 import abi
+    p = configs.wca_params(gamma=5.0)
+    reps = [configs.brush_channel(15.0, 12.0, 0.2, 20, seed=11),
+            configs.brush_channel(18.0, 10.0, 0.15, 15, seed=12)]
+    systems, a_type, r0, v = configs.concat(reps)
+    g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed")
+    g.step(20)
+    n = g.n
+    pin = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    pag = [np.zeros((n, 3)) for _ in range(4)]
+    dp = abi.dptr
+    abi.check(g.lib.mfa_sync_to_host(g.ctx, dp(pin[0]), dp(pin[1]), dp(pin[2]), dp(pin[3])), g.ctx)
+    abi.check(g.lib.mfa_sync_to_host(g.ctx, dp(pag[0]), dp(pag[1]), dp(pag[2]), dp(pag[3])), g.ctx)
+    for x, y in zip(pin, pag):
+        assert np.array_equal(x, y)
+    rb = g.rebuild_count()
+    abi.check(g.lib.mfa_set_state(g.ctx, dp(pin[0]), dp(pin[1]), dp(pin[2])), g.ctx)
+    assert g.rebuild_count() == rb
+    out = [np.zeros((n, 3)) for _ in range(3)]
+    abi.check(g.lib.mfa_sync_to_host(g.ctx, dp(out[0]), dp(out[1]), dp(out[2]), None), g.ctx)
+    for x, y in zip(out, pin[:3]):
+        assert np.array_equal(x, y)
+    # a moved state (pageable) is taken, and the lists follow it
+    moved = pag[0].copy()
+    moved[:, 2] += 0.0  # same z
+    moved[:, 0] = (moved[:, 0] + 3.0) % np.array([s.boundary[0] for s in systems]).repeat([s.n_part for s in systems])
+    g.set_state(moved, None, None)
+    assert g.rebuild_count() == rb + 1
+    r_back = g.state()[0]
+    assert np.abs(r_back - moved).max() < 1e-12
