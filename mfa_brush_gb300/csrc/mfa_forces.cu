@@ -4,13 +4,18 @@
 //            One thread per particle walks its full Verlet list (no atomics, no Newton-3 scatter);
 //            each unordered pair is therefore evaluated from both sides, and the DPD noise is a
 //            Philox draw keyed on (seed, step, min tag, max tag) so both sides see the same g and
-//            momentum is conserved exactly in exact arithmetic.  Energies are halved per visit.
+//            momentum is conserved exactly in exact arithmetic.  Energies are halved per visit
+//            (a fixed wall bead has no list: its pairs count in full).
 //            MIXED: positions are fixed-point int4 (the int32 difference is the x,y minimum image),
-//            all pair arithmetic is FP32, the per-particle sum is FP32 and stored as FP64.
+//            all pair arithmetic is FP32, the per-particle sum is FP32 (the FP32 force array of
+//            the fused step, or added to the FP64 force).  In the fused mixed step the particle's
+//            bonded terms are evaluated by the same thread (BONDED), and with a single cut-off
+//            for every type pair the screening compares against one constant (UNI).
 // k_bonded : intra_molec.f90:16-188 (FENE), bending.f90:19-121 / bending_melt.f90:22-108 and
 //            orientation.f90:24-88.  Owner computes: the thread of bead m evaluates every bond,
 //            angle and orientation term that acts on m (terms centred on m-1, m, m+1) and adds
-//            its own share, so no two threads write one particle.
+//            its own share, so no two threads write one particle.  The body (bonded_of) is
+//            shared with the fused pair kernel.
 // k_wall   : fluid_wall.f90:77-125 (implicit 9-3 walls), FP64.
 // k_cforce : constant_force.f90:17-21 (Poiseuille body force m*g on every non-head bead).
 #include <type_traits>
@@ -400,79 +405,79 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
         if (screen(j)) jl[m++] = j;
       }
 #pragma unroll 2
-    for (int t = 0; t < m; ++t) {
-      const int j = jl[t];
-      real dx, dy, dz;
-      const int wj = delta(j, dx, dy, dz);
-      const real r2raw = dx * dx + dy * dy + dz * dz;
-      const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
-      const int fl = e.flags;
-      real r2 = r2raw;
-      const bool in_lj = r2raw < e.range2;
-      real fs = 0;  // force factor along d = r_i - r_j
-      if (in_lj) {
-        r2 = r2raw < r2min ? r2min : r2raw;
-        // MIXED: the hardware reciprocal (2 ulp) instead of the IEEE division sequence
-        real inv_r2;
-        if constexpr (MIXED) inv_r2 = __fdividef(1.f, r2); else inv_r2 = (real)1 / r2;
-        const real s2 = e.sig2 * inv_r2;
-        const real s6 = s2 * s2 * s2;
-        const real s12 = s6 * s6;
-        fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
-        // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
-        if (EFLAG) e_lj += (info_mobile(wj) ? (real)0.5 : (real)1) * e.eps4 * ((s12 - s6) - e.shift);
+      for (int t = 0; t < m; ++t) {
+        const int j = jl[t];
+        real dx, dy, dz;
+        const int wj = delta(j, dx, dy, dz);
+        const real r2raw = dx * dx + dy * dy + dz * dz;
+        const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
+        const int fl = e.flags;
+        real r2 = r2raw;
+        const bool in_lj = r2raw < e.range2;
+        real fs = 0;  // force factor along d = r_i - r_j
+        if (in_lj) {
+          r2 = r2raw < r2min ? r2min : r2raw;
+          // MIXED: the hardware reciprocal (2 ulp) instead of the IEEE division sequence
+          real inv_r2;
+          if constexpr (MIXED) inv_r2 = __fdividef(1.f, r2); else inv_r2 = (real)1 / r2;
+          const real s2 = e.sig2 * inv_r2;
+          const real s6 = s2 * s2 * s2;
+          const real s12 = s6 * s6;
+          fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
+          // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
+          if (EFLAG) e_lj += (info_mobile(wj) ? (real)0.5 : (real)1) * e.eps4 * ((s12 - s6) - e.shift);
+        }
+        const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
+        if (dpd) {
+          real vjx, vjy, vjz;
+          int tag_j;
+          if constexpr (MIXED) {
+            float4 v4 = __ldg(&s.vf[j]);
+            vjx = v4.x; vjy = v4.y; vjz = v4.z;
+            tag_j = __float_as_int(v4.w) - p0;
+          } else {
+            dbl4 v4 = s.vd[j];
+            vjx = v4.x; vjy = v4.y; vjz = v4.z;
+            tag_j = (int)__double_as_longlong(v4.w) - p0;
+          }
+          real r, ir;
+          if constexpr (MIXED) {  // one hardware reciprocal square root (2 ulp)
+            ir = rsqrtf(r2);
+            r = r2 * ir;
+          } else {
+            r = sqrt(r2);
+            ir = (real)1 / r;
+          }
+          real wr, wd;
+          if (C.dpd_weight1) {
+            wr = wd = 1;
+          } else {
+            wr = (real)1 - r * ((fl & PF_DPD_OWN) ? e.inv_dpd_rc : e.inv_rc);
+            wd = wr * wr;
+          }
+          real g;
+          if constexpr (MIXED) g = pair_gauss_f(seed, step, tag_i, tag_j);
+          else g = pair_gauss_d(seed, step, tag_i, tag_j);
+          const real rdot = ((vix - vjx) * dx + (viy - vjy) * dy + (viz - vjz) * dz) * ir;
+          fs += (sig * wr * g - gam * wd * rdot) * ir;
+        }
+        if (fl & PF_COUL) {
+          const bool in_c = (coul_rc2 > 0) ? (r2raw < coul_rc2) : in_lj;
+          if (in_c) {
+            const real rc2 = in_lj ? r2 : r2raw;
+            const real r = sqrt(rc2), ir = (real)1 / r;
+            const real qq = e.qq;
+            const real sqa = cst<MIXED>(C.sqrt_alpha, C.sqrt_alpha_f);
+            const real ec = erfc(sqa * r);
+            if (EFLAG) e_c += (info_mobile(wj) ? (real)0.5 : (real)1) * qq * ec * ir;
+            const real isp = cst<MIXED>(C.inv_sqrt_pi, C.inv_sqrt_pi_f), ac = cst<MIXED>(C.alpha_c, C.alpha_c_f);
+            fs += (qq * sqa * isp * (real)2 * exp(-ac * rc2) * ir + qq * ec * ir * ir) * ir;
+          }
+        }
+        fx += fs * dx;
+        fy += fs * dy;
+        fz += fs * dz;
       }
-      const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
-      if (dpd) {
-        real vjx, vjy, vjz;
-        int tag_j;
-        if constexpr (MIXED) {
-          float4 v4 = __ldg(&s.vf[j]);
-          vjx = v4.x; vjy = v4.y; vjz = v4.z;
-          tag_j = __float_as_int(v4.w) - p0;
-        } else {
-          dbl4 v4 = s.vd[j];
-          vjx = v4.x; vjy = v4.y; vjz = v4.z;
-          tag_j = (int)__double_as_longlong(v4.w) - p0;
-        }
-        real r, ir;
-        if constexpr (MIXED) {  // one hardware reciprocal square root (2 ulp)
-          ir = rsqrtf(r2);
-          r = r2 * ir;
-        } else {
-          r = sqrt(r2);
-          ir = (real)1 / r;
-        }
-        real wr, wd;
-        if (C.dpd_weight1) {
-          wr = wd = 1;
-        } else {
-          wr = (real)1 - r * ((fl & PF_DPD_OWN) ? e.inv_dpd_rc : e.inv_rc);
-          wd = wr * wr;
-        }
-        real g;
-        if constexpr (MIXED) g = pair_gauss_f(seed, step, tag_i, tag_j);
-        else g = pair_gauss_d(seed, step, tag_i, tag_j);
-        const real rdot = ((vix - vjx) * dx + (viy - vjy) * dy + (viz - vjz) * dz) * ir;
-        fs += (sig * wr * g - gam * wd * rdot) * ir;
-      }
-      if (fl & PF_COUL) {
-        const bool in_c = (coul_rc2 > 0) ? (r2raw < coul_rc2) : in_lj;
-        if (in_c) {
-          const real rc2 = in_lj ? r2 : r2raw;
-          const real r = sqrt(rc2), ir = (real)1 / r;
-          const real qq = e.qq;
-          const real sqa = cst<MIXED>(C.sqrt_alpha, C.sqrt_alpha_f);
-          const real ec = erfc(sqa * r);
-          if (EFLAG) e_c += (info_mobile(wj) ? (real)0.5 : (real)1) * qq * ec * ir;
-          fs += (qq * sqa * cst<MIXED>(C.inv_sqrt_pi, C.inv_sqrt_pi_f) * (real)2 * exp(-cst<MIXED>(C.alpha_c, C.alpha_c_f) * rc2) * ir +
-                 qq * ec * ir * ir) * ir;
-        }
-      }
-      fx += fs * dx;
-      fy += fs * dy;
-      fz += fs * dz;
-    }
     }
   }
   real eb[4] = {0, 0, 0, 0};
