@@ -187,6 +187,19 @@ typedef struct mfa_energies {
   double inv_n;             /* 1/(n_mon_tot - n_chain) (init_params.f90:479-481)              */
 } mfa_energies;
 
+/* Observation quantities of one replica (observation.f90 and verlet_velocities.f90:18). */
+typedef struct mfa_observables {
+  int64_t step;             /* absolute step of the positions and velocities used               */
+  double rg2_brush[3];      /* mean over brush chains of the per-axis Rg^2, chains unfolded bond
+                               by bond (observation.f90:187-201,214-245)                        */
+  double rg2_melt[3];       /* the same over the melt chains (observation.f90:262-272; chains
+                               counted from the first melt particle)                            */
+  double momentum[3];       /* sum of m v over the mobile particles (observation.f90:286-291)   */
+  double f_heads[2][3];     /* minus the summed force on the heads of chains 1..n_chain/2 and of
+                               the other chains, at the last energy record (verlet_velocities.f90:18,
+                               observation.f90:324-327)                                          */
+} mfa_observables;
+
 typedef struct mfa_ctx mfa_ctx;
 
 /* ---- library / device ------------------------------------------------------------------ */
@@ -273,6 +286,10 @@ int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* for
 int mfa_set_state(mfa_ctx* ctx, const double* r0, const double* v, const double* a);
 /* Energies of the last energy record, one mfa_energies per replica. */
 int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out);
+/* Observation quantities of every replica (one mfa_observables each) on the current state; the
+   head forces are those of the last energy record (mfa_step every energy_every steps, or the
+   last mfa_verlet_velocities call).                                                           */
+int mfa_observe(mfa_ctx* ctx, mfa_observables* out);
 /* Accumulated profiles of replica rep: dens[hist_dim*3], vsum[hist_dim*3*3], v2sum[...],
    layout [bin][species][dim]; species 0 brush, 1 melt, 2 particle 4.  *n_obs = steps summed. */
 int mfa_get_profiles(mfa_ctx* ctx, int32_t rep, double* dens, double* vsum, double* v2sum,

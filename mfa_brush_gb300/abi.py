@@ -99,6 +99,15 @@ class Energies(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Observables(C.Structure):
+    _fields_ = [("step", i64), ("rg2_brush", f64 * 3), ("rg2_melt", f64 * 3), ("momentum", f64 * 3),
+                ("f_heads", (f64 * 3) * 2)]
+
+    def as_dict(self):
+        return {"step": self.step, "rg2_brush": list(self.rg2_brush), "rg2_melt": list(self.rg2_melt),
+                "momentum": list(self.momentum), "f_heads": [list(self.f_heads[0]), list(self.f_heads[1])]}
+
+
 P = C.POINTER
 vp = C.c_void_p
 dp = P(f64)
@@ -144,6 +153,7 @@ SIGNATURES = {
     "mfa_set_state": (i32, [vp, dp, dp, dp]),
     "mfa_get_energies": (i32, [vp, P(Energies)]),
     "mfa_get_profiles": (i32, [vp, i32, dp, dp, dp, P(i64)]),
+    "mfa_observe": (i32, [vp, P(Observables)]),
     "mfa_reset_profiles": (i32, [vp]),
     "mfa_cell_list": (i32, [vp, i32, i32, ip, ip, i32, ip]),
     "mfa_cell_neigh_list": (i32, [ip, i32, ip]),

@@ -49,6 +49,7 @@ struct mfa_ctx {
   long long launches = 0;
   std::vector<void*> allocs;
   double* stage = nullptr;  // 4 x 3N doubles for host <-> device state movement, made on first use
+  double* obs = nullptr;    // [nrep][9] of mfa_observe, made on first use
   std::string err;
   double rl_max = 0.;
 };
@@ -844,6 +845,8 @@ int mfa_verlet_velocities(mfa_ctx* ctx, mfa_energies* e) {
   if (!ctx) return MFA_ERR_ARG;
   int r;
   if ((r = zero_call_slot(ctx, O_TFLUID))) return r;
+  for (int k = 0; k < 6; ++k)
+    if ((r = zero_call_slot(ctx, O_FH + k))) return r;
   launch_integrate(ctx->S, ctx->C, ctx->st, 1, false, true, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -1046,6 +1049,34 @@ int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out) {
   int r = check_status(ctx);
   if (r) return r;
   for (int k = 0; k < ctx->nrep; ++k) fill_energies(ctx, h.data(), k, &out[k]);
+  return MFA_OK;
+}
+
+int mfa_observe(mfa_ctx* ctx, mfa_observables* out) {
+  if (!ctx || !out) return MFA_ERR_ARG;
+  const int R = ctx->nrep;
+  if (!ctx->obs) RET(dalloc(ctx, &ctx->obs, (size_t)9 * R));
+  launch_observe(ctx->S, ctx->C, ctx->st, ctx->obs);
+  ctx->launches += 1;
+  std::vector<double> h((size_t)9 * R), a((size_t)NOBS * R);
+  CK(cudaMemcpyAsync(h.data(), ctx->obs, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+  const double* src = ctx->last_source == 2 ? ctx->acc_call : ctx->rec;
+  CK(cudaMemcpyAsync(a.data(), src, sizeof(double) * a.size(), cudaMemcpyDeviceToHost, ctx->st));
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (r) return r;
+  for (int k = 0; k < R; ++k) {
+    mfa_observables& o = out[k];
+    std::memset(&o, 0, sizeof o);
+    o.step = ctx->sys[k].s_time + ctx->host_steps;
+    for (int d = 0; d < 3; ++d) {
+      o.rg2_brush[d] = h[(size_t)9 * k + d];
+      o.rg2_melt[d] = h[(size_t)9 * k + 3 + d];
+      o.momentum[d] = h[(size_t)9 * k + 6 + d];
+      o.f_heads[0][d] = a[(size_t)(O_FH + d) * R + k];
+      o.f_heads[1][d] = a[(size_t)(O_FH + 3 + d) * R + k];
+    }
+  }
   return MFA_OK;
 }
 

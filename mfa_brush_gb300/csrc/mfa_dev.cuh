@@ -21,8 +21,9 @@ namespace mfa {
 
 constexpr int MAXT = 6;
 constexpr int NPAIR = MAXT * MAXT;
-constexpr int NOBS = 12;  // per-replica energy accumulator slots
-enum Obs { O_VFF = 0, O_VFW, O_VWW, O_VINTRA, O_VBEND, O_VBENDM, O_VOR, O_VCOUL, O_TFLUID, O_VCOULK, O_VDIP };
+constexpr int NOBS = 17;  // per-replica accumulator slots (energies, head forces)
+enum Obs { O_VFF = 0, O_VFW, O_VWW, O_VINTRA, O_VBEND, O_VBENDM, O_VOR, O_VCOUL, O_TFLUID, O_VCOULK, O_VDIP,
+           O_FH = 11 /* 6 slots: -sum of head forces, chains 1..n_chain/2 (xyz) then the others */ };
 
 // status bits
 constexpr unsigned ST_NLIST_OVERFLOW = 1u, ST_OUT_OF_BOX = 2u, ST_NAN = 4u;

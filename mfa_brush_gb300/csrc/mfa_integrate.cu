@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
   const bool mob = inside && info_mobile(w);
   const int rep = info_rep(w);
   double ke = 0., efw = 0.;
+  double fh[6] = {0., 0., 0., 0., 0., 0.};  // minus the head force, by half of the chains
   if (mob) {
     const RepDesc& R = s.reps[rep];
     const int t = info_type(w);
@@ -66,6 +67,10 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       vy = vy + C.half_dt * ay;
       vz = vz + C.half_dt * az;
       if (info_head(w)) {
+        if (EFLAG) {  // f_on_heads before the heads are held (verlet_velocities.f90:18)
+          const int h = (s.tag[i] - R.p0) / R.n_mon < R.n_chain / 2 ? 0 : 3;
+          fh[h] = -Fx; fh[h + 1] = -Fy; fh[h + 2] = -Fz;
+        }
         vx = vy = vz = 0.;
         ax = ay = az = 0.;
         if (MODE == 1) { s.fx[i] = 0.; s.fy[i] = 0.; s.fz[i] = 0.; }
@@ -103,6 +108,7 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
   if (EFLAG && MODE >= 1) {
     add_obs(acc.col(O_TFLUID), rep, ke, mob, acc.nrep);
     if (ADDEXT && C.wall == 2) add_obs(acc.col(O_VFW), rep, efw, mob, acc.nrep);
+    for (int k = 0; k < 6; ++k) add_obs(acc.col(O_FH + k), rep, fh[k], mob, acc.nrep);
   }
 }
 
@@ -149,6 +155,7 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
   const bool mob = inside && info_mobile(w);
   const int rep = info_rep(w);
   float ke = 0.f, efw = 0.f;
+  float fh[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // minus the head force, by half of the chains
   if (mob) {
     const RepDesc& R = s.reps[rep];
     const int t = info_type(w);
@@ -176,6 +183,10 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
       const float im = C.inv_mass_f[t];
       ax = Fx * im; ay = Fy * im; az = Fz * im;
       if (info_head(w)) {
+        if (EFLAG) {  // f_on_heads before the heads are held (verlet_velocities.f90:18)
+          const int h = (s.tag[i] - R.p0) / R.n_mon < R.n_chain / 2 ? 0 : 3;
+          fh[h] = -Fx; fh[h + 1] = -Fy; fh[h + 2] = -Fz;
+        }
         vx = vy = vz = 0.;
         ax = ay = az = 0.f;
         Fx = Fy = Fz = 0.f;
@@ -222,6 +233,7 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
   if (EFLAG && MODE >= 1) {
     add_obs(acc.col(O_TFLUID), rep, (double)ke, mob, acc.nrep);
     if (FUSED && C.wall == 2) add_obs(acc.col(O_VFW), rep, (double)efw, mob, acc.nrep);
+    for (int k = 0; k < 6; ++k) add_obs(acc.col(O_FH + k), rep, (double)fh[k], mob, acc.nrep);
   }
 }
 
@@ -328,6 +340,77 @@ __global__ void k_record(Acc acc, double* out) {
   if (k >= n) return;
   out[k] = acc.a[k];
   acc.a[k] = 0.;
+}
+
+// Observation quantities (observation.f90): one block per replica.  Rg^2 of each chain from its
+// bonded beads unfolded one bond at a time (a coordinate that jumps by more than half the box
+// from the previous bead is moved by one box length, observation.f90:187-201, all three axes as
+// there), about the chain's centre of mass; averaged over the brush chains and over the melt
+// chains (taken from the first melt particle on; the reference's melt loop starts at chain index
+// n_chain with the melt stride, observation.f90:262, which only agrees when n_mon_d = n_mon).
+// Momentum: sum of m v over the mobile particles.  Partial sums per thread, then a fixed-order
+// tree: the result does not depend on timing.
+constexpr int OBS_THREADS = 128;
+
+__global__ void __launch_bounds__(OBS_THREADS) k_observe(DevState s, SimConst C, double* out) {
+  __shared__ double part[OBS_THREADS][9];
+  const int r = blockIdx.x;
+  const RepDesc& R = s.reps[r];
+  double acc[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
+  const int nb = R.n_chain, nm = (R.n_mon_d > 0) ? R.n_chain_d : 0;
+  const double half[3] = {0.5 * R.L[0], 0.5 * R.L[1], 0.5 * R.L[2]};
+  for (int c = threadIdx.x; c < nb + nm; c += OBS_THREADS) {
+    const bool brush = c < nb;
+    const int len = brush ? R.n_mon : R.n_mon_d;
+    const int t0 = R.p0 + (brush ? c * R.n_mon : R.part_init_d + (c - nb) * R.n_mon_d);
+    double cm[3] = {0., 0., 0.}, rg[3] = {0., 0., 0.};
+    for (int pass = 0; pass < 2; ++pass) {
+      double prev[3] = {0., 0., 0.};
+      for (int b = 0; b < len; ++b) {
+        const int slot = s.slot_of_tag[t0 + b];
+        double p[3] = {s.rx[slot], s.ry[slot], s.rz[slot]};
+        if (b > 0) {
+          for (int d = 0; d < 3; ++d) {
+            if (p[d] - prev[d] > half[d]) p[d] -= R.L[d];
+            else if (prev[d] - p[d] > half[d]) p[d] += R.L[d];
+          }
+        }
+        for (int d = 0; d < 3; ++d) {
+          prev[d] = p[d];
+          if (pass == 0) cm[d] += p[d];
+          else rg[d] += (p[d] - cm[d]) * (p[d] - cm[d]);
+        }
+      }
+      if (pass == 0)
+        for (int d = 0; d < 3; ++d) cm[d] /= (double)len;
+    }
+    for (int d = 0; d < 3; ++d) acc[(brush ? 0 : 3) + d] += rg[d] / (double)len;
+  }
+  for (int t = threadIdx.x; t < R.n_mon_tot; t += OBS_THREADS) {
+    const int slot = s.slot_of_tag[R.p0 + t];
+    const double m = C.mass[info_type(s.info[slot])];
+    acc[6] += m * s.vx[slot];
+    acc[7] += m * s.vy[slot];
+    acc[8] += m * s.vz[slot];
+  }
+  for (int k = 0; k < 9; ++k) part[threadIdx.x][k] = acc[k];
+  __syncthreads();
+  for (int w = OBS_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 9; ++k) part[threadIdx.x][k] += part[threadIdx.x + w][k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int d = 0; d < 3; ++d) {
+      out[9 * r + d] = nb > 0 ? part[0][d] / (double)nb : 0.;
+      out[9 * r + 3 + d] = nm > 0 ? part[0][3 + d] / (double)nm : 0.;
+      out[9 * r + 6 + d] = part[0][6 + d];
+    }
+  }
+}
+
+void launch_observe(const DevState& s, const SimConst& C, cudaStream_t st, double* out) {
+  k_observe<<<s.nrep, OBS_THREADS, 0, st>>>(s, C, out);
 }
 
 void launch_record(Acc acc, double* out, cudaStream_t st) {

@@ -72,6 +72,8 @@ void launch_integrate(const DevState& s, const SimConst& C, cudaStream_t st, int
                       bool eflag, Acc acc);
 void launch_profiles(const DevState& s, const SimConst& C, cudaStream_t st, double* prof, int hist);
 void launch_record(Acc acc, double* out, cudaStream_t st);
+// observation quantities per replica: out[9 r + 0..2] brush Rg^2, 3..5 melt Rg^2, 6..8 momentum
+void launch_observe(const DevState& s, const SimConst& C, cudaStream_t st, double* out);
 // ---- host <-> device layout ----------------------------------------------------------------------
 // canonical AoS (3*tag+d) <-> slot order
 void launch_scatter_state(const DevState& s, cudaStream_t st, const double* r, const double* v,

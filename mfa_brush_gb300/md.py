@@ -239,6 +239,12 @@ class MdSystem:
         self._ck(self.lib.mfa_get_energies(self.ctx, e))
         return [x.as_dict() for x in e]
 
+    def observe(self):
+        """observation.f90 quantities of every replica: Rg^2 (brush, melt), momentum, head forces."""
+        o = (abi.Observables * self.nrep)()
+        self._ck(self.lib.mfa_observe(self.ctx, o))
+        return [x.as_dict() for x in o]
+
     def state(self):
         r, v, a, f = (np.zeros((self.n, 3)) for _ in range(4))
         self._ck(self.lib.mfa_sync_to_host(self.ctx, abi.dptr(r), abi.dptr(v), abi.dptr(a), abi.dptr(f)))

@@ -295,6 +295,7 @@ typedef struct orc_sys {
   int *part_in_cell, *r_nei, *l_nei, *cell_neigh_ls; /* 1-based particle ids, 0 = none */
   /* energies */
   double v_ff, v_coul, v_fw, v_ww, v_intra, v_bend, v_bend_melt, v_or, t_fluid;
+  double f_heads[6];  /* -sum of the head forces, chains 1..n_chain/2 then the others */
   double r_2_min;
   int64_t step;       /* absolute step being computed: s_time + i_time - 1 */
   int i_time;
@@ -529,6 +530,59 @@ int64_t orc_get_step(const orc_sys* o) { return o->step; }
 void orc_set_r2min(orc_sys* o, double r2min) { o->r_2_min = r2min; }
 
 /* Energies in mfa_energies field order (step excluded). */
+/* Observation quantities (observation.f90:187-291): out[0..2] brush Rg^2 per axis (chains unfolded
+ * one bond at a time, observation.f90:187-201, then about the centre of mass, 214-245), out[3..5]
+ * the same for the melt chains counted from the first melt particle (the reference's loop at
+ * observation.f90:262 starts at chain index n_chain with the melt stride, which agrees only when
+ * n_mon_d = n_mon), out[6..8] the momentum (286-291), out[9..14] the head forces of the last
+ * verlet_velocities. */
+static void chain_rg2(const orc_sys* o, int t0, int len, double* rg) {
+  const double* L = o->s.boundary;
+  double cm[3] = {0, 0, 0}, prev[3] = {0, 0, 0};
+  double* sp = (double*)malloc(sizeof(double) * 3 * (size_t)len);
+  for (int b = 0; b < len; ++b) {
+    for (int d = 0; d < 3; ++d) {
+      double x = o->r0[3 * (t0 + b) + d];
+      if (b > 0) {
+        if (x - prev[d] > 0.5 * L[d]) x -= L[d];
+        else if (prev[d] - x > 0.5 * L[d]) x += L[d];
+      }
+      prev[d] = x;
+      sp[3 * b + d] = x;
+      cm[d] += x;
+    }
+  }
+  for (int d = 0; d < 3; ++d) cm[d] /= (double)len;
+  for (int d = 0; d < 3; ++d) {
+    double acc = 0.;
+    for (int b = 0; b < len; ++b) acc += (sp[3 * b + d] - cm[d]) * (sp[3 * b + d] - cm[d]);
+    rg[d] = acc / (double)len;
+  }
+  free(sp);
+}
+
+void orc_observe(const orc_sys* o, double* out) {
+  for (int k = 0; k < 15; ++k) out[k] = 0.;
+  const mfa_system* s = &o->s;
+  double rg[3];
+  for (int c = 0; c < s->n_chain; ++c) {
+    chain_rg2(o, c * s->n_mon, s->n_mon, rg);
+    for (int d = 0; d < 3; ++d) out[d] += rg[d];
+  }
+  if (s->n_chain > 0)
+    for (int d = 0; d < 3; ++d) out[d] /= (double)s->n_chain;
+  if (s->n_mon_d > 0 && s->n_chain_d > 0) {
+    for (int c = 0; c < s->n_chain_d; ++c) {
+      chain_rg2(o, o->part_init_d + c * s->n_mon_d, s->n_mon_d, rg);
+      for (int d = 0; d < 3; ++d) out[3 + d] += rg[d];
+    }
+    for (int d = 0; d < 3; ++d) out[3 + d] /= (double)s->n_chain_d;
+  }
+  for (int i = 0; i < o->nm; ++i)
+    for (int d = 0; d < 3; ++d) out[6 + d] += o->mass[i] * o->v[3 * i + d];
+  for (int k = 0; k < 6; ++k) out[9 + k] = o->f_heads[k];
+}
+
 void orc_get_energies(const orc_sys* o, double* e) {
   e[0] = o->v_ff; e[1] = o->v_fw; e[2] = o->v_ww; e[3] = o->v_intra;
   e[4] = o->v_bend; e[5] = o->v_bend_melt; e[6] = o->v_or; e[7] = o->v_coul; e[8] = o->t_fluid;
@@ -1091,6 +1145,12 @@ void orc_verlet_positions(orc_sys* o) {
 /* verlet_velocities (verlet_velocities.f90:25-178) */
 void orc_verlet_velocities(orc_sys* o) {
   const double dt = o->p.dt;
+  /* f_on_heads (verlet_velocities.f90:18), summed as fort.80 writes it (observation.f90:324-327) */
+  for (int k = 0; k < 6; ++k) o->f_heads[k] = 0.;
+  for (int c = 0; c < o->s.n_chain; ++c) {
+    const int h = c * o->s.n_mon, half = (c < o->s.n_chain / 2) ? 0 : 3;
+    for (int d = 0; d < 3; ++d) o->f_heads[half + d] -= o->force[3 * h + d];
+  }
   for (int i = 0; i < o->nm; ++i)
     for (int d = 0; d < 3; ++d) {
       o->a[3 * i + d] = o->force[3 * i + d] * o->inv_mass[i];

@@ -69,6 +69,7 @@ def lib():
             "orc_get_step": (C.c_int64, [vp]),
             "orc_set_r2min": (None, [vp, C.c_double]),
             "orc_get_energies": (None, [vp, dp]),
+            "orc_observe": (None, [vp, dp]),
             "orc_pair_gauss": (C.c_double, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32]),
             "orc_philox": (None, [C.c_uint64, C.c_int64, C.c_uint32, C.c_uint32, P(C.c_uint32)]),
         }
@@ -139,6 +140,13 @@ class Oracle:
         # orc_<routine>(handle) pass-throughs: fluid_fluid, fluid_wall, intra_molec, ...
         f = getattr(lib(), "orc_" + name)
         return lambda *a: f(self.h, *a)
+
+    def observe(self):
+        """observation.f90 quantities (see orc_observe)."""
+        out = np.zeros(15)
+        self.L.orc_observe(self.h, _d(out))
+        return {"rg2_brush": out[0:3].tolist(), "rg2_melt": out[3:6].tolist(), "momentum": out[6:9].tolist(),
+                "f_heads": [out[9:12].tolist(), out[12:15].tolist()]}
 
     def cell_info(self):
         nm = self.system.n_mon_tot

@@ -226,3 +226,29 @@ def test_two_liquid_poiseuille_channel(gpu, oracle_mod, precision):
         # a bead within ~1e-7 sigma of a bin edge may land in the neighbouring bin
         assert np.abs(dg - do).sum() <= 8
         assert np.abs(vg.sum(0) - vo.sum(0)).max() < 1e-3 * max(1.0, np.abs(vo).sum())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_observation_quantities(gpu, try_deck, oracle_mod, precision):
+    """mfa_observe against the oracle's observation.f90 restatement after five steps: brush and
+    melt Rg^2 per axis, total momentum, and the summed head forces of the last velocity step."""
+    inp = melt_brush_inputs(try_deck)
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(14.0, 12.0, 0.15, 16, rho=0.85, n_mon_d=10, seed=9, max_fill=0.75)
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    if precision == "fp64":
+        for _ in range(5):
+            g.md_step()
+    else:
+        g.step(5)
+    o.step(5, 1, 0)
+    og, oo = g.observe()[0], o.observe()
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    for key in ("rg2_brush", "rg2_melt"):
+        assert np.allclose(og[key], oo[key], rtol=tol, atol=0), key
+    m = np.array([p.mass_type[t - 1] for t in a_type[: s.n_mon_tot]])
+    scale = np.abs(m[:, None] * o.state()[1][: s.n_mon_tot]).sum()
+    assert np.abs(np.array(og["momentum"]) - np.array(oo["momentum"])).max() < tol * scale
+    fh, fo = np.array(og["f_heads"]), np.array(oo["f_heads"])
+    assert np.abs(fh - fo).max() < (1e-9 if precision == "fp64" else 1e-5) * np.abs(fo).max()
