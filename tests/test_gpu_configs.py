@@ -252,3 +252,49 @@ def test_observation_quantities(gpu, try_deck, oracle_mod, precision):
     assert np.abs(np.array(og["momentum"]) - np.array(oo["momentum"])).max() < tol * scale
     fh, fo = np.array(og["f_heads"]), np.array(oo["f_heads"])
     assert np.abs(fh - fo).max() < (1e-9 if precision == "fp64" else 1e-5) * np.abs(fo).max()
+
+
+def test_ragged_batch_edge_cases(gpu, oracle_mod):
+    """A batch of a pure-solvent replica, a one-chain-per-wall replica and a short-box replica:
+    every replica against its own FP64 oracle after five drop-in steps, and the same batch built
+    with a list capacity far too small (the context grows it at start-up)."""
+    p = configs.wca_params(gamma=5.0)
+    reps = [configs.brush_channel(10.0, 8.0, 0.0, 10, seed=51),
+            configs.brush_channel(12.0, 10.0, 1.0 / 144.0, 25, seed=52),
+            configs.brush_channel(7.5, 12.0, 0.2, 8, seed=53)]
+    assert reps[0][0].n_chain == 0 and reps[1][0].n_chain == 2
+    systems, a_type, r0, v = configs.concat(reps)
+    for cap in (0, 4):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="fp64", nbr_capacity=cap)
+        for _ in range(5):
+            g.md_step()
+        r, vv, _, _ = g.state()
+        off = 0
+        for (s, at, rr, v0) in reps:
+            o = oracle_mod.Oracle(p, s, at, rr, v0)
+            o.step(5, 1, 0)
+            ro, vo, _, _ = o.state()
+            n = s.n_part
+            L = np.array(list(s.boundary))
+            d = r[off:off + n] - ro
+            d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+            assert np.abs(d).max() < 1e-9
+            assert np.abs(vv[off:off + n] - vo).max() < 1e-7 * max(1.0, np.abs(vo).max())
+            off += n
+        assert g.step_index() == 1 + 5
+        g.step(0)  # no-op
+        g.close()
+
+
+def test_invalid_systems_are_refused(gpu):
+    p = configs.wca_params(gamma=5.0)
+    s, a_type, r0, v = configs.brush_channel(10.0, 8.0, 0.1, 10, seed=54)
+    bad = abi.System.from_buffer_copy(s)
+    bad.boundary[0] = bad.boundary[1] = 2.0  # shorter than 2.5 list cut-offs
+    with pytest.raises(abi.MfaError) as e:
+        md.MdSystem(p, bad, a_type, r0, v)
+    assert e.value.code == -9  # MFA_ERR_UNSUPPORTED
+    bad = abi.System.from_buffer_copy(s)
+    bad.n_mon_tot = s.n_mon_tot - 1  # inconsistent with the chain counts
+    with pytest.raises(abi.MfaError):
+        md.MdSystem(p, bad, a_type, r0, v)
