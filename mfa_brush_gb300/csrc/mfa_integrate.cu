@@ -270,7 +270,7 @@ void launch_integrate(const DevState& s, const SimConst& C, cudaStream_t st, int
 // and flushes to the replica's global FP64 profile whenever the replica changes.
 // prof layout per replica: [hist][3 species][7] (count, vx, vy, vz, vx^2, vy^2, vz^2).
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_profiles(DevState s, SimConst C, double* __restrict__ prof, int H,
+__global__ void __launch_bounds__(256) k_profiles(DevState s, SimConst C, double* __restrict__ prof, int H,
                                                   int chunk) {
   extern __shared__ double sh[];
   const int n_sh = H * 3 * 7;
@@ -322,7 +322,9 @@ __global__ void __launch_bounds__(512) k_profiles(DevState s, SimConst C, double
 }
 
 void launch_profiles(const DevState& s, const SimConst& C, cudaStream_t st, double* prof, int H) {
-  const int chunk = 16384;
+  // small chunks: enough blocks to fill the GPU for one large replica as for many small ones (a
+  // block of sorted particles touches few bins, so its flush is short)
+  const int chunk = 1024;
   const int g = (s.N + chunk - 1) / chunk;
   const size_t shm = sizeof(double) * H * 3 * 7;
   static size_t shm_set = 48 * 1024;
@@ -330,7 +332,7 @@ void launch_profiles(const DevState& s, const SimConst& C, cudaStream_t st, doub
     cudaFuncSetAttribute(k_profiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     shm_set = shm;
   }
-  k_profiles<<<g, 512, shm, st>>>(s, C, prof, H, chunk);
+  k_profiles<<<g, 256, shm, st>>>(s, C, prof, H, chunk);
 }
 
 // energy record: out[k*nrep + r] = acc, acc = 0
