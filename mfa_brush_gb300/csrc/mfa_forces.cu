@@ -387,10 +387,17 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
     while (k < n) {
       int m = 0;
       // groups of G independent entries (index loads first, then the position gathers)
-      while (k + G <= n && m <= BATCH - G) {
-        int jg[G];
+      // (the next group's list indices are loaded one group ahead, hiding their DRAM latency)
+      int jg[G];
+      if (k + G <= n) {
 #pragma unroll
         for (int u = 0; u < G; ++u) jg[u] = __ldg(nb + (size_t)(k + u) * s.Np);
+      }
+      while (k + G <= n && m <= BATCH - G) {
+        int jn[G];
+        const bool more = k + 2 * G <= n;
+#pragma unroll
+        for (int u = 0; u < G; ++u) jn[u] = more ? __ldg(nb + (size_t)(k + G + u) * s.Np) : 0;
         bool hg[G];
 #pragma unroll
         for (int u = 0; u < G; ++u) hg[u] = screen(jg[u]);
@@ -398,6 +405,8 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
         for (int u = 0; u < G; ++u)
           if (hg[u]) jl[m++] = jg[u];
         k += G;
+#pragma unroll
+        for (int u = 0; u < G; ++u) jg[u] = jn[u];
       }
       while (k < n && m < BATCH) {
         const int j = __ldg(nb + (size_t)k * s.Np);
