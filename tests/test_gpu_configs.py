@@ -298,3 +298,32 @@ def test_invalid_systems_are_refused(gpu):
     bad.n_mon_tot = s.n_mon_tot - 1  # inconsistent with the chain counts
     with pytest.raises(abi.MfaError):
         md.MdSystem(p, bad, a_type, r0, v)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_restart_continues_the_noise_stream(gpu, precision):
+    """Ten steps, the state taken out, a new context started at the next step with that state, ten
+    more steps: the same trajectory as twenty uninterrupted steps (the DPD noise is keyed on the
+    step, so no generator state needs saving).  Agreement to round-off: the new context sorts its
+    particles afresh, which changes the order of the force sums."""
+    p = configs.wca_params(gamma=5.0)
+    s, a_type, r0, v = configs.brush_channel(14.0, 12.0, 0.2, 20, seed=61)
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+    g.step(20)
+    r20, v20, _, _ = g.state()
+    g.close()
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+    g.step(10)
+    r10, v10, a10, _ = g.state()
+    g.close()
+    s2 = abi.System.from_buffer_copy(s)
+    s2.s_time = s.s_time + 10
+    g = md.MdSystem(p, s2, a_type, r10, v10, a10, precision=precision)
+    g.step(10)
+    rr, vv, _, _ = g.state()
+    L = np.array(list(s.boundary))
+    d = rr - r20
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    tol = 1e-10 if precision == "fp64" else 1e-5
+    assert np.abs(d).max() < tol
+    assert np.abs(vv - v20).max() < tol * 100
