@@ -277,6 +277,10 @@ int mfa_profiles_accumulate(mfa_ctx* ctx);
  * Runs nsteps complete md_main steps (positions, lists, all forces, velocities, energies every
  * energy_every steps, profiles) on the device; graph-captured when opt.use_graphs.           */
 int mfa_step(mfa_ctx* ctx, int32_t nsteps);
+/* Neighbour-list capacity (entries per particle) and the largest count seen at the rebuilds so
+   far.  When the largest count passes 85 % of the capacity, the next mfa_step or
+   mfa_verlet_positions raises the capacity by half (up to its maximum) and rebuilds the lists. */
+int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count);
 /* Absolute step counter of replica 0 (s_time + steps done). */
 int mfa_get_step(mfa_ctx* ctx, int64_t* step);
 

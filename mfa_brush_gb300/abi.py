@@ -154,6 +154,7 @@ SIGNATURES = {
     "mfa_get_energies": (i32, [vp, P(Energies)]),
     "mfa_get_profiles": (i32, [vp, i32, dp, dp, dp, P(i64)]),
     "mfa_observe": (i32, [vp, P(Observables)]),
+    "mfa_list_stats": (i32, [vp, ip, ip]),
     "mfa_reset_profiles": (i32, [vp]),
     "mfa_cell_list": (i32, [vp, i32, i32, ip, ip, i32, ip]),
     "mfa_cell_neigh_list": (i32, [ip, i32, ip]),

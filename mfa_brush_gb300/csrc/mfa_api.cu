@@ -38,7 +38,8 @@ struct mfa_ctx {
   std::vector<double> v_ff_walls;  // LJ energy of the fixed wall beads among themselves (WALL 1)
   KSpace K;
   bool kspace = false;
-  unsigned* h_status = nullptr;  // pinned
+  unsigned* h_status = nullptr;  // pinned: [0] status bits, [1] largest list count seen
+  bool grow_pending = false;     // the list capacity is to be raised before the next step
   long long* h_rebuilds = nullptr;
   long long* d_rebuilds = nullptr;
   long long last_rebuilds = 0;
@@ -98,7 +99,11 @@ Acc acc_of(double* a, int nrep) { return Acc{a, nrep}; }
 
 int check_status(mfa_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->st));
-  unsigned s = *ctx->h_status;
+  unsigned s = ctx->h_status[0];
+  // a list count past 85 % of the capacity: raise the capacity before the next step, so that a
+  // density fluctuation later in the run does not overflow it
+  if (ctx->h_status[1] * 20u > (unsigned)ctx->S.nbr_cap * 17u && ctx->S.nbr_cap < NL_CAP_MAX)
+    ctx->grow_pending = true;
   if (s & ST_NAN) return fail(ctx, MFA_ERR_NAN, "non-finite position detected");
   if (s & ST_OUT_OF_BOX) return fail(ctx, MFA_ERR_OUT_OF_BOX, "a particle left the channel");
   if (s & ST_NLIST_OVERFLOW) return fail(ctx, MFA_ERR_NLIST_OVERFLOW, "neighbour list capacity exceeded");
@@ -106,7 +111,7 @@ int check_status(mfa_ctx* ctx) {
 }
 
 int post_status(mfa_ctx* ctx) {
-  CK(cudaMemcpyAsync(ctx->h_status, ctx->S.status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->h_status, ctx->S.status, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
   return MFA_OK;
 }
 
@@ -576,7 +581,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.cell_start, cell_off + 1);
   DA(S.scan_blk, (cell_off + 1023) / 1024 + 1);
   DA(S.rebuild_flag, 1);
-  DA(S.status, 1);
+  DA(S.status, 2);  // [0] status bits, [1] largest list count of the rebuilds so far
   DA(S.steps_done, 1);
   DA(ctx->d_rebuilds, 1);
   DA(ctx->dreps, n_rep);
@@ -586,9 +591,9 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(ctx->acc_call, NOBS * n_rep);
   DA(ctx->rec, NOBS * n_rep);
   DA(ctx->prof, (size_t)n_rep * C.hist_dim * 21);
-  CK(cudaMallocHost(&ctx->h_status, sizeof(unsigned)));
+  CK(cudaMallocHost(&ctx->h_status, 2 * sizeof(unsigned)));
   CK(cudaMallocHost(&ctx->h_rebuilds, sizeof(long long)));
-  *ctx->h_status = 0;
+  ctx->h_status[0] = ctx->h_status[1] = 0;
   S.reps = ctx->dreps;
   S.tabf = ctx->dtabf;
   S.tabd = ctx->dtabd;
@@ -611,7 +616,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaMemcpyAsync(S.tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(S.slot_of_tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(S.rebuild_flag, 0, sizeof(int), st));
-  CK(cudaMemsetAsync(S.status, 0, sizeof(unsigned), st));
+  CK(cudaMemsetAsync(S.status, 0, 2 * sizeof(unsigned), st));
   CK(cudaMemsetAsync(S.steps_done, 0, sizeof(long long), st));
   CK(cudaMemsetAsync(ctx->d_rebuilds, 0, sizeof(long long), st));
   CK(cudaMemsetAsync(ctx->acc_step, 0, sizeof(double) * NOBS * n_rep, st));
@@ -660,8 +665,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       if (newcap <= cap) return fail(ctx, MFA_ERR_CAPACITY, "more neighbours per particle than the list builder holds");
       S.nbr_cap = newcap;
       DA(S.nbr, (size_t)newcap * Nn);
-      CK(cudaMemsetAsync(S.status, 0, sizeof(unsigned), st));
-      *ctx->h_status = 0;
+      CK(cudaMemsetAsync(S.status, 0, 2 * sizeof(unsigned), st));
+      ctx->h_status[0] = ctx->h_status[1] = 0;
       rebuild(ctx, true);
       RET(post_status(ctx));
       rc = check_status(ctx);
@@ -723,8 +728,11 @@ static int read_call_slot(mfa_ctx* ctx, int slot, double* out, double add_self) 
   return MFA_OK;
 }
 
+static int grow_lists(mfa_ctx* ctx);
+
 int mfa_verlet_positions(mfa_ctx* ctx) {
   if (!ctx) return MFA_ERR_ARG;
+  if (ctx->grow_pending) RET(grow_lists(ctx));
   launch_integrate(ctx->S, ctx->C, ctx->st, 0, false, false, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 1;
   rebuild(ctx, false);
@@ -874,6 +882,28 @@ int mfa_profiles_accumulate(mfa_ctx* ctx) {
 // ---- fused step -----------------------------------------------------------------------------
 // Issues the kernels of `n` steps; eflag on steps where (absolute step) % energy_every == 0 and
 // on the last step.  Returns the number of launches issued.
+// Raises the neighbour-list capacity by half (at most NL_CAP_MAX), rebuilds the lists and drops
+// the captured step graphs, which hold the old list address and capacity.
+static int grow_lists(mfa_ctx* ctx) {
+  ctx->grow_pending = false;
+  DevState& S = ctx->S;
+  const int seen = (int)ctx->h_status[1];
+  const int newcap = std::min(NL_CAP_MAX, std::max(S.nbr_cap * 3 / 2, seen * 3 / 2 + 16));
+  if (newcap <= S.nbr_cap) return MFA_OK;
+  CK(cudaStreamSynchronize(ctx->st));
+  auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void*)S.nbr);
+  if (it != ctx->allocs.end()) { cudaFree(*it); ctx->allocs.erase(it); }
+  S.nbr = nullptr;
+  DA(S.nbr, (size_t)newcap * S.Np);
+  S.nbr_cap = newcap;
+  for (auto& g : ctx->graphs) cudaGraphExecDestroy(g.second.first);
+  ctx->graphs.clear();
+  CK(cudaMemsetAsync(S.status + 1, 0, sizeof(unsigned), ctx->st));
+  ctx->h_status[1] = 0;
+  rebuild(ctx, true);
+  return MFA_OK;
+}
+
 static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool capturing, int* err) {
   const DevState& S = ctx->S;
   const SimConst& C = ctx->C;
@@ -920,9 +950,19 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool cap
   return L;
 }
 
+int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count) {
+  if (!ctx) return MFA_ERR_ARG;
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (capacity) *capacity = ctx->S.nbr_cap;
+  if (max_count) *max_count = (int32_t)ctx->h_status[1];
+  return r;
+}
+
 int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
   if (!ctx) return MFA_ERR_ARG;
   if (nsteps <= 0) return MFA_OK;
+  if (ctx->grow_pending) RET(grow_lists(ctx));
   const long long s0 = ctx->sys[0].s_time + ctx->host_steps;
   bool prof = ctx->P.flags.profiles && (ctx->host_steps >= ctx->opt.profile_from_step);
   if (ctx->P.flags.profiles && !prof && ctx->host_steps + nsteps > ctx->opt.profile_from_step) {

@@ -377,6 +377,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
   }
   atomicMax(&blk_max, cnt);
   __syncthreads();
+  if (threadIdx.x == 0) atomicMax(s.status + 1, (unsigned)blk_max);  // largest count, for the host
   const int mx = min(blk_max, NL_STAGE);
   if (i < s.N) {
     for (int k = 0; k < mx; ++k)

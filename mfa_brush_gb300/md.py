@@ -239,6 +239,12 @@ class MdSystem:
         self._ck(self.lib.mfa_get_energies(self.ctx, e))
         return [x.as_dict() for x in e]
 
+    def list_stats(self):
+        """(neighbour-list capacity, largest list count seen at the rebuilds so far)."""
+        cap, mx = abi.i32(0), abi.i32(0)
+        self._ck(self.lib.mfa_list_stats(self.ctx, C.byref(cap), C.byref(mx)))
+        return cap.value, mx.value
+
     def observe(self):
         """observation.f90 quantities of every replica: Rg^2 (brush, melt), momentum, head forces."""
         o = (abi.Observables * self.nrep)()

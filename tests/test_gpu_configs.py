@@ -327,3 +327,21 @@ def test_restart_continues_the_noise_stream(gpu, precision):
     tol = 1e-10 if precision == "fp64" else 1e-5
     assert np.abs(d).max() < tol
     assert np.abs(vv - v20).max() < tol * 100
+
+
+def test_list_capacity_grows_before_it_overflows(gpu):
+    """A context made with a list capacity just above the largest count raises the capacity at its
+    first step (the count is past 85 % of it) and then runs exactly like one with ample room."""
+    p = configs.wca_params(gamma=5.0)
+    s, a_type, r0, v = configs.brush_channel(14.0, 12.0, 0.2, 20, seed=71)
+    ref = md.MdSystem(p, s, a_type, r0, v, precision="fp64")
+    cap0, mx0 = ref.list_stats()
+    assert 0 < mx0 < cap0
+    tight = md.MdSystem(p, s, a_type, r0, v, precision="fp64", nbr_capacity=mx0 + 1)
+    assert tight.list_stats() == (mx0 + 1, mx0)
+    tight.step(30)
+    ref.step(30)
+    cap1, mx1 = tight.list_stats()
+    assert cap1 > mx0 + 1 and mx1 <= cap1
+    for x, y in zip(tight.state(), ref.state()):
+        assert np.array_equal(x, y)
