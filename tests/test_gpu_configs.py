@@ -345,3 +345,34 @@ def test_list_capacity_grows_before_it_overflows(gpu):
     assert cap1 > mx0 + 1 and mx1 <= cap1
     for x, y in zip(tight.state(), ref.state()):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_force_switch_on_ramp(gpu, try_deck, oracle_mod, precision):
+    """FORCE_SWITCH_ON from s_time = 1 (init_force_switch_on.f90:12-28, fluid_fluid.f90:35-42):
+    pair distances are clamped at a radius that shrinks with time.  Pair forces at the first step
+    and three md_main steps against the oracle."""
+    import ctypes as C
+    inp, p, s, a_type, r0, v, a = try_deck
+    p1 = abi.Params.from_buffer_copy(p)
+    abi.check(md._lib().mfa_force_switch_on(C.byref(p1), 10000, 0))
+    assert p1.r_2_min_init > 0.5 and p1.r_2_min_time >= 40.0
+    s1 = abi.System.from_buffer_copy(s)
+    s1.s_time = 1
+    g = md.MdSystem(p1, s1, a_type, r0, v, a, precision=precision)
+    o = oracle_mod.Oracle(p1, s1, a_type, r0, v, a)
+    g.zero_force()
+    vff = g.fluid_fluid()[0][0]
+    o.zero_force()
+    o.fluid_fluid()
+    assert rel(vff, o.energies()["v_fluid_fluid"]) < (1e-10 if precision == "fp64" else 1e-5)
+    assert abs(vff - (-1131.60193205932)) > 1.0  # the clamp is active (unclamped: the try/log value)
+    assert_force_parity(g.state()[3], o.state()[3], precision)
+    if precision == "fp64":
+        for _ in range(3):
+            g.md_step()
+        o.step(3, 1, 0)
+        d = g.state()[0] - o.state()[0]
+        L = np.array(list(s.boundary))
+        d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+        assert np.abs(d).max() < 1e-9
