@@ -376,3 +376,38 @@ def test_force_switch_on_ramp(gpu, try_deck, oracle_mod, precision):
         L = np.array(list(s.boundary))
         d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
         assert np.abs(d).max() < 1e-9
+
+
+@pytest.mark.parametrize("compat", [1, 4, 5])  # MFA_COMPAT_EWALD_INV_PI, MFA_COMPAT_COUL_IN_LJ, both
+def test_reference_defect_switches(gpu, oracle_mod, compat):
+    """The reference's Ewald defects reproduced behind compat bits: 1/pi for 1/sqrt(pi)
+    (init_config.f90:232) and real-space Coulomb only inside the LJ cut-off (fluid_fluid.f90:
+    203-209).  Real-space forces and energy, FP64, against the oracle with the same bits; the
+    forces (and, for the shorter range, the energy) must differ from the corrected ones."""
+    def system(bits):
+        inp = configs.wca_inputs(gamma=1.0, thermostat=0)
+        inp.flags.system = 3
+        inp.charge[1], inp.charge[2] = -1.0, 1.0
+        inp.alpha_c, inp.n_kmax, inp.rc_coul = 0.81, 4, 3.0
+        inp.compat = bits
+        p, _ = md.derive(inp)
+        return p
+    s, a_type, r0, v = configs.brush_channel(10.0, 10.0, 0.08, 10, rho=0.5, seed=22)
+    out = {}
+    for bits in (0, compat):
+        p = system(bits)
+        g = md.MdSystem(p, s, a_type, r0, v, precision="fp64")
+        o = oracle_mod.Oracle(p, s, a_type, r0, v)
+        g.zero_force()
+        _, vc = g.fluid_fluid()
+        o.zero_force()
+        o.fluid_fluid()
+        assert abs(vc[0] - o.energies()["v_coul"]) < 1e-10 * abs(o.energies()["v_coul"])
+        f = g.state()[3]
+        assert_force_parity(f, o.state()[3], "fp64")
+        out[bits] = (vc[0], f)
+        g.close()
+    # 1/pi only scales the force's Gaussian term; the shorter Coulomb range changes both
+    assert np.abs(out[compat][1] - out[0][1]).max() > 1e-6 * np.abs(out[0][1]).max()
+    if compat & 4:
+        assert abs(out[compat][0] - out[0][0]) > 1e-6 * abs(out[0][0])
