@@ -249,25 +249,82 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   K.lz_half = L[2] / 2.;
   K.rep = 0;
   std::vector<int> qt;
+  std::vector<double> qv;
   for (int t = 0; t < s.n_mon_tot; ++t)
-    if (p.charge[a_type[t] - 1] != 0.) qt.push_back(t);
+    if (p.charge[a_type[t] - 1] != 0.) {
+      qt.push_back(t);
+      qv.push_back(p.charge[a_type[t] - 1]);
+    }
   K.nq = (int)qt.size();
+  std::vector<float> qvf(qv.begin(), qv.end());
+  // rows: maximal runs of k with one (ky, kz)
+  std::vector<int4> rows;
+  std::vector<int> krow(K.nk);
+  for (int k = 0; k < K.nk; ++k) {
+    if (k == 0 || kn[k].y != kn[k - 1].y || kn[k].z != kn[k - 1].z) rows.push_back(make_int4(k, k, kn[k].y, kn[k].z));
+    rows.back().y = k + 1;
+    krow[k] = (int)rows.size() - 1;
+  }
+  K.nrows = (int)rows.size();
+  K.rho_rows_max = 1;
+  for (int k0 = 0; k0 < K.nk; k0 += KS_KB)
+    K.rho_rows_max = std::max(K.rho_rows_max, krow[std::min(K.nk, k0 + KS_KB) - 1] - krow[k0] + 1);
+  // force chunks: whole rows, at most KS_FK k-vectors each (a row holds at most 2 nx + 1 <= KS_FK)
+  std::vector<int> chunk_row{0};
+  K.fchunk_k_max = K.fchunk_rows_max = 1;
+  for (int r = 0; r < K.nrows; ++r) {
+    const int beg = rows[chunk_row.back()].x;
+    if (r > chunk_row.back() && rows[r].y - beg > KS_FK) chunk_row.push_back(r);
+  }
+  chunk_row.push_back(K.nrows);
+  K.nkchunks = (int)chunk_row.size() - 1;
+  for (int c = 0; c < K.nkchunks; ++c) {
+    K.fchunk_k_max = std::max(K.fchunk_k_max, rows[chunk_row[c + 1] - 1].y - rows[chunk_row[c]].x);
+    K.fchunk_rows_max = std::max(K.fchunk_rows_max, chunk_row[c + 1] - chunk_row[c]);
+  }
+  if (K.fchunk_k_max > KS_FK) return fail(ctx, MFA_ERR_CAPACITY, "ewald_k: a row of k-vectors is longer than 512");
+  // rho particle chunks: about six blocks per SM, chunks a multiple of the 32-particle tile
+  const int kb = (K.nk + KS_KB - 1) / KS_KB;
+  int pch = std::max(1, std::min(256, (6 * 152 + kb - 1) / kb));
+  K.pchunk = std::max(32, ((K.nq + pch - 1) / pch + 31) / 32 * 32);
+  K.npchunks = std::max(1, (K.nq + K.pchunk - 1) / K.pchunk);
   DA(K.kn, K.nk);
   DA(K.kvec, 3 * K.nk);
   DA(K.kfac, K.nk);
   DA(K.rho, 2 * K.nk);
   DA(K.mz, 1);
-  K.kchunk = 512;
-  K.nkchunks = (K.nk + K.kchunk - 1) / K.kchunk;
+  DA(K.rows, K.nrows);
+  DA(K.krow, K.nk);
+  DA(K.chunk_row, K.nkchunks + 1);
+  DA(K.rho_part, (size_t)K.npchunks * 2 * K.nk);
   DA(K.fpart, (size_t)K.nkchunks * std::max(K.nq, 1) * 3);
+  DA(K.red_part, 2 * KS_RED_MAX);
+  DA(K.ticket, 2);
   DA(K.qtag, K.nq);
-  if (ctx->S.mixed) DA(K.tabf, (size_t)K.nq * K.ncol); else DA(K.tabd, (size_t)K.nq * K.ncol);
+  DA(K.qval, K.nq);
+  DA(K.qvalf, K.nq);
+  if (ctx->S.mixed) {
+    DA(K.tabf, (size_t)K.nq * K.ncol);
+    DA(K.kdf, K.nk);
+  } else {
+    DA(K.tabd, (size_t)K.nq * K.ncol);
+    DA(K.kdd, K.nk);
+  }
   cudaStream_t st = ctx->st;
   CK(cudaMemcpyAsync(K.kn, kn.data(), sizeof(int4) * K.nk, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(K.kvec, kv.data(), sizeof(double) * 3 * K.nk, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(K.kfac, kf.data(), sizeof(double) * K.nk, cudaMemcpyHostToDevice, st));
-  if (K.nq) CK(cudaMemcpyAsync(K.qtag, qt.data(), sizeof(int) * K.nq, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.rows, rows.data(), sizeof(int4) * K.nrows, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.krow, krow.data(), sizeof(int) * K.nk, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.chunk_row, chunk_row.data(), sizeof(int) * (K.nkchunks + 1), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(K.ticket, 0, 2 * sizeof(unsigned), st));
+  if (K.nq) {
+    CK(cudaMemcpyAsync(K.qtag, qt.data(), sizeof(int) * K.nq, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(K.qval, qv.data(), sizeof(double) * K.nq, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(K.qvalf, qvf.data(), sizeof(float) * K.nq, cudaMemcpyHostToDevice, st));
+  }
   CK(cudaStreamSynchronize(st));
+  CK((cudaError_t)kspace_prepare(K, ctx->S.mixed));
   ctx->kspace = true;
   return MFA_OK;
 }

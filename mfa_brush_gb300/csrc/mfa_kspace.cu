@@ -3,17 +3,21 @@
 // ewald_k.f90:128-202 evaluates rho(k) = sum_i q_i exp(i k.r_i) over N_k half-space vectors and
 // then F_i = -(8 pi q_i / V) sum_k k G(k) (cos(k.r_i) Im rho - sin(k.r_i) Re rho),
 // U = (4 pi / V) sum_k G(k) |rho(k)|^2, G(k) = exp(-k^2/(4 alpha_c)) / k^2, storing an N x N_k
-// phase array.  Here nothing of size N x N_k is stored:
-//   k_ks_tables: per charged particle, X(nx) = exp(i nx dkx x), Y(ny), Z(nz) for n >= 0, each
-//                from an FP64 phase reduced to [-1/2, 1/2) turns (sincospi), so every factor is
-//                accurate to the working precision;
-//   k_ks_rho:    thread per k-vector, particles staged through shared memory, exp(i k.r) =
-//                X Y Z (conjugated for negative n), FP32 Kahan-compensated partial sums (MIXED)
-//                or FP64 sums, partials of particle chunks combined with FP64 atomics;
-//   k_ks_energy: U in FP64;
-//   k_ks_force:  thread per charged particle and k-chunk, the same factorised phase, forces
-//                added to the FP64 force array.
+// phase array.  Here nothing of size N x N_k is stored.  The k-vectors come kz outer, ky, kx
+// inner, so a (ky, kz) "row" of k shares the factor Y(ky) Z(kz) and only X(kx) varies along it:
+//   k_ks_tables:  per charged particle, X(nx) = exp(i nx dkx x), Y(ny), Z(nz) for n >= 0, each
+//                 from an FP64 phase reduced to [-1/2, 1/2) turns (sincospi); stored column-major
+//                 ([column][particle]) so that a warp reads 32 particles of one column at once;
+//   k_ks_rho:     thread per k-vector, tiles of 32 particles in shared memory holding X(+-nx) and
+//                 A = q Y Z for the rows the block spans: one complex product per (k, particle),
+//                 FP32 Kahan-compensated sums (MIXED) or FP64 sums, one partial per particle chunk;
+//   k_ks_rho_sum: the partials of each k summed in a fixed order, G Re rho and G Im rho for the
+//                 force, and U reduced deterministically (per-block partials, the last block sums);
+//   k_ks_force:   thread per particle, a chunk of whole rows per block: per row Y Z once, per k
+//                 one complex product; sum_k kx s_k per k, and ky, kz times the row sum of s_k;
+//   k_ks_force_sum: the chunk partials in a fixed order, times -8 pi q / V, into the force array.
 // dipolar_correction.f90:20-33 (Yeh-Berkowitz slab term) is k_ks_dipole + k_ks_dipole_force, FP64.
+// Every sum has a fixed order, so a charged run is reproducible bit for bit.
 #include <type_traits>
 
 #include "mfa_state.cuh"
@@ -32,12 +36,30 @@ __device__ __forceinline__ void cmul(double2 a, double2 b, double2& c) {
   c = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// s += y: Kahan-compensated in FP32 (c carries the negated lost low part), plain in FP64
+template <bool MIXED>
+__device__ __forceinline__ void ksum(kreal<MIXED>& s, kreal<MIXED>& c, kreal<MIXED> y) {
+  if constexpr (MIXED) {
+    const float z = y - c;
+    const float t = s + z;
+    c = (t - s) - z;
+    s = t;
+  } else {
+    s += y;
+  }
+}
+
+template <bool MIXED>
+__device__ __forceinline__ const kcplx<MIXED>* ktab(const KSpace& K) {
+  if constexpr (MIXED) return K.tabf; else return K.tabd;
+}
+
 template <bool MIXED>
 __global__ void k_ks_tables(DevState s, KSpace K) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= K.nq * K.ncol) return;
-  int p = idx / K.ncol, col = idx % K.ncol;
-  int i = s.slot_of_tag[K.qtag[p]];
+  const int col = idx / K.nq, p = idx - col * K.nq;
+  const int i = s.slot_of_tag[K.qtag[p]];
   double u;
   if (col <= K.nxm) u = (double)col * K.cx * s.rx[i];
   else if (col <= K.nxm + 1 + K.nym) u = (double)(col - K.nxm - 1) * K.cy * s.ry[i];
@@ -54,130 +76,232 @@ __global__ void k_ks_tables(DevState s, KSpace K) {
   }
 }
 
-template <bool MIXED>
-__device__ __forceinline__ kcplx<MIXED> phase_of(const kcplx<MIXED>* T, int nxm, int nym, int4 n) {
-  using C = kcplx<MIXED>;
-  C X = T[abs(n.x)];
-  if (n.x < 0) X.y = -X.y;
-  C Y = T[nxm + 1 + abs(n.y)];
-  if (n.y < 0) Y.y = -Y.y;
-  C Z = T[nxm + nym + 2 + n.z];
-  C XY, E;
-  cmul(X, Y, XY);
-  cmul(XY, Z, E);
-  return E;
-}
-
-constexpr int KS_TILE = 32;  // particles per shared-memory tile
+constexpr int KS_TILE = 32;  // particles per shared-memory tile of k_ks_rho (one per lane)
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_ks_rho(DevState s, SimConst C, KSpace K, int chunk) {
+__global__ void __launch_bounds__(KS_KB) k_ks_rho(KSpace K) {
   using real = kreal<MIXED>;
   using Cx = kcplx<MIXED>;
-  extern __shared__ unsigned char shraw[];
-  Cx* T = reinterpret_cast<Cx*>(shraw);           // [KS_TILE][ncol]
-  real* q = reinterpret_cast<real*>(T + KS_TILE * K.ncol);
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool act = k < K.nk;
-  const int4 n = act ? K.kn[k] : make_int4(0, 0, 0, 0);
-  const int p_beg = blockIdx.y * chunk, p_end = min(K.nq, p_beg + chunk);
-  real sr = 0, si = 0, cr = 0, ci = 0;  // Kahan sums
-  const Cx* tab;
-  if constexpr (MIXED) tab = K.tabf; else tab = K.tabd;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  const int nxc = 2 * K.nxm + 1;
+  const int k0 = blockIdx.x * KS_KB, k1 = min(K.nk, k0 + KS_KB);
+  const int r0 = K.krow[k0], nr = K.krow[k1 - 1] - r0 + 1;
+  Cx* Xs = reinterpret_cast<Cx*>(shraw);  // [KS_TILE][nxc]: X(nx) for nx = -nxm..nxm
+  Cx* As = Xs + KS_TILE * nxc;            // [KS_TILE][nr]:  q Y Z for the block's rows
+  const Cx* tab = ktab<MIXED>(K);
+  const int k = k0 + threadIdx.x;
+  const bool act = k < k1;
+  int xi = 0, ri = 0;
+  if (act) {
+    xi = K.kn[k].x + K.nxm;
+    ri = K.krow[k] - r0;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p_beg = blockIdx.y * K.pchunk, p_end = min(K.nq, p_beg + K.pchunk);
+  real sr = 0, si = 0, cr = 0, ci = 0;
   for (int t0 = p_beg; t0 < p_end; t0 += KS_TILE) {
     const int nt = min(KS_TILE, p_end - t0);
     __syncthreads();
-    for (int e = threadIdx.x; e < nt * K.ncol; e += blockDim.x) T[e] = tab[(size_t)t0 * K.ncol + e];
-    for (int e = threadIdx.x; e < nt; e += blockDim.x) {
-      int i = s.slot_of_tag[K.qtag[t0 + e]];
-      q[e] = (real)C.charge[info_type(s.info[i])];
+    if (lane < nt) {
+      const int pq = t0 + lane;
+      for (int c = warp; c < nxc; c += KS_KB / 32) {
+        Cx v = tab[(size_t)abs(c - K.nxm) * K.nq + pq];
+        if (c < K.nxm) v.y = -v.y;
+        Xs[lane * nxc + c] = v;
+      }
+      real q;
+      if constexpr (MIXED) q = K.qvalf[pq]; else q = K.qval[pq];
+      for (int rr = warp; rr < nr; rr += KS_KB / 32) {
+        const int4 R = K.rows[r0 + rr];
+        Cx Y = tab[(size_t)(K.nxm + 1 + abs(R.z)) * K.nq + pq];
+        if (R.z < 0) Y.y = -Y.y;
+        const Cx Z = tab[(size_t)(K.nxm + K.nym + 2 + R.w) * K.nq + pq];
+        Cx A;
+        cmul(Y, Z, A);
+        A.x *= q;
+        A.y *= q;
+        As[lane * nr + rr] = A;
+      }
     }
     __syncthreads();
     if (act) {
+#pragma unroll 4
       for (int p = 0; p < nt; ++p) {
-        Cx E = phase_of<MIXED>(T + p * K.ncol, K.nxm, K.nym, n);
-        real yr = q[p] * E.x - cr;
-        real tr = sr + yr;
-        cr = (tr - sr) - yr;
-        sr = tr;
-        real yi = q[p] * E.y - ci;
-        real ti = si + yi;
-        ci = (ti - si) - yi;
-        si = ti;
+        Cx E;
+        cmul(Xs[p * nxc + xi], As[p * nr + ri], E);
+        ksum<MIXED>(sr, cr, E.x);
+        ksum<MIXED>(si, ci, E.y);
       }
     }
   }
   if (act) {
-    atomicAdd(&K.rho[2 * k], (double)sr);
-    atomicAdd(&K.rho[2 * k + 1], (double)si);
+    double* o = K.rho_part + (size_t)blockIdx.y * 2 * K.nk;
+    o[2 * k] = (double)sr - (double)cr;
+    o[2 * k + 1] = (double)si - (double)ci;
   }
 }
 
-__global__ void __launch_bounds__(1024) k_ks_energy(KSpace K, double pi4, Acc acc, bool eflag) {
+// Block sum of v (all threads), then the last block of the grid to finish adds the per-block
+// partials in block order; returns true in thread 0 of that block, with the total in `total`.
+__device__ __forceinline__ bool grid_sum_last(double v, double* part, unsigned* ticket, double& total) {
   __shared__ double red[32];
-  double u = 0.;
-  for (int k = threadIdx.x; k < K.nk; k += blockDim.x) {
-    double re = K.rho[2 * k], im = K.rho[2 * k + 1];
-    u += K.kfac[k] * (re * re + im * im);
-  }
-  u = warp_sum(u);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = u;
+  __shared__ bool last;
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
-    v = warp_sum(v);
-    if (threadIdx.x == 0 && eflag) acc.col(O_VCOULK)[K.rep] += v * pi4 * K.inv_V;
+  if (threadIdx.x == 0) {
+    double b = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
+    part[blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
   }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return false;
+  __threadfence();
+  double t = 0.;
+  for (unsigned b = 0; b < gridDim.x; ++b) t += ((volatile double*)part)[b];
+  total = t;
+  *ticket = 0u;  // ready for the next launch
+  return true;
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(128) k_ks_force(DevState s, SimConst C, KSpace K, int kchunk, double pi8) {
-  using real = kreal<MIXED>;
-  using Cx = kcplx<MIXED>;
-  extern __shared__ unsigned char shraw[];
-  int4* kn = reinterpret_cast<int4*>(shraw);                  // [kchunk]
-  real* kd = reinterpret_cast<real*>(kn + kchunk);             // [kchunk][6] kx ky kz G Re Im
-  const int k0 = blockIdx.y * kchunk, k1 = min(K.nk, k0 + kchunk);
-  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-    int kk = k - k0;
-    kn[kk] = K.kn[k];
-    kd[kk * 6 + 0] = (real)K.kvec[3 * k];
-    kd[kk * 6 + 1] = (real)K.kvec[3 * k + 1];
-    kd[kk * 6 + 2] = (real)K.kvec[3 * k + 2];
-    kd[kk * 6 + 3] = (real)K.kfac[k];
-    kd[kk * 6 + 4] = (real)K.rho[2 * k];
-    kd[kk * 6 + 5] = (real)K.rho[2 * k + 1];
+__global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, Acc acc, bool eflag) {
+  double u = 0.;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K.nk; k += gridDim.x * blockDim.x) {
+    double re = 0., im = 0.;
+    for (int c = 0; c < K.npchunks; ++c) {
+      const double2 v = reinterpret_cast<const double2*>(K.rho_part + (size_t)c * 2 * K.nk)[k];
+      re += v.x;
+      im += v.y;
+    }
+    reinterpret_cast<double2*>(K.rho)[k] = make_double2(re, im);
+    const double G = K.kfac[k];
+    u += G * (re * re + im * im);
+    if constexpr (MIXED)
+      K.kdf[k] = make_float4((float)K.kvec[3 * k], (float)(G * re), (float)(G * im), __int_as_float(K.kn[k].x + K.nxm));
+    else
+      K.kdd[k] = make_double2(G * re, G * im);
   }
-  __syncthreads();
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= K.nq) return;
-  const Cx* T;
-  if constexpr (MIXED) T = K.tabf + (size_t)p * K.ncol; else T = K.tabd + (size_t)p * K.ncol;
-  real fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;
-  for (int kk = 0; kk < k1 - k0; ++kk) {
-    Cx E = phase_of<MIXED>(T, K.nxm, K.nym, kn[kk]);
-    const real sgl = kd[kk * 6 + 3] * (E.x * kd[kk * 6 + 5] - E.y * kd[kk * 6 + 4]);
-    real y, t;
-    y = kd[kk * 6 + 0] * sgl - cx; t = fx + y; cx = (t - fx) - y; fx = t;
-    y = kd[kk * 6 + 1] * sgl - cy; t = fy + y; cy = (t - fy) - y; fy = t;
-    y = kd[kk * 6 + 2] * sgl - cz; t = fz + y; cz = (t - fz) - y; fz = t;
-  }
-  double* o = K.fpart + ((size_t)blockIdx.y * K.nq + p) * 3;
-  o[0] = (double)fx;
-  o[1] = (double)fy;
-  o[2] = (double)fz;
+  double tot;
+  if (grid_sum_last(u, K.red_part, K.ticket, tot) && eflag) acc.col(O_VCOULK)[K.rep] += tot * pi4 * K.inv_V;
 }
 
-// F_i = -(8 pi q_i / V) * sum over k-chunks in a fixed order (deterministic), added to the FP64
-// force array or, in the fused mixed-precision step, to the FP32 one.
-__global__ void k_ks_force_sum(DevState s, SimConst C, KSpace K, double pi8, bool to_f4) {
+template <bool MIXED>
+struct KD;
+template <>
+struct KD<true> {
+  float kx, a, b;  // kx, G Re rho, G Im rho
+  int xi;          // nx + nxm
+};
+template <>
+struct KD<false> {
+  double kx, a, b;
+  int xi, pad;
+};
+
+template <bool MIXED>
+__global__ void __launch_bounds__(KS_FB) k_ks_force(KSpace K) {
+  using real = kreal<MIXED>;
+  using Cx = kcplx<MIXED>;
+  using real2 = kcplx<MIXED>;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  const int nxc = 2 * K.nxm + 1;
+  Cx* Xs = reinterpret_cast<Cx*>(shraw);                              // [nxc][KS_FB]
+  KD<MIXED>* kd = reinterpret_cast<KD<MIXED>*>(Xs + nxc * KS_FB);     // [fchunk_k_max]
+  int4* rs = reinterpret_cast<int4*>(kd + K.fchunk_k_max);            // [fchunk_rows_max]
+  real2* ryz = reinterpret_cast<real2*>(rs + K.fchunk_rows_max);      // [fchunk_rows_max] ky, kz
+  const int rb = K.chunk_row[blockIdx.y], re = K.chunk_row[blockIdx.y + 1];
+  const int kb = K.rows[rb].x, ke = K.rows[re - 1].y;
+  for (int k = kb + threadIdx.x; k < ke; k += KS_FB) {
+    KD<MIXED> d;
+    if constexpr (MIXED) {
+      const float4 v = K.kdf[k];
+      d.kx = v.x;
+      d.a = v.y;
+      d.b = v.z;
+      d.xi = __float_as_int(v.w);
+    } else {
+      const double2 v = K.kdd[k];
+      d.kx = K.kvec[3 * k];
+      d.a = v.x;
+      d.b = v.y;
+      d.xi = K.kn[k].x + K.nxm;
+      d.pad = 0;
+    }
+    kd[k - kb] = d;
+  }
+  for (int r = rb + threadIdx.x; r < re; r += KS_FB) {
+    const int4 R = K.rows[r];
+    const int yc = K.nxm + 1 + abs(R.z);
+    rs[r - rb] = make_int4(R.x - kb, R.y - kb, R.z < 0 ? -yc : yc, K.nxm + K.nym + 2 + R.w);
+    real2 w;
+    w.x = (real)K.kvec[3 * R.x + 1];
+    w.y = (real)K.kvec[3 * R.x + 2];
+    ryz[r - rb] = w;
+  }
+  const Cx* tab = ktab<MIXED>(K);
+  const int p = blockIdx.x * KS_FB + threadIdx.x;
+  const int pc = min(p, K.nq - 1);
+  for (int c = 0; c < nxc; ++c) {
+    Cx v = tab[(size_t)abs(c - K.nxm) * K.nq + pc];
+    if (c < K.nxm) v.y = -v.y;
+    Xs[c * KS_FB + threadIdx.x] = v;
+  }
+  __syncthreads();
+  if (p >= K.nq) return;
+  const Cx* T = tab + pc;
+  const Cx* X = Xs + threadIdx.x;
+  real fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;
+  const int nr = re - rb;
+  int4 R = rs[0];
+  Cx Y = T[(size_t)abs(R.z) * K.nq], Z = T[(size_t)R.w * K.nq];
+  for (int r = 0; r < nr; ++r) {
+    // the next row's factors are loaded while this row is summed
+    int4 Rn = R;
+    Cx Yn = Y, Zn = Z;
+    if (r + 1 < nr) {
+      Rn = rs[r + 1];
+      Yn = T[(size_t)abs(Rn.z) * K.nq];
+      Zn = T[(size_t)Rn.w * K.nq];
+    }
+    if (R.z < 0) Y.y = -Y.y;
+    Cx YZ;
+    cmul(Y, Z, YZ);
+    real srow = 0;
+#pragma unroll 4
+    for (int k = R.x; k < R.y; ++k) {
+      const KD<MIXED> d = kd[k];
+      Cx E;
+      cmul(X[d.xi * KS_FB], YZ, E);
+      const real sg = E.x * d.b - E.y * d.a;
+      ksum<MIXED>(fx, cx, d.kx * sg);
+      srow += sg;
+    }
+    const real2 w = ryz[r];
+    ksum<MIXED>(fy, cy, w.x * srow);
+    ksum<MIXED>(fz, cz, w.y * srow);
+    R = Rn;
+    Y = Yn;
+    Z = Zn;
+  }
+  double* o = K.fpart + ((size_t)blockIdx.y * K.nq + p) * 3;
+  o[0] = (double)fx - (double)cx;
+  o[1] = (double)fy - (double)cy;
+  o[2] = (double)fz - (double)cz;
+}
+
+// F_i = -(8 pi q_i / V) * sum over k-chunks in a fixed order, added to the FP64 force array or,
+// in the fused mixed-precision step, to the FP32 one.
+__global__ void k_ks_force_sum(DevState s, KSpace K, double pi8, bool to_f4) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= K.nq) return;
   double f[3] = {0., 0., 0.};
   for (int c = 0; c < K.nkchunks; ++c)
     for (int d = 0; d < 3; ++d) f[d] += K.fpart[((size_t)c * K.nq + p) * 3 + d];
   const int i = s.slot_of_tag[K.qtag[p]];
-  const double qf = -pi8 * C.charge[info_type(s.info[i])] * K.inv_V;
+  const double qf = -pi8 * K.qval[p] * K.inv_V;
   if (to_f4) {
     float4 g = s.f4[i];
     g.x += (float)(qf * f[0]);
@@ -191,67 +315,82 @@ __global__ void k_ks_force_sum(DevState s, SimConst C, KSpace K, double pi8, boo
   }
 }
 
+namespace {
+size_t rho_smem(const KSpace& K, bool mixed) {
+  return (size_t)KS_TILE * (2 * K.nxm + 1 + K.rho_rows_max) * (mixed ? sizeof(float2) : sizeof(double2));
+}
+size_t force_smem(const KSpace& K, bool mixed) {
+  const size_t cx = mixed ? sizeof(float2) : sizeof(double2);
+  return (size_t)(2 * K.nxm + 1) * KS_FB * cx + (size_t)K.fchunk_k_max * (mixed ? sizeof(KD<true>) : sizeof(KD<false>)) +
+         (size_t)K.fchunk_rows_max * (sizeof(int4) + cx);
+}
+}  // namespace
+
+int kspace_prepare(const KSpace& K, bool mixed) {
+  const size_t a = rho_smem(K, mixed), b = force_smem(K, mixed);
+  if (a > 227 * 1024 || b > 227 * 1024) return (int)cudaErrorInvalidConfiguration;
+  cudaError_t e;
+  if (mixed) {
+    e = cudaFuncSetAttribute(k_ks_rho<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
+  } else {
+    e = cudaFuncSetAttribute(k_ks_rho<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
+  }
+  return (int)e;
+}
+
 void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
                    bool fused) {
   if (K.nk == 0 || K.nq == 0) return;
   const double pi = (double)3.1415926536f;  // mfa_common.f90:315 (single-precision literal)
-  int nt = K.nq * K.ncol;
+  const int nt = K.nq * K.ncol;
   if (s.mixed) k_ks_tables<true><<<(nt + 255) / 256, 256, 0, st>>>(s, K);
   else k_ks_tables<false><<<(nt + 255) / 256, 256, 0, st>>>(s, K);
-  cudaMemsetAsync(K.rho, 0, sizeof(double) * 2 * K.nk, st);
-  const int kb = (K.nk + 255) / 256;
-  int pchunks = max(1, min(64, (2 * 152 + kb - 1) / kb));
-  int chunk = (K.nq + pchunks - 1) / pchunks;
-  chunk = ((chunk + KS_TILE - 1) / KS_TILE) * KS_TILE;
-  pchunks = (K.nq + chunk - 1) / chunk;
-  size_t esz = s.mixed ? sizeof(float2) : sizeof(double2), rsz = s.mixed ? sizeof(float) : sizeof(double);
-  size_t shm = KS_TILE * K.ncol * esz + KS_TILE * rsz;
-  dim3 g1(kb, pchunks);
-  if (s.mixed) k_ks_rho<true><<<g1, 256, shm, st>>>(s, C, K, chunk);
-  else k_ks_rho<false><<<g1, 256, shm, st>>>(s, C, K, chunk);
-  k_ks_energy<<<1, 1024, 0, st>>>(K, 4. * pi, acc, eflag);
-  dim3 g2((K.nq + 127) / 128, K.nkchunks);
-  size_t shm2 = K.kchunk * sizeof(int4) + K.kchunk * 6 * rsz;
-  if (s.mixed) k_ks_force<true><<<g2, 128, shm2, st>>>(s, C, K, K.kchunk, 8. * pi);
-  else k_ks_force<false><<<g2, 128, shm2, st>>>(s, C, K, K.kchunk, 8. * pi);
-  k_ks_force_sum<<<(K.nq + 127) / 128, 128, 0, st>>>(s, C, K, 8. * pi, fused && s.mixed);
+  const dim3 g1((K.nk + KS_KB - 1) / KS_KB, K.npchunks);
+  const size_t shm1 = rho_smem(K, s.mixed);
+  if (s.mixed) k_ks_rho<true><<<g1, KS_KB, shm1, st>>>(K);
+  else k_ks_rho<false><<<g1, KS_KB, shm1, st>>>(K);
+  const int gs = std::min(KS_RED_MAX, (K.nk + 255) / 256);
+  if (s.mixed) k_ks_rho_sum<true><<<gs, 256, 0, st>>>(K, 4. * pi, acc, eflag);
+  else k_ks_rho_sum<false><<<gs, 256, 0, st>>>(K, 4. * pi, acc, eflag);
+  const dim3 g2((K.nq + KS_FB - 1) / KS_FB, K.nkchunks);
+  const size_t shm2 = force_smem(K, s.mixed);
+  if (s.mixed) k_ks_force<true><<<g2, KS_FB, shm2, st>>>(K);
+  else k_ks_force<false><<<g2, KS_FB, shm2, st>>>(K);
+  k_ks_force_sum<<<(K.nq + 127) / 128, 128, 0, st>>>(s, K, 8. * pi, fused && s.mixed);
 }
 
-__global__ void __launch_bounds__(1024) k_ks_dipole(DevState s, SimConst C, KSpace K, double pi, Acc acc, bool eflag) {
-  __shared__ double red[32];
+__global__ void __launch_bounds__(256) k_ks_dipole(DevState s, KSpace K, double pi, Acc acc, bool eflag) {
   double m = 0.;
-  for (int p = threadIdx.x; p < K.nq; p += blockDim.x) {
-    int i = s.slot_of_tag[K.qtag[p]];
-    m += C.charge[info_type(s.info[i])] * (s.rz[i] - K.lz_half);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K.nq; p += gridDim.x * blockDim.x) {
+    const int i = s.slot_of_tag[K.qtag[p]];
+    m += K.qval[p] * (s.rz[i] - K.lz_half);
   }
-  m = warp_sum(m);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
-    v = warp_sum(v);
-    if (threadIdx.x == 0) {
-      K.mz[0] = v;
-      if (eflag) acc.col(O_VDIP)[K.rep] += 2. * pi * v * v * K.inv_V;
-    }
+  double tot;
+  if (grid_sum_last(m, K.red_part + KS_RED_MAX, K.ticket + 1, tot)) {
+    K.mz[0] = tot;
+    if (eflag) acc.col(O_VDIP)[K.rep] += 2. * pi * tot * tot * K.inv_V;
   }
 }
 
-__global__ void k_ks_dipole_force(DevState s, SimConst C, KSpace K, double pi, bool to_f4) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_ks_dipole_force(DevState s, KSpace K, double pi, bool to_f4) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= K.nq) return;
-  int i = s.slot_of_tag[K.qtag[p]];
-  const double f = -4. * pi * C.charge[info_type(s.info[i])] * K.mz[0] * K.inv_V;
+  const int i = s.slot_of_tag[K.qtag[p]];
+  const double f = -4. * pi * K.qval[p] * K.mz[0] * K.inv_V;
   if (to_f4) s.f4[i].z += (float)f;
   else s.fz[i] += f;
 }
 
 void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
                     bool fused) {
+  (void)C;
   if (K.nq == 0) return;
   const double pi = (double)3.1415926536f;
-  k_ks_dipole<<<1, 1024, 0, st>>>(s, C, K, pi, acc, eflag);
-  k_ks_dipole_force<<<(K.nq + 255) / 256, 256, 0, st>>>(s, C, K, pi, fused && s.mixed);
+  const int g = std::min(KS_RED_MAX, (K.nq + 255) / 256);
+  k_ks_dipole<<<g, 256, 0, st>>>(s, K, pi, acc, eflag);
+  k_ks_dipole_force<<<(K.nq + 255) / 256, 256, 0, st>>>(s, K, pi, fused && s.mixed);
 }
 
 }  // namespace mfa

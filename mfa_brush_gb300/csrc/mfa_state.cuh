@@ -90,24 +90,48 @@ void launch_pair_list(const DevState& s, const SimConst& C, cudaStream_t st, int
                       long long cap, unsigned long long* count);
 // ---- k-space Ewald (ewald_k.f90, dipolar_correction.f90) ------------------------------------
 // exp(i k.r) = X(nx) Y(ny) Z(nz) per charged particle: the tables hold X for nx = 0..nxm,
-// Y for ny = 0..nym and Z for nz = 0..nzm (negative n by conjugation), so a (k, particle) term
-// costs two complex products instead of a sin/cos of a large argument.
+// Y for ny = 0..nym and Z for nz = 0..nzm (negative n by conjugation).
+// The k-vectors come in the reference's order: kz outer, ky, kx inner, so every (ky, kz) pair
+// owns one contiguous run of k ("row") whose phases share the factor Y Z: a (k, particle) term
+// then costs one complex product instead of a sin/cos of a large argument.
 struct KSpace {
   int nk, nq, nxm, nym, nzm, ncol;
   int4* kn;             // [nk] (nx, ny, nz, 0) in the reference's enumeration order
   double* kvec;         // [3*nk]
   double* kfac;         // [nk] exp(-k^2/(4 alpha_c)) / k^2
   double* rho;          // [2*nk] Re, Im of sum_q q exp(i k.r)
-  float2* tabf;         // [nq][ncol] (mixed)
-  double2* tabd;        // [nq][ncol] (fp64)
+  float2* tabf;         // [ncol][nq] (mixed): X(0..nxm), Y(0..nym), Z(0..nzm) per particle
+  double2* tabd;        // [ncol][nq] (fp64)
   int* qtag;            // [nq] tags of the charged particles
+  double* qval;         // [nq] their charges
+  float* qvalf;         // [nq] the same in FP32
   double cx, cy, cz;    // dk/(2 pi) per axis
   double inv_V, lz_half;
   double* mz;           // [1] dipole moment M_z
-  double* fpart;        // [kchunks][nq][3] per-k-chunk force partials, summed in a fixed order
-  int kchunk, nkchunks;
+  // rows
+  int nrows;
+  int4* rows;           // [nrows] (first k, end k, ny, nz)
+  int* krow;            // [nk] row of each k
+  // rho: blocks of KS_KB k-vectors x particle chunks; partials summed in a fixed order
+  int pchunk, npchunks, rho_rows_max;
+  double* rho_part;     // [npchunks][2*nk]
+  float4* kdf;          // [nk] (kx, G Re rho, G Im rho, nx + nxm as int bits)   (mixed)
+  double2* kdd;         // [nk] (G Re rho, G Im rho)                              (fp64)
+  // force: chunks of whole rows
+  int nkchunks, fchunk_k_max, fchunk_rows_max;
+  int* chunk_row;       // [nkchunks+1] first row of each chunk
+  double* fpart;        // [nkchunks][nq][3] per-chunk force partials, summed in a fixed order
+  // deterministic grid reductions: per-block partials, the last block to finish sums them
+  double* red_part;     // [2*KS_RED_MAX]: rho_sum energy, dipole moment
+  unsigned* ticket;     // [2] zero between launches
   int rep;
 };
+constexpr int KS_KB = 256;       // k-vectors per rho block
+constexpr int KS_FB = 128;       // particles per force block
+constexpr int KS_FK = 512;       // k-vectors per force chunk, at most (whole rows)
+constexpr int KS_RED_MAX = 256;  // blocks of a grid reduction, at most
+// host-side preparation of the kernels (shared-memory opt-in); returns a CUDA error
+int kspace_prepare(const KSpace& K, bool mixed);
 // fused: the mixed-precision fused step adds into the FP32 force array, otherwise into FP64
 void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
                    bool fused = false);
