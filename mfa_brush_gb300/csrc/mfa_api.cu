@@ -266,26 +266,41 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
     krow[k] = (int)rows.size() - 1;
   }
   K.nrows = (int)rows.size();
-  K.rho_rows_max = 1;
-  for (int k0 = 0; k0 < K.nk; k0 += KS_KB)
-    K.rho_rows_max = std::max(K.rho_rows_max, krow[std::min(K.nk, k0 + KS_KB) - 1] - krow[k0] + 1);
-  // force chunks: whole rows, at most KS_FK k-vectors each (a row holds at most 2 nx + 1 <= KS_FK)
-  std::vector<int> chunk_row{0};
-  K.fchunk_k_max = K.fchunk_rows_max = 1;
-  for (int r = 0; r < K.nrows; ++r) {
-    const int beg = rows[chunk_row.back()].x;
-    if (r > chunk_row.back() && rows[r].y - beg > KS_FK) chunk_row.push_back(r);
-  }
+  // slots of a row: nx = -nxm .. -nxm + 4 qx - 1 (the dense slot table of the force kernel)
+  K.qx = (2 * nx + 1 + 3) / 4;
+  // force chunks: KS_FR whole rows
+  std::vector<int> chunk_row;
+  for (int r = 0; r < K.nrows; r += KS_FR) chunk_row.push_back(r);
   chunk_row.push_back(K.nrows);
   K.nkchunks = (int)chunk_row.size() - 1;
+  K.fchunk_k_max = K.fchunk_rows_max = 1;
   for (int c = 0; c < K.nkchunks; ++c) {
     K.fchunk_k_max = std::max(K.fchunk_k_max, rows[chunk_row[c + 1] - 1].y - rows[chunk_row[c]].x);
     K.fchunk_rows_max = std::max(K.fchunk_rows_max, chunk_row[c + 1] - chunk_row[c]);
   }
-  if (K.fchunk_k_max > KS_FK) return fail(ctx, MFA_ERR_CAPACITY, "ewald_k: a row of k-vectors is longer than 512");
-  // rho particle chunks: about six blocks per SM, chunks a multiple of the 32-particle tile
-  const int kb = (K.nk + KS_KB - 1) / KS_KB;
-  int pch = std::max(1, std::min(256, (6 * 152 + kb - 1) / kb));
+  // force order of the rows (dense kernel): by slot range, widest first, so that the KS_FR rows
+  // of a chunk share a narrow window of slots
+  std::vector<int> frow(K.nrows), fpos(K.nrows);
+  for (int r = 0; r < K.nrows; ++r) frow[r] = r;
+  auto lo_of = [&](int r) { return kn[rows[r].x].x + nx; };
+  auto hi_of = [&](int r) { return lo_of(r) + rows[r].y - rows[r].x - 1; };
+  std::stable_sort(frow.begin(), frow.end(), [&](int a, int b) {
+    const int wa = hi_of(a) - lo_of(a), wb = hi_of(b) - lo_of(b);
+    return wa != wb ? wa > wb : lo_of(a) < lo_of(b);
+  });
+  for (int f = 0; f < K.nrows; ++f) fpos[frow[f]] = f;
+  std::vector<int2> fwin(K.nkchunks);
+  for (int c = 0; c < K.nkchunks; ++c) {
+    int lo = 1 << 30, hi = -1;
+    for (int f = c * KS_FR; f < std::min(K.nrows, (c + 1) * KS_FR); ++f) {
+      lo = std::min(lo, lo_of(frow[f]));
+      hi = std::max(hi, hi_of(frow[f]));
+    }
+    fwin[c] = make_int2(lo, hi);
+  }
+  // rho particle chunks: one wave of three blocks per SM, chunks a multiple of the 32-particle tile
+  const int kb = (K.nrows + 63) / 64 * ((2 * nx + 1 + 31) / 32);  // k_ks_rho: 64 rows x 32 slots
+  int pch = std::max(1, std::min(256, (3 * 152 + kb - 1) / kb));
   K.pchunk = std::max(32, ((K.nq + pch - 1) / pch + 31) / 32 * 32);
   K.npchunks = std::max(1, (K.nq + K.pchunk - 1) / K.pchunk);
   DA(K.kn, K.nk);
@@ -296,6 +311,9 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   DA(K.rows, K.nrows);
   DA(K.krow, K.nk);
   DA(K.chunk_row, K.nkchunks + 1);
+  DA(K.frow, K.nrows);
+  DA(K.fpos, K.nrows);
+  DA(K.fwin, K.nkchunks);
   DA(K.rho_part, (size_t)K.npchunks * 2 * K.nk);
   DA(K.fpart, (size_t)K.nkchunks * std::max(K.nq, 1) * 3);
   DA(K.red_part, 2 * KS_RED_MAX);
@@ -306,6 +324,7 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   if (ctx->S.mixed) {
     DA(K.tabf, (size_t)K.nq * K.ncol);
     DA(K.kdf, K.nk);
+    DA(K.wdense, (size_t)K.nrows * 4 * K.qx);
   } else {
     DA(K.tabd, (size_t)K.nq * K.ncol);
     DA(K.kdd, K.nk);
@@ -317,7 +336,11 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   CK(cudaMemcpyAsync(K.rows, rows.data(), sizeof(int4) * K.nrows, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(K.krow, krow.data(), sizeof(int) * K.nk, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(K.chunk_row, chunk_row.data(), sizeof(int) * (K.nkchunks + 1), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.frow, frow.data(), sizeof(int) * K.nrows, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.fpos, fpos.data(), sizeof(int) * K.nrows, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(K.fwin, fwin.data(), sizeof(int2) * K.nkchunks, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(K.ticket, 0, 2 * sizeof(unsigned), st));
+  if (K.wdense) CK(cudaMemsetAsync(K.wdense, 0, sizeof(float4) * K.nrows * 4 * K.qx, st));
   if (K.nq) {
     CK(cudaMemcpyAsync(K.qtag, qt.data(), sizeof(int) * K.nq, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(K.qval, qv.data(), sizeof(double) * K.nq, cudaMemcpyHostToDevice, st));

@@ -10,11 +10,13 @@
 //                 ([column][particle]) so that a warp reads 32 particles of one column at once;
 //   k_ks_rho:     thread per k-vector, tiles of 32 particles in shared memory holding X(+-nx) and
 //                 A = q Y Z for the rows the block spans: one complex product per (k, particle),
-//                 FP32 Kahan-compensated sums (MIXED) or FP64 sums, one partial per particle chunk;
+//                 plain sums over a tile and Kahan-compensated sums across tiles in FP32 (MIXED),
+//                 or FP64 sums; one partial per particle chunk;
 //   k_ks_rho_sum: the partials of each k summed in a fixed order, G Re rho and G Im rho for the
 //                 force, and U reduced deterministically (per-block partials, the last block sums);
 //   k_ks_force:   thread per particle, a chunk of whole rows per block: per row Y Z once, per k
-//                 one complex product; sum_k kx s_k per k, and ky, kz times the row sum of s_k;
+//                 one complex product; per row sum_k kx s_k and ky, kz times sum_k s_k, rows
+//                 added with Kahan compensation (MIXED);
 //   k_ks_force_sum: the chunk partials in a fixed order, times -8 pi q / V, into the force array.
 // dipolar_correction.f90:20-33 (Yeh-Berkowitz slab term) is k_ks_dipole + k_ks_dipole_force, FP64.
 // Every sum has a fixed order, so a charged run is reproducible bit for bit.
@@ -78,66 +80,139 @@ __global__ void k_ks_tables(DevState s, KSpace K) {
 
 constexpr int KS_TILE = 32;  // particles per shared-memory tile of k_ks_rho (one per lane)
 
+// rho(row, nx) = sum_p A(p, row) X(p, nx), A = q Y(ny) Z(nz): a complex matrix product per
+// block of KS_RB rows, 32 nx slots (blockIdx.z) and a chunk of particles.  Lane l owns slot
+// nx = 32 z + l - nxm, warp w owns rows 8 w .. 8 w + 7; slots outside a row's k-range are
+// computed and not stored.  Per particle a lane reads its X (the warp reads one contiguous
+// 256-byte row) and the eight A of its warp (broadcasts, four 16-byte loads) for 32 FMAs.
+// The staging stores, one particle per lane, use odd (X) or 4 mod 32 word (A) row strides.
+constexpr int KS_RHO_T = 256;  // threads of a k_ks_rho block (8 warps)
+constexpr int KS_RW = 8;       // rows per warp
+constexpr int KS_RB = 64;      // rows per block
+constexpr int KS_XS = 33;      // X row stride (8-byte slots)
+constexpr int KS_AS = KS_RB + 2;  // A row stride (8-byte slots; 16-byte aligned rows)
+
 template <bool MIXED>
-__global__ void __launch_bounds__(KS_KB) k_ks_rho(KSpace K) {
+__global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
   using real = kreal<MIXED>;
   using Cx = kcplx<MIXED>;
   extern __shared__ __align__(16) unsigned char shraw[];
-  const int nxc = 2 * K.nxm + 1;
-  const int k0 = blockIdx.x * KS_KB, k1 = min(K.nk, k0 + KS_KB);
-  const int r0 = K.krow[k0], nr = K.krow[k1 - 1] - r0 + 1;
-  Cx* Xs = reinterpret_cast<Cx*>(shraw);  // [KS_TILE][nxc]: X(nx) for nx = -nxm..nxm
-  Cx* As = Xs + KS_TILE * nxc;            // [KS_TILE][nr]:  q Y Z for the block's rows
+  Cx* Xs = reinterpret_cast<Cx*>(shraw);              // [KS_TILE][KS_XS]
+  Cx* As = Xs + KS_TILE * KS_XS;                      // [KS_TILE][KS_AS] (16-byte aligned)
+  int2* rc = reinterpret_cast<int2*>(As + KS_TILE * KS_AS);  // [KS_RB] signed Y column, Z column
   const Cx* tab = ktab<MIXED>(K);
-  const int k = k0 + threadIdx.x;
-  const bool act = k < k1;
-  int xi = 0, ri = 0;
-  if (act) {
-    xi = K.kn[k].x + K.nxm;
-    ri = K.krow[k] - r0;
-  }
+  const int rbeg = blockIdx.x * KS_RB, nr = min(KS_RB, K.nrows - rbeg);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = KS_RHO_T / 32;
+  const int sbase = blockIdx.z * 32;
+  const bool act = warp * KS_RW < nr;
+  for (int r = threadIdx.x; r < nr; r += KS_RHO_T) {
+    const int4 R = K.rows[rbeg + r];
+    const int yc = K.nxm + 1 + abs(R.z);
+    rc[r] = make_int2(R.z < 0 ? -yc : yc, K.nxm + K.nym + 2 + R.w);
+  }
   const int p_beg = blockIdx.y * K.pchunk, p_end = min(K.nq, p_beg + K.pchunk);
-  real sr = 0, si = 0, cr = 0, ci = 0;
+  real sr[KS_RW], si[KS_RW], cr[KS_RW], ci[KS_RW];
+#pragma unroll
+  for (int i = 0; i < KS_RW; ++i) sr[i] = si[i] = cr[i] = ci[i] = 0;
   for (int t0 = p_beg; t0 < p_end; t0 += KS_TILE) {
     const int nt = min(KS_TILE, p_end - t0);
     __syncthreads();
     if (lane < nt) {
       const int pq = t0 + lane;
-      for (int c = warp; c < nxc; c += KS_KB / 32) {
-        Cx v = tab[(size_t)abs(c - K.nxm) * K.nq + pq];
-        if (c < K.nxm) v.y = -v.y;
-        Xs[lane * nxc + c] = v;
-      }
       real q;
       if constexpr (MIXED) q = K.qvalf[pq]; else q = K.qval[pq];
-      for (int rr = warp; rr < nr; rr += KS_KB / 32) {
-        const int4 R = K.rows[r0 + rr];
-        Cx Y = tab[(size_t)(K.nxm + 1 + abs(R.z)) * K.nq + pq];
-        if (R.z < 0) Y.y = -Y.y;
-        const Cx Z = tab[(size_t)(K.nxm + K.nym + 2 + R.w) * K.nq + pq];
-        Cx A;
-        cmul(Y, Z, A);
-        A.x *= q;
-        A.y *= q;
-        As[lane * nr + rr] = A;
+      Cx xv[32 / NW];
+#pragma unroll
+      for (int i = 0; i < 32 / NW; ++i) {  // slot columns warp + NW i
+        const int nx = sbase + warp + NW * i - K.nxm;
+        xv[i].x = 0;
+        xv[i].y = 0;
+        if (nx <= K.nxm) {
+          xv[i] = tab[(size_t)abs(nx) * K.nq + pq];
+          if (nx < 0) xv[i].y = -xv[i].y;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 32 / NW; ++i) Xs[lane * KS_XS + warp + NW * i] = xv[i];
+#pragma unroll
+      for (int h = 0; h < KS_RB / NW; h += 4) {  // rows warp + NW (h .. h+3)
+        Cx yv[4], zv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = warp + NW * (h + i);
+          if (r < nr) {
+            const int2 R = rc[r];
+            yv[i] = tab[(size_t)abs(R.x) * K.nq + pq];
+            zv[i] = tab[(size_t)R.y * K.nq + pq];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = warp + NW * (h + i);
+          if (r < nr) {
+            if (rc[r].x < 0) yv[i].y = -yv[i].y;
+            Cx A;
+            cmul(yv[i], zv[i], A);
+            A.x *= q;
+            A.y *= q;
+            As[lane * KS_AS + r] = A;
+          }
+        }
       }
     }
     __syncthreads();
     if (act) {
-#pragma unroll 4
+      // plain sums over the tile's particles, compensated sums across tiles
+      real tr[KS_RW], ti[KS_RW];
+#pragma unroll
+      for (int i = 0; i < KS_RW; ++i) tr[i] = ti[i] = 0;
+#pragma unroll 1
       for (int p = 0; p < nt; ++p) {
-        Cx E;
-        cmul(Xs[p * nxc + xi], As[p * nr + ri], E);
-        ksum<MIXED>(sr, cr, E.x);
-        ksum<MIXED>(si, ci, E.y);
+        const Cx x = Xs[p * KS_XS + lane];
+        Cx A[KS_RW];
+        if constexpr (MIXED) {
+          const float4* A4 = reinterpret_cast<const float4*>(As + p * KS_AS + warp * KS_RW);
+#pragma unroll
+          for (int i = 0; i < KS_RW / 2; ++i) {
+            const float4 u = A4[i];
+            A[2 * i] = make_float2(u.x, u.y);
+            A[2 * i + 1] = make_float2(u.z, u.w);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < KS_RW; ++i) A[i] = As[p * KS_AS + warp * KS_RW + i];
+        }
+#pragma unroll
+        for (int i = 0; i < KS_RW; ++i) {
+          tr[i] = fma(x.x, A[i].x, tr[i]);
+          tr[i] = fma(-x.y, A[i].y, tr[i]);
+          ti[i] = fma(x.x, A[i].y, ti[i]);
+          ti[i] = fma(x.y, A[i].x, ti[i]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < KS_RW; ++i) {
+        ksum<MIXED>(sr[i], cr[i], tr[i]);
+        ksum<MIXED>(si[i], ci[i], ti[i]);
       }
     }
   }
   if (act) {
+    const int nx = sbase + lane - K.nxm;
     double* o = K.rho_part + (size_t)blockIdx.y * 2 * K.nk;
-    o[2 * k] = (double)sr - (double)cr;
-    o[2 * k + 1] = (double)si - (double)ci;
+#pragma unroll
+    for (int i = 0; i < KS_RW; ++i) {
+      const int r = warp * KS_RW + i;
+      if (r < nr) {
+        const int4 R = K.rows[rbeg + r];
+        const int k = R.x + nx - K.kn[R.x].x;
+        if (k >= R.x && k < R.y) {
+          o[2 * k] = (double)sr[i] - (double)cr[i];
+          o[2 * k + 1] = (double)si[i] - (double)ci[i];
+        }
+      }
+    }
   }
 }
 
@@ -166,23 +241,49 @@ __device__ __forceinline__ bool grid_sum_last(double v, double* part, unsigned* 
   return true;
 }
 
+// Thread (k, g) of a block of 32 k x 8 groups sums the chunk partials c = g, g + 8, ..; the
+// eight group sums are then added in group order: a fixed order for every k.
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, Acc acc, bool eflag) {
+  __shared__ double2 part[8][32];
+  const int kl = threadIdx.x & 31, g = threadIdx.x >> 5;
   double u = 0.;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K.nk; k += gridDim.x * blockDim.x) {
+  const int nkb = (K.nk + 31) / 32;
+  for (int kb = blockIdx.x; kb < nkb; kb += gridDim.x) {
+    const int k = kb * 32 + kl;
     double re = 0., im = 0.;
-    for (int c = 0; c < K.npchunks; ++c) {
-      const double2 v = reinterpret_cast<const double2*>(K.rho_part + (size_t)c * 2 * K.nk)[k];
-      re += v.x;
-      im += v.y;
+    if (k < K.nk) {
+#pragma unroll 4
+      for (int c = g; c < K.npchunks; c += 8) {
+        const double2 v = reinterpret_cast<const double2*>(K.rho_part + (size_t)c * 2 * K.nk)[k];
+        re += v.x;
+        im += v.y;
+      }
     }
-    reinterpret_cast<double2*>(K.rho)[k] = make_double2(re, im);
-    const double G = K.kfac[k];
-    u += G * (re * re + im * im);
-    if constexpr (MIXED)
-      K.kdf[k] = make_float4((float)K.kvec[3 * k], (float)(G * re), (float)(G * im), __int_as_float(K.kn[k].x + K.nxm));
-    else
-      K.kdd[k] = make_double2(G * re, G * im);
+    part[g][kl] = make_double2(re, im);
+    __syncthreads();
+    if (g == 0 && k < K.nk) {
+      re = 0.;
+      im = 0.;
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        re += part[h][kl].x;
+        im += part[h][kl].y;
+      }
+      reinterpret_cast<double2*>(K.rho)[k] = make_double2(re, im);
+      const double G = K.kfac[k];
+      u += G * (re * re + im * im);
+      if constexpr (MIXED) {
+        const double kx = K.kvec[3 * k], a = G * re, b = G * im;
+        const int xi = K.kn[k].x + K.nxm;
+        K.kdf[k] = make_float4((float)kx, (float)a, (float)b, __int_as_float(xi));
+        K.wdense[(size_t)K.fpos[K.krow[k]] * 4 * K.qx + xi] =
+            make_float4((float)a, (float)b, (float)(kx * a), (float)(kx * b));
+      } else {
+        K.kdd[k] = make_double2(G * re, G * im);
+      }
+    }
+    __syncthreads();
   }
   double tot;
   if (grid_sum_last(u, K.red_part, K.ticket, tot) && eflag) acc.col(O_VCOULK)[K.rep] += tot * pi4 * K.inv_V;
@@ -269,19 +370,105 @@ __global__ void __launch_bounds__(KS_FB) k_ks_force(KSpace K) {
     if (R.z < 0) Y.y = -Y.y;
     Cx YZ;
     cmul(Y, Z, YZ);
-    real srow = 0;
+    // plain sums along the row (at most 2 nxm + 1 terms), compensated sums across rows
+    real srow = 0, sxrow = 0;
 #pragma unroll 4
     for (int k = R.x; k < R.y; ++k) {
       const KD<MIXED> d = kd[k];
       Cx E;
       cmul(X[d.xi * KS_FB], YZ, E);
       const real sg = E.x * d.b - E.y * d.a;
-      ksum<MIXED>(fx, cx, d.kx * sg);
+      sxrow = fma(d.kx, sg, sxrow);
       srow += sg;
     }
     const real2 w = ryz[r];
+    ksum<MIXED>(fx, cx, sxrow);
     ksum<MIXED>(fy, cy, w.x * srow);
     ksum<MIXED>(fz, cz, w.y * srow);
+    R = Rn;
+    Y = Yn;
+    Z = Zn;
+  }
+  double* o = K.fpart + ((size_t)blockIdx.y * K.nq + p) * 3;
+  o[0] = (double)fx - (double)cx;
+  o[1] = (double)fy - (double)cy;
+  o[2] = (double)fz - (double)cz;
+}
+
+// Mixed precision, 4 QX = 4..32 slots: the thread keeps X(p, nx) for every slot in registers and
+// reads the dense slot table (W, kx W), W = G rho, of a chunk of rows from shared memory (one
+// broadcast 16-byte load per slot).  With S = sum_nx conj(X) W and Sx = sum_nx conj(X) kx W over
+// a row, that row adds Im(conj(Y Z) Sx) to F_x and ky, kz times Im(conj(Y Z) S) to F_y, F_z.
+// The rows are taken in order of their slot range (frow), so that the rows of a chunk share a
+// narrow window of slots; slots outside the window are skipped (a branch uniform over the block).
+template <int QX>
+__global__ void __launch_bounds__(KS_FB) k_ks_force_dense(KSpace K) {
+  constexpr int NXP = 4 * QX;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  float4* Wd = reinterpret_cast<float4*>(shraw);          // [KS_FR][NXP]
+  int2* rc = reinterpret_cast<int2*>(Wd + KS_FR * NXP);   // [KS_FR] signed Y column, Z column
+  float2* ryz = reinterpret_cast<float2*>(rc + KS_FR);    // [KS_FR] ky, kz
+  const int rbeg = blockIdx.y * KS_FR, nr = min(KS_FR, K.nrows - rbeg);
+  const int2 win = K.fwin[blockIdx.y];  // slots win.x .. win.y
+  const float4* wsrc = K.wdense + (size_t)rbeg * NXP;
+  for (int e = threadIdx.x; e < nr * NXP; e += KS_FB) Wd[e] = wsrc[e];
+  for (int r = threadIdx.x; r < nr; r += KS_FB) {
+    const int4 R = K.rows[K.frow[rbeg + r]];
+    const int yc = K.nxm + 1 + abs(R.z);
+    rc[r] = make_int2(R.z < 0 ? -yc : yc, K.nxm + K.nym + 2 + R.w);
+    ryz[r] = make_float2((float)K.kvec[3 * R.x + 1], (float)K.kvec[3 * R.x + 2]);
+  }
+  const int p = blockIdx.x * KS_FB + threadIdx.x;
+  const int pc = min(p, K.nq - 1);
+  const float2* T = K.tabf + pc;
+  float2 X[NXP];
+#pragma unroll
+  for (int j = 0; j < NXP; ++j) {
+    X[j] = make_float2(0.f, 0.f);
+    if (j >= win.x && j <= win.y) {
+      X[j] = T[(size_t)abs(j - K.nxm) * K.nq];
+      if (j < K.nxm) X[j].y = -X[j].y;
+    }
+  }
+  __syncthreads();
+  if (p >= K.nq) return;
+  float fx = 0.f, fy = 0.f, fz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  int2 R = rc[0];
+  float2 Y = T[(size_t)abs(R.x) * K.nq], Z = T[(size_t)R.y * K.nq];
+  for (int r = 0; r < nr; ++r) {
+    int2 Rn = R;
+    float2 Yn = Y, Zn = Z;
+    if (r + 1 < nr) {
+      Rn = rc[r + 1];
+      Yn = T[(size_t)abs(Rn.x) * K.nq];
+      Zn = T[(size_t)Rn.y * K.nq];
+    }
+    if (R.x < 0) Y.y = -Y.y;
+    float2 YZ;
+    cmul(Y, Z, YZ);
+    const float4* w = Wd + r * NXP;
+    float s_re = 0.f, s_im = 0.f, x_re = 0.f, x_im = 0.f;
+#pragma unroll
+    for (int g = 0; g < QX; ++g) {  // groups of four slots; a group outside the window is skipped
+      if (4 * g + 3 < win.x || 4 * g > win.y) continue;
+      float4 v[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) v[i] = w[4 * g + i];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {  // conj(X) W = (X.x W.x + X.y W.y) + i (X.x W.y - X.y W.x)
+        const float2 x = X[4 * g + i];
+        s_re = fmaf(x.x, v[i].x, fmaf(x.y, v[i].y, s_re));
+        s_im = fmaf(x.x, v[i].y, fmaf(-x.y, v[i].x, s_im));
+        x_re = fmaf(x.x, v[i].z, fmaf(x.y, v[i].w, x_re));
+        x_im = fmaf(x.x, v[i].w, fmaf(-x.y, v[i].z, x_im));
+      }
+    }
+    const float srow = YZ.x * s_im - YZ.y * s_re;
+    const float sxrow = YZ.x * x_im - YZ.y * x_re;
+    const float2 kyz = ryz[r];
+    ksum<true>(fx, cx, sxrow);
+    ksum<true>(fy, cy, kyz.x * srow);
+    ksum<true>(fz, cz, kyz.y * srow);
     R = Rn;
     Y = Yn;
     Z = Zn;
@@ -317,13 +504,28 @@ __global__ void k_ks_force_sum(DevState s, KSpace K, double pi8, bool to_f4) {
 
 namespace {
 size_t rho_smem(const KSpace& K, bool mixed) {
-  return (size_t)KS_TILE * (2 * K.nxm + 1 + K.rho_rows_max) * (mixed ? sizeof(float2) : sizeof(double2));
+  return (size_t)KS_TILE * (KS_XS + KS_AS) * (mixed ? sizeof(float2) : sizeof(double2)) +
+         (size_t)KS_RB * sizeof(int2);
 }
 size_t force_smem(const KSpace& K, bool mixed) {
   const size_t cx = mixed ? sizeof(float2) : sizeof(double2);
   return (size_t)(2 * K.nxm + 1) * KS_FB * cx + (size_t)K.fchunk_k_max * (mixed ? sizeof(KD<true>) : sizeof(KD<false>)) +
          (size_t)K.fchunk_rows_max * (sizeof(int4) + cx);
 }
+size_t dense_smem(const KSpace& K) {
+  return (size_t)KS_FR * (4 * K.qx * sizeof(float4) + sizeof(int2) + sizeof(float2));
+}
+constexpr int KS_DENSE_QX_MAX = 8;  // the register-resident X of k_ks_force_dense: nxm <= 15
+
+template <int QX>
+void launch_dense(const KSpace& K, dim3 g, cudaStream_t st) {
+  k_ks_force_dense<QX><<<g, KS_FB, dense_smem(K), st>>>(K);
+}
+typedef void (*dense_launcher)(const KSpace&, dim3, cudaStream_t);
+const dense_launcher kDense[KS_DENSE_QX_MAX + 1] = {nullptr,          launch_dense<1>, launch_dense<2>,
+                                                    launch_dense<3>, launch_dense<4>, launch_dense<5>,
+                                                    launch_dense<6>, launch_dense<7>, launch_dense<8>};
+bool use_dense(const KSpace& K, bool mixed) { return mixed && K.qx <= KS_DENSE_QX_MAX; }
 }  // namespace
 
 int kspace_prepare(const KSpace& K, bool mixed) {
@@ -337,7 +539,7 @@ int kspace_prepare(const KSpace& K, bool mixed) {
     e = cudaFuncSetAttribute(k_ks_rho<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
   }
-  return (int)e;
+  return (int)e;  // dense_smem stays below 48 KB: 32 rows x 32 slots x 16 B + 512 B
 }
 
 void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
@@ -347,17 +549,21 @@ void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaSt
   const int nt = K.nq * K.ncol;
   if (s.mixed) k_ks_tables<true><<<(nt + 255) / 256, 256, 0, st>>>(s, K);
   else k_ks_tables<false><<<(nt + 255) / 256, 256, 0, st>>>(s, K);
-  const dim3 g1((K.nk + KS_KB - 1) / KS_KB, K.npchunks);
+  const dim3 g1((K.nrows + KS_RB - 1) / KS_RB, K.npchunks, (2 * K.nxm + 1 + 31) / 32);
   const size_t shm1 = rho_smem(K, s.mixed);
-  if (s.mixed) k_ks_rho<true><<<g1, KS_KB, shm1, st>>>(K);
-  else k_ks_rho<false><<<g1, KS_KB, shm1, st>>>(K);
-  const int gs = std::min(KS_RED_MAX, (K.nk + 255) / 256);
+  if (s.mixed) k_ks_rho<true><<<g1, KS_RHO_T, shm1, st>>>(K);
+  else k_ks_rho<false><<<g1, KS_RHO_T, shm1, st>>>(K);
+  const int gs = std::min(KS_RED_MAX, (K.nk + 31) / 32);
   if (s.mixed) k_ks_rho_sum<true><<<gs, 256, 0, st>>>(K, 4. * pi, acc, eflag);
   else k_ks_rho_sum<false><<<gs, 256, 0, st>>>(K, 4. * pi, acc, eflag);
   const dim3 g2((K.nq + KS_FB - 1) / KS_FB, K.nkchunks);
-  const size_t shm2 = force_smem(K, s.mixed);
-  if (s.mixed) k_ks_force<true><<<g2, KS_FB, shm2, st>>>(K);
-  else k_ks_force<false><<<g2, KS_FB, shm2, st>>>(K);
+  if (use_dense(K, s.mixed)) {
+    kDense[K.qx](K, g2, st);
+  } else {
+    const size_t shm2 = force_smem(K, s.mixed);
+    if (s.mixed) k_ks_force<true><<<g2, KS_FB, shm2, st>>>(K);
+    else k_ks_force<false><<<g2, KS_FB, shm2, st>>>(K);
+  }
   k_ks_force_sum<<<(K.nq + 127) / 128, 128, 0, st>>>(s, K, 8. * pi, fused && s.mixed);
 }
 

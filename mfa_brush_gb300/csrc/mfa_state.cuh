@@ -112,12 +112,19 @@ struct KSpace {
   int nrows;
   int4* rows;           // [nrows] (first k, end k, ny, nz)
   int* krow;            // [nk] row of each k
-  // rho: blocks of KS_KB k-vectors x particle chunks; partials summed in a fixed order
-  int pchunk, npchunks, rho_rows_max;
+  // rho: blocks of rows and nx slots x particle chunks; partials summed in a fixed order.
+  // The dense slot table has 4 qx slots per row, nx = -nxm .. -nxm + 4 qx - 1.
+  int qx;
+  int pchunk, npchunks;
   double* rho_part;     // [npchunks][2*nk]
   float4* kdf;          // [nk] (kx, G Re rho, G Im rho, nx + nxm as int bits)   (mixed)
   double2* kdd;         // [nk] (G Re rho, G Im rho)                              (fp64)
-  // force: chunks of whole rows
+  float4* wdense;       // [nrows][4 qx] (W, kx W) per slot, W = G rho, rows in frow order;
+                        // zero where no k (mixed)
+  int* frow;            // [nrows] rows in order of their slot range (force order) ...
+  int* fpos;            // [nrows] ... and the position of each row in that order
+  int2* fwin;           // [nkchunks] slot window of each force chunk (dense kernel)
+  // force: chunks of KS_FR whole rows
   int nkchunks, fchunk_k_max, fchunk_rows_max;
   int* chunk_row;       // [nkchunks+1] first row of each chunk
   double* fpart;        // [nkchunks][nq][3] per-chunk force partials, summed in a fixed order
@@ -126,9 +133,8 @@ struct KSpace {
   unsigned* ticket;     // [2] zero between launches
   int rep;
 };
-constexpr int KS_KB = 256;       // k-vectors per rho block
 constexpr int KS_FB = 128;       // particles per force block
-constexpr int KS_FK = 512;       // k-vectors per force chunk, at most (whole rows)
+constexpr int KS_FR = 32;        // rows per force chunk
 constexpr int KS_RED_MAX = 256;  // blocks of a grid reduction, at most
 // host-side preparation of the kernels (shared-memory opt-in); returns a CUDA error
 int kspace_prepare(const KSpace& K, bool mixed);

@@ -286,6 +286,26 @@ def test_deterministic_and_momentum(gpu):
     assert np.abs(f.sum(0)).max() < 1e-5 * np.abs(f).sum()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_charged_run_deterministic(gpu, precision):
+    """A charged system (slab Ewald + dipolar correction) run twice gives bit-identical states and
+    energies: every k-space sum (rho over particle chunks, U over blocks, forces over k-chunks,
+    M_z) is taken in a fixed order, without floating-point atomics."""
+    p, s, a_type, r0, v = charged_system()
+    out = []
+    for _ in range(2):
+        g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+        g.step(30)
+        g.zero_force()
+        uk = g.ewald_k()[0]
+        ud = g.dipolar_correction()[0]
+        out.append((uk, ud) + tuple(g.state()))
+        g.close()
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    for x, y in zip(out[0][2:], out[1][2:]):
+        assert np.array_equal(x, y)
+
+
 def test_state_round_trip_pinned_and_pageable(gpu):
     """mfa_set_state reads page-locked arrays directly and pageable ones through the staging
     buffer; mfa_sync_to_host fills both kinds alike.  Both give the same state, and a round trip
