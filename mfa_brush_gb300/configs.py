@@ -327,6 +327,25 @@ def two_liquid_inputs(gamma=5.0, kT=1.0, dt=0.005, eps_ab=0.5, f_x=0.01):
     return inp
 
 
+def charged_brush(gamma=5.0, seed=41):
+    """The charged-brush channel at full size: 40 x 40 x 30, grafting density 0.1, N = 40, solvent
+    to 0.7; slab Ewald (SYSTEM 3) with alpha_c = 0.81, real-space cut-off 3 and |k| <= 12 (2 pi / L)
+    (8070 k-vectors under the reference's k-set rule), dipolar correction.  The line charge of
+    "every 10th bead -1" is spread as -0.1 per brush bead and neutralised by the solvent.  The
+    lattice is filled to 75 % (a fuller lattice at this seed starts with a contact that the FP64
+    reference algorithm does not survive).  Returns (mfa_params, (System, a_type, r0, v))."""
+    s, a_type, r0, v = brush_channel(40.0, 30.0, 0.1, 40, rho=0.7, seed=seed, max_fill=0.75)
+    n_brush = int(np.sum(a_type == 2))
+    n_solv = int(np.sum(a_type == 3))
+    inp = wca_inputs(gamma=gamma, thermostat=0)
+    inp.flags.system = 3
+    inp.charge[1] = -0.1
+    inp.charge[2] = 0.1 * n_brush / n_solv
+    inp.alpha_c, inp.n_kmax, inp.rc_coul = 0.81, 12, 3.0
+    p, _ = md.derive(inp)
+    return p, (s, a_type, r0, v)
+
+
 def small_channel(seed=1):
     """20x20x20 channel, 40 chains of 30 beads per wall (grafting density 0.1), solvent to 0.8."""
     return brush_channel(20.0, 20.0, 0.1, 30, rho=0.8, seed=seed)

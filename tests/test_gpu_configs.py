@@ -146,6 +146,63 @@ def test_nve_drift_mixed_within_2x_fp64_oracle(gpu, oracle_mod):
     assert slope_g <= 2.0 * max(slope_o, 1e-9)
 
 
+def test_charged_nve_energy_excursion_within_3x_fp64_oracle(gpu, oracle_mod):
+    """2000 NVE steps (no thermostat) of a strongly charged brush channel (brush beads -1, solvent
+    +1, slab Ewald, dipolar correction) through the fused mixed-precision step: the total energy,
+    Coulomb terms included, starts where the FP64 oracle's does, and its largest excursion from
+    the start stays within 3x of the oracle's (or 1e-5 of |E|)."""
+    inp = configs.wca_inputs(gamma=0.0, thermostat=1)
+    inp.flags.system = 3
+    inp.charge[1], inp.charge[2] = -1.0, 1.0
+    inp.alpha_c, inp.n_kmax, inp.rc_coul = 0.81, 5, 3.0
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(10.0, 10.0, 0.08, 10, rho=0.5, seed=21, kT=0.5, max_fill=0.75)
+    n, every = 2000, 200
+    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+
+    def run_g(k):
+        g.step(k)
+        return g.energies()[0]["e_total"]
+
+    threads = max(1, os.cpu_count() or 1)
+
+    def run_o(k):
+        o.step(k, threads, 0)
+        return sum(o.energies().values())
+
+    eg = _energy_series(run_g, n, every)
+    eo = _energy_series(run_o, n, every)
+    dg = np.abs(eg - eg[0]).max()
+    do = np.abs(eo - eo[0]).max()
+    print("charged NVE, %d steps: E %.4f (mixed) %.4f (fp64 oracle); largest excursion %.3e / %.3e"
+          % (n, eg[0], eo[0], dg, do))
+    assert np.all(np.isfinite(eg))
+    assert abs(eg[0] - eo[0]) < 1e-3 * abs(eo[0])
+    assert dg <= 3.0 * max(do, 1e-5 * abs(eo[0]))
+
+
+def test_charged_brush_full_size_stays_in_channel(gpu):
+    """The full-size charged brush (33,600 particles, 8070 k-vectors) for 300 fused mixed steps
+    under the DPD thermostat: every particle stays in the channel and the energies stay finite.
+    The lattice start releases heat that the DPD thermostat, acting inside the WCA range only,
+    removes over ~10^3 steps: the FP64 oracle on the same start (without the weak charges) has
+    <v^2> = 2.05 per component at step 300, and the charged run must be close to that."""
+    p, (s, a_type, r0, v) = configs.charged_brush()
+    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
+    g.step(300)
+    r, vv, _, _ = g.state()
+    e = g.energies()[0]
+    g.close()
+    assert np.all(np.isfinite(r)) and np.all(np.isfinite(vv))
+    assert r[:, 2].min() > 0.0 and r[:, 2].max() < s.boundary[2]
+    mob = a_type != 1
+    t_kin = np.mean(vv[mob] ** 2)
+    print("charged brush after 300 steps: <v^2> per component %.3f, e_total %.1f" % (t_kin, e["e_total"]))
+    assert 1.8 < t_kin < 2.3
+    assert np.isfinite(e["e_total"])
+
+
 def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod):
     """The charged-brush case at its full size: 40 x 40 x 30 channel, grafting density 0.1, N = 40,
     slab Ewald with alpha = 0.9 (alpha_c = 0.81), real-space cut-off 3, |k| <= 12 (2 pi / L) with
