@@ -6,7 +6,7 @@ gamma=5, kT=1, dt=0.005), ~4.7M particles, batched in one context, mixed precisi
 bond arithmetic on fixed-point positions, FP64 integration), graph-captured 10-step chunks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision mixed|fp64]
-  python bench.py --workload charged-brush [--steps K] [--warmup W] [--precision mixed|fp64]
+  python bench.py --workload charged-brush|melt-brush [--steps K] [--warmup W] [--precision mixed|fp64]
 
 A step is one full MD step of all replicas.  `value` times K steps with the state resident on the
 device (CUDA events on the library's stream).  `e2e` times the same steps through the C ABI with
@@ -174,12 +174,26 @@ def run_reference(args, rank, world):
     return 0
 
 
-def run_charged(args):
-    """The charged-brush channel (one replica, 33,600 particles, slab Ewald with 8070 k-vectors):
-    the same step, timed the same way; per-kernel-family times show the k-space share."""
-    from mfa_brush_gb300 import build, configs, md
+SINGLE = {
+    "charged-brush": "charged brush channel 40x40x30, N=40, grafting 0.1, -4 per chain + 1280 +1 "
+                     "counterions, slab Ewald (alpha_c 0.81, 8070 k-vectors, r_c 3) + DPD",
+    "melt-brush": "melt in brush 100x100x40, grafting 0.2 per wall, N=50, melt N=20 to 0.85, cosine "
+                  "bending k_b=2, LJ 2*2^(1/6) with eps_bm=1.2, brush WCA, DPD",
+}
+
+
+def run_single(args):
+    """One large system (the charged-brush channel or the melt-in-brush channel): the same step,
+    timed the same way, with the FP32 roofline of its dominant kernel family: the k-space sums
+    (8 FLOP per (k, charged particle) for the structure factor, 15 for the force) or the pair
+    kernel (LJ 18 + DPD 22 FLOP per evaluation of an interacting pair, each pair evaluated from
+    both sides), against the FP32 FMA throughput measured by mfa_fp32_fma_peak."""
+    from mfa_brush_gb300 import abi, build, configs, md
     build.build()
-    p, (s, a_type, r0, v) = configs.charged_brush()
+    if args.workload == "charged-brush":
+        p, (s, a_type, r0, v) = configs.charged_brush()
+    else:
+        p, (s, a_type, r0, v) = configs.melt_brush()
     skin = 0.5 if args.skin == "auto" else float(args.skin)
     g = md.MdSystem(p, s, a_type, r0, v, precision=args.precision, skin=skin)
     done = 0
@@ -203,16 +217,34 @@ def run_charged(args):
     kt = g.kernel_times(args.kernel_steps)
     t = ms / 1000.0
     n = int(s.n_part)
+    peak = abi.f64(0.0)
+    roof = None
+    if abi.load_library().mfa_fp32_fma_peak(0, abi.C.byref(peak)) == 0:
+        if args.workload == "charged-brush":
+            nk, nq = g.kspace_info()
+            fam, flop = "kspace", 23.0 * nk * nq
+            what = "k-space family (k_ks_*), %d k-vectors x %d charged particles" % (nk, nq)
+        else:
+            npair = len(g.pair_list(0))
+            fam, flop = "pair", 2.0 * 40.0 * npair
+            what = "k_pair, %d interacting pairs (each evaluated from both sides)" % npair
+        if kt.get(fam, (0, 0))[1]:
+            achieved = flop / (kt[fam][0] / 1000.0) / 1e12
+            roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                    "frac": achieved / peak.value, "traffic": None, "kernel": what,
+                    "peak_kind": "measured (mfa_fp32_fma_peak: FMA chains, 8 warps per sub-partition)"}
     line = {"metric": METRIC, "value": n * args.steps / t, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
-            "data": "synthetic (seeded charged brush channel)",
-            "config": {"workload": "charged brush channel 40x40x30, N=40, grafting 0.1, slab Ewald "
-                                   "(alpha_c 0.81, 8070 k-vectors, r_c 3) + DPD",
-                       "particles": n, "precision": args.precision, "chunk_steps": CHUNK, "skin": skin,
-                       "l2_flush": "none: the 33.6k-particle working set fits in L2 (charged case)"},
+            "data": "synthetic (seeded %s channel)" % args.workload,
+            "config": {"workload": SINGLE[args.workload], "particles": n, "precision": args.precision,
+                       "chunk_steps": CHUNK, "skin": skin,
+                       "l2_flush": ("inputs larger than L2" if n * 96 > 129e6
+                                    else "none: the working set fits in L2")},
             "gpu_launches": int(launches + 10 * rebuilds),
+            "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
+            "roofline": roof,
             "clocks": clocks}
     print(json.dumps(line), flush=True)
     g.close()
@@ -221,8 +253,9 @@ def run_charged(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="brush-replicas", choices=["brush-replicas", "charged-brush"],
-                    help="brush-replicas: the benchmark; charged-brush: the slab-Ewald channel")
+    ap.add_argument("--workload", default="brush-replicas", choices=["brush-replicas", "charged-brush", "melt-brush"],
+                    help="brush-replicas: the benchmark; charged-brush: the slab-Ewald channel; "
+                         "melt-brush: the 340k-particle melt-in-brush channel")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=60)
@@ -250,12 +283,12 @@ def main():
         if torch.cuda.is_available():
             torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    if args.workload == "charged-brush":
+    if args.workload in SINGLE:
         if args.impl == "reference" or world > 1:
-            print(json.dumps({"impl": args.impl, "unavailable": "the charged-brush workload is timed "
-                              "for the library on one GPU only"}), flush=True)
+            print(json.dumps({"impl": args.impl, "unavailable": "the %s workload is timed for the "
+                              "library on one GPU only" % args.workload}), flush=True)
             return 0
-        return run_charged(args)
+        return run_single(args)
     if args.impl == "reference":
         r = run_reference(args, rank, world)
         if dist is not None:

@@ -281,6 +281,9 @@ int mfa_step(mfa_ctx* ctx, int32_t nsteps);
    far.  When the largest count passes 85 % of the capacity, the next mfa_step or
    mfa_verlet_positions raises the capacity by half (up to its maximum) and rebuilds the lists. */
 int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count);
+/* Size of the reciprocal-space sum: k-vectors of the reference's k-set (ewald_k.f90:47-124) and
+   charged particles; both 0 for an uncharged context.                                         */
+int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged);
 /* Absolute step counter of replica 0 (s_time + steps done). */
 int mfa_get_step(mfa_ctx* ctx, int64_t* step);
 
@@ -332,6 +335,10 @@ int mfa_event_elapsed(mfa_ctx* ctx, int32_t slot_a, int32_t slot_b, float* ms);
 #define MFA_NKFAM 8
 int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* launches);
 const char* mfa_kernel_name(int32_t fam);
+/* FP32 FMA throughput of `device` in TFLOP/s (2 FLOP per FMA), measured by eight independent
+   FMA chains per thread on 8 warps per SM sub-partition, best of 10 timed launches: the roof
+   for the FP32-issue-bound kernels.  No counterpart in the reference (a measurement aid).    */
+int mfa_fp32_fma_peak(int32_t device, double* tflops);
 /* Number of kernel launches issued by the library since the context was created. */
 int mfa_launch_count(mfa_ctx* ctx, int64_t* n);
 /* Number of cell-sort + neighbour-list rebuilds since the context was created (synchronises). */

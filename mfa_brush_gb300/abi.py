@@ -155,6 +155,7 @@ SIGNATURES = {
     "mfa_get_profiles": (i32, [vp, i32, dp, dp, dp, P(i64)]),
     "mfa_observe": (i32, [vp, P(Observables)]),
     "mfa_list_stats": (i32, [vp, ip, ip]),
+    "mfa_kspace_info": (i32, [vp, ip, ip]),
     "mfa_reset_profiles": (i32, [vp]),
     "mfa_cell_list": (i32, [vp, i32, i32, ip, ip, i32, ip]),
     "mfa_cell_neigh_list": (i32, [ip, i32, ip]),
@@ -164,6 +165,7 @@ SIGNATURES = {
     "mfa_event_elapsed": (i32, [vp, i32, i32, P(C.c_float)]),
     "mfa_kernel_times": (i32, [vp, i32, P(C.c_float), ip]),
     "mfa_kernel_name": (C.c_char_p, [i32]),
+    "mfa_fp32_fma_peak": (i32, [i32, dp]),
     "mfa_launch_count": (i32, [vp, P(i64)]),
     "mfa_rebuild_count": (i32, [vp, P(i64)]),
 }

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + INCLUDE]
 SOURCES = ["mfa_rebuild.cu", "mfa_forces.cu", "mfa_integrate.cu", "mfa_kspace.cu", "mfa_api.cu",
-           "mfa_host.cpp"]
+           "mfa_probe.cu", "mfa_host.cpp"]
 
 
 def nvcc():

@@ -71,11 +71,18 @@ def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=No
     occ[:, :, nz - 1] = True
     sites = np.zeros((n, 3), np.int64)
 
-    def regrow(pos, ci, k, w0):
-        """Serial self-avoiding regrowth of beads 1..k of chain ci (its old sites are freed)."""
+    def regrow(pos, ci, k, w0, movable=False):
+        """Serial self-avoiding regrowth of beads 1..k of chain ci (its old sites are freed).  A
+        free chain (movable) whose start is walled in moves its start to another free site after
+        every 20 failed attempts; a grafted chain keeps its anchor."""
         old = pos[ci, 1:k]
         occ[old[:, 0], old[:, 1], old[:, 2]] = False
-        for _ in range(200):
+        for attempt in range(200):
+            if movable and attempt and attempt % 20 == 0:
+                occ[tuple(pos[ci, 0])] = False
+                free_idx = np.flatnonzero(~occ.ravel())
+                pos[ci, 0] = np.unravel_index(rng.choice(free_idx), occ.shape)
+                occ[tuple(pos[ci, 0])] = True
             placed = []
             cur = pos[ci, 0]
             ok = True
@@ -128,7 +135,7 @@ def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=No
                 if np.any(stuck):
                     # a walk trapped itself: regrow that chain alone (beads 1..k) from its anchor
                     for ci in todo[stuck]:
-                        regrow(pos, ci, k, wdir[ci])
+                        regrow(pos, ci, k, wdir[ci], movable=zdir is None)
                     todo = todo[~stuck]
                     if len(todo) == 0:
                         break
@@ -328,21 +335,65 @@ def two_liquid_inputs(gamma=5.0, kT=1.0, dt=0.005, eps_ab=0.5, f_x=0.01):
 
 
 def charged_brush(gamma=5.0, seed=41):
-    """The charged-brush channel at full size: 40 x 40 x 30, grafting density 0.1, N = 40, solvent
-    to 0.7; slab Ewald (SYSTEM 3) with alpha_c = 0.81, real-space cut-off 3 and |k| <= 12 (2 pi / L)
-    (8070 k-vectors under the reference's k-set rule), dipolar correction.  The line charge of
-    "every 10th bead -1" is spread as -0.1 per brush bead and neutralised by the solvent.  The
-    lattice is filled to 75 % (a fuller lattice at this seed starts with a contact that the FP64
-    reference algorithm does not survive).  Returns (mfa_params, (System, a_type, r0, v))."""
+    """The charged-brush channel at full size: 40 x 40 x 30, grafting density 0.1, N = 40, total
+    density 0.7; slab Ewald (SYSTEM 3) with alpha_c = 0.81, real-space cut-off 3 and
+    |k| <= 12 (2 pi / L) (8070 k-vectors under the reference's k-set rule), dipolar correction.
+    Charge is per type in the reference, so "every 10th bead -1" (four charges per 40-bead chain)
+    is spread over the 39 non-head beads of each chain (q = -4/39).  The same number of +1
+    counterions (1280) are the fourth species (PARTICLE_4, single beads, WCA with everything),
+    drawn at random among the free beads and stored after the neutral solvent, as the reference
+    orders its molecules.  The lattice is filled to 75 % (a fuller lattice at this seed starts
+    with a contact that the FP64 reference algorithm does not survive).
+    Returns (mfa_params, (System, a_type, r0, v))."""
     s, a_type, r0, v = brush_channel(40.0, 30.0, 0.1, 40, rho=0.7, seed=seed, max_fill=0.75)
-    n_brush = int(np.sum(a_type == 2))
-    n_solv = int(np.sum(a_type == 3))
+    n_brush = s.n_mon * s.n_chain
+    n_ci = 4 * s.n_chain
+    rng = np.random.default_rng(seed + 1)
+    free = np.arange(n_brush, s.n_mon_tot)
+    ci = np.sort(rng.choice(free, n_ci, replace=False))
+    solv = np.setdiff1d(free, ci)
+    order = np.concatenate([np.arange(n_brush), solv, ci])
+    a_type, r0, v = a_type[order].copy(), r0[order].copy(), v[order].copy()
+    a_type[n_brush + len(solv):] = 4
+    s.n_mon_d, s.n_chain_d = 1, len(solv)
+    s.n_mon_e, s.n_chain_e = 1, n_ci
     inp = wca_inputs(gamma=gamma, thermostat=0)
-    inp.flags.system = 3
-    inp.charge[1] = -0.1
-    inp.charge[2] = 0.1 * n_brush / n_solv
+    f = inp.flags
+    f.system, f.particle_4 = 3, 1
+    inp.inter4 = 1
+    inp.a_w4, inp.sigma_w4 = inp.a_w, inp.sigma_w
+    inp.charge[1] = -4.0 / (s.n_mon - 1)
+    inp.charge[2] = 0.0
+    inp.charge[3] = 1.0
     inp.alpha_c, inp.n_kmax, inp.rc_coul = 0.81, 12, 3.0
     p, _ = md.derive(inp)
+    return p, (s, a_type, r0, v)
+
+
+def melt_brush_inputs(gamma=5.0, kT=1.0, dt=0.005, eps_bm=1.2, k_bend=2.0):
+    """abi.Inputs of the melt-in-brush model in the reference's switches: SOLVENT 3 (pairs cut at
+    2 * 2^(1/6) sigma, the reference's nearest cut-off to 2.5 sigma) with BRUSH_IN_GOOD_SV
+    (brush-brush WCA), eps = eps_bm between brush (heads included) and melt, eps = 1 otherwise,
+    cosine bending (BENDING and BENDING_MELT, bend_form 1) with k_b on every chain, DPD inside
+    each pair's LJ range, WALL 2.  The reference has no switch for a WCA melt next to an
+    attractive brush-melt pair, so the melt-melt pairs share the 2 * 2^(1/6) sigma range."""
+    inp = wca_inputs(gamma=gamma, kT=kT, dt=dt, bending=True, k_bend=k_bend)
+    f = inp.flags
+    f.solvent, f.brush_in_good_sv = 3, 1
+    f.bending, f.bending_melt, f.orientation = 1, 1, 0
+    inp.bend_form = 1
+    inp.delta_sig[0] = 1.0  # SOLVENT >= 2 takes the brush-liquid sigma from system_input
+    for b in (0, 1):
+        inp.epsil[b * abi.MAXT + 2] = inp.epsil[2 * abi.MAXT + b] = eps_bm
+    return inp
+
+
+def melt_brush(L=100.0, D=40.0, sigma_g=0.2, n_mon=50, n_mon_d=20, rho=0.85, seed=5, **kw):
+    """The large melt-in-brush channel: L x L x D, grafting density sigma_g per wall, brush chains
+    of n_mon beads, free melt chains of n_mon_d beads to total density rho (340,000 particles at
+    the defaults), lattice filled to 75 %.  Returns (mfa_params, (System, a_type, r0, v))."""
+    s, a_type, r0, v = brush_channel(L, D, sigma_g, n_mon, rho=rho, n_mon_d=n_mon_d, seed=seed, max_fill=0.75)
+    p, _ = md.derive(melt_brush_inputs(**kw))
     return p, (s, a_type, r0, v)
 
 

@@ -1039,6 +1039,13 @@ int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count) {
   return r;
 }
 
+int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (n_k) *n_k = ctx->kspace ? ctx->K.nk : 0;
+  if (n_charged) *n_charged = ctx->kspace ? ctx->K.nq : 0;
+  return MFA_OK;
+}
+
 int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
   if (!ctx) return MFA_ERR_ARG;
   if (nsteps <= 0) return MFA_OK;

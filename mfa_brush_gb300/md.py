@@ -245,6 +245,12 @@ class MdSystem:
         self._ck(self.lib.mfa_list_stats(self.ctx, C.byref(cap), C.byref(mx)))
         return cap.value, mx.value
 
+    def kspace_info(self):
+        """(k-vectors, charged particles) of the reciprocal-space sum; (0, 0) when uncharged."""
+        nk, nq = abi.i32(0), abi.i32(0)
+        self._ck(self.lib.mfa_kspace_info(self.ctx, C.byref(nk), C.byref(nq)))
+        return nk.value, nq.value
+
     def observe(self):
         """observation.f90 quantities of every replica: Rg^2 (brush, melt), momentum, head forces."""
         o = (abi.Observables * self.nrep)()

@@ -203,24 +203,30 @@ def test_charged_brush_full_size_stays_in_channel(gpu):
     assert np.isfinite(e["e_total"])
 
 
-def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod):
+@pytest.mark.parametrize("model", ["counterions", "uniform"])
+def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod, model):
     """The charged-brush case at its full size: 40 x 40 x 30 channel, grafting density 0.1, N = 40,
     slab Ewald with alpha = 0.9 (alpha_c = 0.81), real-space cut-off 3, |k| <= 12 (2 pi / L) with
-    the reference's k-set rule (8071 vectors), dipolar correction.  The line charge of "every
-    10th bead -1" is spread as -0.1 per brush bead, neutralised by the solvent.  Prints the
-    k-space energy and force errors of the FP64 and the mixed (Kahan-compensated FP32) paths
-    against the FP64 oracle; the mixed path must meet the 1e-5 force criterion."""
-    s, a_type, r0, v = configs.brush_channel(40.0, 30.0, 0.1, 40, rho=0.7, seed=41)
-    n_brush = int(np.sum(a_type == 2))
-    n_solv = int(np.sum(a_type == 3))
-    inp = configs.wca_inputs(gamma=1.0, thermostat=0)
-    inp.flags.system = 3
-    inp.charge[1] = -0.1
-    inp.charge[2] = 0.1 * n_brush / n_solv
-    inp.alpha_c = 0.81
-    inp.n_kmax = 12
-    inp.rc_coul = 3.0
-    p, _ = md.derive(inp)
+    the reference's k-set rule (8070 vectors), dipolar correction.  "counterions": the brush charge
+    -4 per chain spread over its beads, 1280 +1 counterions, neutral solvent (13,760 charged
+    particles; configs.charged_brush).  "uniform": -0.1 per brush bead neutralised by the whole
+    solvent (33,280 charged particles).  Prints the k-space energy and force errors of the FP64
+    and the mixed (Kahan-compensated FP32) paths against the FP64 oracle; the mixed path must
+    meet the 1e-5 force criterion."""
+    if model == "counterions":
+        p, (s, a_type, r0, v) = configs.charged_brush(gamma=1.0)
+    else:
+        s, a_type, r0, v = configs.brush_channel(40.0, 30.0, 0.1, 40, rho=0.7, seed=41)
+        n_brush = int(np.sum(a_type == 2))
+        n_solv = int(np.sum(a_type == 3))
+        inp = configs.wca_inputs(gamma=1.0, thermostat=0)
+        inp.flags.system = 3
+        inp.charge[1] = -0.1
+        inp.charge[2] = 0.1 * n_brush / n_solv
+        inp.alpha_c = 0.81
+        inp.n_kmax = 12
+        inp.rc_coul = 3.0
+        p, _ = md.derive(inp)
     o = oracle_mod.Oracle(p, s, a_type, r0, v)
     o.ewald_init()
     o.zero_force()
@@ -236,8 +242,8 @@ def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod):
         a, b = (np.linalg.norm(fk - fko, axis=1).max() / rms, None)
         out[precision] = (rel(uk, uko), a)
         g.close()
-    print("k-space vs FP64 oracle (N=%d, rel energy error, max|dF|/F_rms): fp64 %.2e %.2e  mixed %.2e %.2e"
-          % (s.n_mon_tot, *out["fp64"], *out["mixed"]))
+    print("k-space vs FP64 oracle (%s, N=%d, rel energy error, max|dF|/F_rms): fp64 %.2e %.2e  mixed %.2e %.2e"
+          % (model, s.n_mon_tot, *out["fp64"], *out["mixed"]))
     assert out["fp64"][0] < 1e-10 and out["fp64"][1] < 1e-9
     assert out["mixed"][0] < 1e-5 and out["mixed"][1] < 1e-5
 
