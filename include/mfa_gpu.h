@@ -176,6 +176,9 @@ typedef struct mfa_options {
   int32_t use_graphs;       /* capture mfa_step sequences as CUDA graphs (default 1)            */
   int32_t block_size;       /* threads per block of the pair kernel, 0 = built-in choice        */
   int32_t profile_from_step;/* mfa_step accumulates z-profiles for steps > this (n_relax)       */
+  int32_t kspace_plain_sums;/* 1: mixed-precision k-space sums in plain FP32, without the Kahan
+                               compensation across particle tiles and k rows (a precision study;
+                               default 0)                                                       */
 } mfa_options;
 
 typedef struct mfa_energies {

@@ -248,6 +248,7 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   K.inv_V = (1. / L[0]) * (1. / L[1]) / (L[2] * (1. + z_slab));
   K.lz_half = L[2] / 2.;
   K.rep = 0;
+  K.plain = ctx->opt.kspace_plain_sums ? 1 : 0;
   std::vector<int> qt;
   std::vector<double> qv;
   for (int t = 0; t < s.n_mon_tot; ++t)

@@ -38,10 +38,15 @@ __device__ __forceinline__ void cmul(double2 a, double2 b, double2& c) {
   c = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// s += y: Kahan-compensated in FP32 (c carries the negated lost low part), plain in FP64
+// s += y: Kahan-compensated in FP32 (c carries the negated lost low part) unless `plain` (the
+// precision study of mfa_options.kspace_plain_sums), plain in FP64
 template <bool MIXED>
-__device__ __forceinline__ void ksum(kreal<MIXED>& s, kreal<MIXED>& c, kreal<MIXED> y) {
+__device__ __forceinline__ void ksum(kreal<MIXED>& s, kreal<MIXED>& c, kreal<MIXED> y, bool plain = false) {
   if constexpr (MIXED) {
+    if (plain) {
+      s += y;
+      return;
+    }
     const float z = y - c;
     const float t = s + z;
     c = (t - s) - z;
@@ -193,8 +198,8 @@ __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
       }
 #pragma unroll
       for (int i = 0; i < KS_RW; ++i) {
-        ksum<MIXED>(sr[i], cr[i], tr[i]);
-        ksum<MIXED>(si[i], ci[i], ti[i]);
+        ksum<MIXED>(sr[i], cr[i], tr[i], K.plain);
+        ksum<MIXED>(si[i], ci[i], ti[i], K.plain);
       }
     }
   }
@@ -382,9 +387,9 @@ __global__ void __launch_bounds__(KS_FB) k_ks_force(KSpace K) {
       srow += sg;
     }
     const real2 w = ryz[r];
-    ksum<MIXED>(fx, cx, sxrow);
-    ksum<MIXED>(fy, cy, w.x * srow);
-    ksum<MIXED>(fz, cz, w.y * srow);
+    ksum<MIXED>(fx, cx, sxrow, K.plain);
+    ksum<MIXED>(fy, cy, w.x * srow, K.plain);
+    ksum<MIXED>(fz, cz, w.y * srow, K.plain);
     R = Rn;
     Y = Yn;
     Z = Zn;
@@ -466,9 +471,9 @@ __global__ void __launch_bounds__(KS_FB) k_ks_force_dense(KSpace K) {
     const float srow = YZ.x * s_im - YZ.y * s_re;
     const float sxrow = YZ.x * x_im - YZ.y * x_re;
     const float2 kyz = ryz[r];
-    ksum<true>(fx, cx, sxrow);
-    ksum<true>(fy, cy, kyz.x * srow);
-    ksum<true>(fz, cz, kyz.y * srow);
+    ksum<true>(fx, cx, sxrow, K.plain);
+    ksum<true>(fy, cy, kyz.x * srow, K.plain);
+    ksum<true>(fz, cz, kyz.y * srow, K.plain);
     R = Rn;
     Y = Yn;
     Z = Zn;

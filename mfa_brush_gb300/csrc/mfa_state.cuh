@@ -132,6 +132,7 @@ struct KSpace {
   double* red_part;     // [2*KS_RED_MAX]: rho_sum energy, dipole moment
   unsigned* ticket;     // [2] zero between launches
   int rep;
+  int plain;            // 1: FP32 sums without Kahan compensation (mfa_options.kspace_plain_sums)
 };
 constexpr int KS_FB = 128;       // particles per force block
 constexpr int KS_FR = 32;        // rows per force chunk

@@ -68,7 +68,7 @@ def read_deck(deck_dir, conf="conf_old"):
 
 
 def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, device=0, nbr_capacity=0,
-            profile_from_step=0, block_size=0):
+            profile_from_step=0, block_size=0, kspace_plain_sums=False):
     o = abi.Options()
     _lib().mfa_default_options(C.byref(o))
     o.precision = abi.PREC_MIXED if precision in ("mixed", abi.PREC_MIXED) else abi.PREC_FP64
@@ -79,6 +79,7 @@ def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, devic
     o.nbr_capacity = nbr_capacity
     o.profile_from_step = profile_from_step
     o.block_size = block_size
+    o.kspace_plain_sums = 1 if kspace_plain_sums else 0
     return o
 
 

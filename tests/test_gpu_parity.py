@@ -287,6 +287,22 @@ def test_deterministic_and_momentum(gpu):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ewald_wide_kset_matches_oracle(gpu, oracle_mod, precision):
+    """n_kmax = 17: nx runs over -17..17, so the structure factor takes two 32-slot groups of
+    k_ks_rho and the mixed force takes the one-k-at-a-time kernel instead of the register-resident
+    slot table (which holds nxm <= 15)."""
+    p, s, a_type, r0, v = charged_system(n_kmax=17)
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, None, precision)
+    o.ewald_init()
+    nk, nq = g.kspace_info()
+    assert nk == o.n_kvec() and nk > 20000 and nq > 0
+    g.zero_force(); uk = g.ewald_k()[0]; fk = g.state()[3]
+    o.zero_force(); uko = o.ewald_k(); fko = o.state()[3]
+    assert rel(uk, uko) < (1e-10 if precision == "fp64" else 1e-5)
+    assert_force_parity(fk, fko, precision)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_charged_run_deterministic(gpu, precision):
     """A charged system (slab Ewald + dipolar correction) run twice gives bit-identical states and
     energies: every k-space sum (rho over particle chunks, U over blocks, forces over k-chunks,
