@@ -221,26 +221,36 @@ __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
   }
 }
 
+// Block sum of v (all threads, warps in order); the same value in every thread.
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double b = 0.;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
+  return b;
+}
+
 // Block sum of v (all threads), then the last block of the grid to finish adds the per-block
-// partials in block order; returns true in thread 0 of that block, with the total in `total`.
+// partials: each of its threads a strided subset in order, then a block sum; a fixed order for
+// a given grid.  Returns true in thread 0 of that block, with the total in `total`.
 __device__ __forceinline__ bool grid_sum_last(double v, double* part, unsigned* ticket, double& total) {
   __shared__ double red[32];
   __shared__ bool last;
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
+  const double b = block_sum(v, red);
   if (threadIdx.x == 0) {
-    double b = 0.;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += red[w];
     part[blockIdx.x] = b;
     __threadfence();
     last = atomicAdd(ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return false;
+  if (!last) return false;
   __threadfence();
   double t = 0.;
-  for (unsigned b = 0; b < gridDim.x; ++b) t += ((volatile double*)part)[b];
+  for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) t += ((volatile double*)part)[k];
+  t = block_sum(t, red);
+  if (threadIdx.x != 0) return false;
   total = t;
   *ticket = 0u;  // ready for the next launch
   return true;
