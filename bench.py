@@ -268,7 +268,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
     ap.add_argument("--skin", default="auto",
-                    help="list skin in sigma, or 'auto': timed on 32 of the replicas at 0.4-0.7")
+                    help="list skin in sigma, or 'auto': the whole set timed at 0.5-0.9")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
@@ -307,9 +307,11 @@ def main():
     tuned = None
     if args.skin == "auto":
         from mfa_brush_gb300 import tune
-        best, rates = tune.tune_skin(p, reps, precision=args.precision, device=local)
+        # every replica of this rank: the rebuild rate depends on the size of the batch
+        best, rates = tune.tune_skin(p, reps, n_sample=len(reps), steps=100, precision=args.precision,
+                                     device=local)
         tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
-                 "unit": "G atom-steps/s on 32 replicas"}
+                 "unit": "G atom-steps/s on the %d replicas of this GPU, 100 steps each" % len(reps)}
         args.skin = best
     args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin)
@@ -379,6 +381,8 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": profiled_traffic(args.precision, n_atoms),
                          "kernel": "k_pair (%s)" % args.precision,
+                         "traffic_source": "ncu DRAM bytes per particle of one full launch at skin 0.6 "
+                                           "(profiles/k_pair_%s_brush_replicas.md), times N" % args.precision,
                          "peak_kind": peak_kind},
             "clocks": clocks}
     if e2e is not None:
