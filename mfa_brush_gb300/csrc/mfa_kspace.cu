@@ -8,15 +8,20 @@
 //   k_ks_tables:  per charged particle, X(nx) = exp(i nx dkx x), Y(ny), Z(nz) for n >= 0, each
 //                 from an FP64 phase reduced to [-1/2, 1/2) turns (sincospi); stored column-major
 //                 ([column][particle]) so that a warp reads 32 particles of one column at once;
-//   k_ks_rho:     thread per k-vector, tiles of 32 particles in shared memory holding X(+-nx) and
-//                 A = q Y Z for the rows the block spans: one complex product per (k, particle),
-//                 plain sums over a tile and Kahan-compensated sums across tiles in FP32 (MIXED),
-//                 or FP64 sums; one partial per particle chunk;
-//   k_ks_rho_sum: the partials of each k summed in a fixed order, G Re rho and G Im rho for the
-//                 force, and U reduced deterministically (per-block partials, the last block sums);
-//   k_ks_force:   thread per particle, a chunk of whole rows per block: per row Y Z once, per k
-//                 one complex product; per row sum_k kx s_k and ky, kz times sum_k s_k, rows
-//                 added with Kahan compensation (MIXED);
+//   k_ks_rho:     rho(row, nx) = sum_p (q Y Z)(p, row) X(p, nx) as a complex matrix product per
+//                 block of 64 rows x 32 nx slots x a particle chunk: lane = slot, warp = 8 rows,
+//                 tiles of 32 particles in shared memory; plain sums over a tile and Kahan-
+//                 compensated sums across tiles in FP32 (MIXED), or FP64 sums; one partial per
+//                 particle chunk;
+//   k_ks_rho_sum: the partials of each k summed in a fixed order; G rho per k and the dense
+//                 (row, slot) table of (G rho, kx G rho) for the force; U reduced
+//                 deterministically (per-block partials, the last block adds them);
+//   k_ks_force_dense (mixed, nxm <= 15): thread per particle with X(-nxm..nxm) in registers, a
+//                 chunk of 32 rows per block streamed from the dense table: per row
+//                 S = sum conj(X) G rho and S_x = sum conj(X) kx G rho, then Im(conj(Y Z) S_x)
+//                 to F_x and ky, kz times Im(conj(Y Z) S) to F_y, F_z; rows added with Kahan
+//                 compensation;
+//   k_ks_force:   the same per row, one k at a time from shared memory (FP64, or nxm > 15);
 //   k_ks_force_sum: the chunk partials in a fixed order, times -8 pi q / V, into the force array.
 // dipolar_correction.f90:20-33 (Yeh-Berkowitz slab term) is k_ks_dipole + k_ks_dipole_force, FP64.
 // Every sum has a fixed order, so a charged run is reproducible bit for bit.
