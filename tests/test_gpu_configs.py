@@ -183,11 +183,12 @@ def test_charged_nve_energy_excursion_within_3x_fp64_oracle(gpu, oracle_mod):
 
 
 def test_charged_brush_full_size_stays_in_channel(gpu):
-    """The full-size charged brush (33,600 particles, 8070 k-vectors) for 300 fused mixed steps
-    under the DPD thermostat: every particle stays in the channel and the energies stay finite.
-    The lattice start releases heat that the DPD thermostat, acting inside the WCA range only,
-    removes over ~10^3 steps: the FP64 oracle on the same start (without the weak charges) has
-    <v^2> = 2.05 per component at step 300, and the charged run must be close to that."""
+    """The full-size charged brush (33,600 particles, 1280 counterions, 8070 k-vectors) for 300
+    fused mixed steps under the DPD thermostat: every particle stays in the channel and the
+    energies stay finite.  The lattice start releases heat that the DPD thermostat, acting inside
+    the WCA range only, removes over ~10^3 steps: the FP64 oracle on the same system and noise
+    (300 oracle steps take ~25 minutes on 8 cores, so the value is written here) has <v^2> = 2.054 per component at
+    step 300, and the mixed run must agree within 0.06."""
     p, (s, a_type, r0, v) = configs.charged_brush()
     g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
     g.step(300)
@@ -199,7 +200,7 @@ def test_charged_brush_full_size_stays_in_channel(gpu):
     mob = a_type != 1
     t_kin = np.mean(vv[mob] ** 2)
     print("charged brush after 300 steps: <v^2> per component %.3f, e_total %.1f" % (t_kin, e["e_total"]))
-    assert 1.8 < t_kin < 2.3
+    assert abs(t_kin - 2.054) < 0.06
     assert np.isfinite(e["e_total"])
 
 
