@@ -186,9 +186,9 @@ def test_charged_brush_full_size_stays_in_channel(gpu):
     """The full-size charged brush (33,600 particles, 1280 counterions, 8070 k-vectors) for 300
     fused mixed steps under the DPD thermostat: every particle stays in the channel and the
     energies stay finite.  The lattice start releases heat that the DPD thermostat, acting inside
-    the WCA range only, removes over ~10^3 steps: the FP64 oracle on the same system and noise
-    (300 oracle steps take ~25 minutes on 8 cores, so the value is written here) has <v^2> = 2.054 per component at
-    step 300, and the mixed run must agree within 0.06."""
+    the WCA range only, removes over ~10^3 steps.  The FP64 oracle on the same system and noise
+    has <v^2> = 2.054 per component at step 300 (its 300 steps take ~25 minutes on 8 cores, so
+    the value is written here); the mixed run must agree within 0.06."""
     p, (s, a_type, r0, v) = configs.charged_brush()
     g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
     g.step(300)
