@@ -30,6 +30,7 @@ def test_abi_struct_sizes_match_header(lib):
     o = abi.Options()
     lib.mfa_default_options(C.byref(o))
     assert (o.precision, o.skin, o.energy_every, o.use_graphs) == (abi.PREC_MIXED, 0.3, 10, 1)
+    assert (o.profile_from_step, o.kspace_plain_sums) == (0, 0)
 
 
 def test_header_flags(try_dir):
@@ -122,3 +123,48 @@ def test_skin_tuner_sample_spans_the_set():
     s = tune.sample_replicas(reps, 32)
     assert len(s) == 32 and s[0] == 0 and s[-1] == 255 and s == sorted(s)
     assert tune.sample_replicas(reps[:5], 32) == reps[:5]
+
+
+def _range_table(p):
+    from mfa_brush_gb300 import abi
+    return np.array([[p.range_2[i * abi.MAXT + j] for j in range(p.n_type)] for i in range(p.n_type)])
+
+
+def test_charged_brush_configuration(lib):
+    """configs.charged_brush: neutral; -4 per chain spread over the 39 non-head beads; 1280 +1
+    counterions stored last as the fourth species; every pair WCA (heads among themselves off);
+    slab Ewald switches."""
+    from mfa_brush_gb300 import configs
+    p, (s, a_type, r0, v) = configs.charged_brush()
+    q = np.array([p.charge[t - 1] for t in a_type])
+    assert s.n_part == 33600 and abs(q.sum()) < 1e-9
+    assert np.count_nonzero(q) == 13760 and np.count_nonzero(q > 0) == 1280
+    assert s.n_chain_e == 1280 and s.n_mon_e == 1 and np.all(a_type[-1280:] == 4)
+    assert np.all(a_type[s.n_mon * s.n_chain: s.n_part - 1280] == 3)
+    wca = (2.0 ** (1.0 / 6.0)) ** 2
+    rt = _range_table(p)
+    assert rt[0, 0] == 0.0 and np.allclose(rt.ravel()[1:], wca, rtol=1e-6)
+    assert p.flags.system == 3 and p.flags.particle_4 == 1 and abs(p.alpha_c - 0.81) < 1e-15
+    assert abs(p.rc_coul_2 - 9.0) < 1e-12 and p.n_kmax == 12
+
+
+def test_melt_brush_tables_and_generation(lib):
+    """configs.melt_brush: brush-melt and melt-melt cut at 2 * 2^(1/6) sigma with eps_bm = 1.2
+    (x4 in the tables), brush-brush WCA, cosine bending on both chain kinds; a reduced box
+    builds with every bond inside the FENE range."""
+    from mfa_brush_gb300 import abi, configs
+    p, (s, a_type, r0, v) = configs.melt_brush(L=20.0)
+    c6 = 2.0 ** (1.0 / 6.0)
+    rt = _range_table(p)
+    assert np.isclose(rt[1, 1], c6 ** 2) and np.isclose(rt[0, 1], c6 ** 2)
+    assert np.isclose(rt[1, 2], (2 * c6) ** 2) and np.isclose(rt[2, 2], (2 * c6) ** 2)
+    assert np.isclose(p.epsil[1 * abi.MAXT + 2], 4.8) and np.isclose(p.epsil[2 * abi.MAXT + 2], 4.0)
+    assert p.flags.bending == 1 and p.flags.bending_melt == 1 and p.bend_form == 1 and p.k_bend == 2.0
+    assert s.n_mon_d == 20 and s.n_chain_d > 0 and abs(s.n_part - 0.85 * 20 * 20 * 40) <= 20
+    L = s.boundary[0]
+    for n0, n_mon, n_ch in ((0, s.n_mon, s.n_chain), (s.n_mon * s.n_chain, s.n_mon_d, s.n_chain_d)):
+        c = r0[n0: n0 + n_mon * n_ch].reshape(n_ch, n_mon, 3)
+        d = np.diff(c, axis=1)
+        d[..., :2] -= L * np.round(d[..., :2] / L)
+        assert np.linalg.norm(d, axis=2).max() < 1.5
+
