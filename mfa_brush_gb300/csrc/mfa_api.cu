@@ -269,15 +269,23 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   K.nrows = (int)rows.size();
   // slots of a row: nx = -nxm .. -nxm + 4 qx - 1 (the dense slot table of the force kernel)
   K.qx = (2 * nx + 1 + 3) / 4;
-  // force chunks: KS_FR whole rows
+  // force chunks of whole rows: KS_FR for the dense kernel; for the one-k-at-a-time kernel as
+  // many as let its shared-memory tables fit (the X table alone grows with nxm)
+  const bool dense = kspace_dense(K, ctx->S.mixed);
   std::vector<int> chunk_row;
-  for (int r = 0; r < K.nrows; r += KS_FR) chunk_row.push_back(r);
-  chunk_row.push_back(K.nrows);
-  K.nkchunks = (int)chunk_row.size() - 1;
-  K.fchunk_k_max = K.fchunk_rows_max = 1;
-  for (int c = 0; c < K.nkchunks; ++c) {
-    K.fchunk_k_max = std::max(K.fchunk_k_max, rows[chunk_row[c + 1] - 1].y - rows[chunk_row[c]].x);
-    K.fchunk_rows_max = std::max(K.fchunk_rows_max, chunk_row[c + 1] - chunk_row[c]);
+  for (int frows = KS_FR;; frows /= 2) {
+    chunk_row.clear();
+    for (int r = 0; r < K.nrows; r += frows) chunk_row.push_back(r);
+    chunk_row.push_back(K.nrows);
+    K.nkchunks = (int)chunk_row.size() - 1;
+    K.fchunk_k_max = K.fchunk_rows_max = 1;
+    for (int c = 0; c < K.nkchunks; ++c) {
+      K.fchunk_k_max = std::max(K.fchunk_k_max, rows[chunk_row[c + 1] - 1].y - rows[chunk_row[c]].x);
+      K.fchunk_rows_max = std::max(K.fchunk_rows_max, chunk_row[c + 1] - chunk_row[c]);
+    }
+    if (dense || kspace_force_smem(K, ctx->S.mixed) <= KS_SMEM_MAX) break;
+    if (frows == 1)
+      return fail(ctx, MFA_ERR_CAPACITY, "ewald_k: the k-set is too wide in x for the force kernel's tables");
   }
   // force order of the rows (dense kernel): by slot range, widest first, so that the KS_FR rows
   // of a chunk share a narrow window of slots

@@ -548,17 +548,20 @@ const dense_launcher kDense[KS_DENSE_QX_MAX + 1] = {nullptr,          launch_den
 bool use_dense(const KSpace& K, bool mixed) { return mixed && K.qx <= KS_DENSE_QX_MAX; }
 }  // namespace
 
+bool kspace_dense(const KSpace& K, bool mixed) { return use_dense(K, mixed); }
+size_t kspace_force_smem(const KSpace& K, bool mixed) { return force_smem(K, mixed); }
+
 int kspace_prepare(const KSpace& K, bool mixed) {
-  const size_t a = rho_smem(K, mixed), b = force_smem(K, mixed);
-  if (a > 227 * 1024 || b > 227 * 1024) return (int)cudaErrorInvalidConfiguration;
-  cudaError_t e;
-  if (mixed) {
-    e = cudaFuncSetAttribute(k_ks_rho<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
-  } else {
-    e = cudaFuncSetAttribute(k_ks_rho<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
-  }
+  const size_t a = rho_smem(K, mixed), b = use_dense(K, mixed) ? dense_smem(K) : force_smem(K, mixed);
+  if (a > KS_SMEM_MAX || b > KS_SMEM_MAX) return (int)cudaErrorInvalidConfiguration;
+  // The opt-in is a property of the kernel for the whole process, not of a context: set it to the
+  // largest allowed size once, so that no context lowers it below another's needs (occupancy
+  // follows the size of each launch, not this limit).
+  const int mx = (int)KS_SMEM_MAX;
+  cudaError_t e = cudaFuncSetAttribute(k_ks_rho<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_rho<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   return (int)e;  // dense_smem stays below 48 KB: 32 rows x 32 slots x 16 B + 512 B
 }
 

@@ -137,6 +137,11 @@ struct KSpace {
 constexpr int KS_FB = 128;       // particles per force block
 constexpr int KS_FR = 32;        // rows per force chunk
 constexpr int KS_RED_MAX = 256;  // blocks of a grid reduction, at most
+constexpr size_t KS_SMEM_MAX = 227 * 1024;  // dynamic shared memory of one block, at most
+// the dense force kernel (X in registers) serves mixed precision with nxm <= 15
+bool kspace_dense(const KSpace& K, bool mixed);
+// shared memory of the one-k-at-a-time force kernel for the chunks set in K
+size_t kspace_force_smem(const KSpace& K, bool mixed);
 // host-side preparation of the kernels (shared-memory opt-in); returns a CUDA error
 int kspace_prepare(const KSpace& K, bool mixed);
 // fused: the mixed-precision fused step adds into the FP32 force array, otherwise into FP64

@@ -301,6 +301,38 @@ def test_ewald_wide_kset_matches_oracle(gpu, oracle_mod, precision):
     assert_force_parity(fk, fko, precision)
 
 
+def test_ewald_very_wide_kset_fp64_smaller_force_chunks(gpu, oracle_mod):
+    """n_kmax = 40 in FP64: the one-k-at-a-time force kernel's X table (81 slots x 128 particles x
+    16 B) leaves no room for 32-row chunks, so the context takes fewer rows per chunk; the sum
+    still matches the oracle."""
+    p, s, a_type, r0, v = charged_system(n_kmax=40)
+    g, o = gpu_and_oracle(oracle_mod, p, s, a_type, r0, v, None, "fp64")
+    nk, _ = g.kspace_info()
+    assert nk == len(o.kvecs())
+    g.zero_force(); uk = g.ewald_k()[0]; fk = g.state()[3]
+    o.zero_force(); uko = o.ewald_k(); fko = o.state()[3]
+    assert rel(uk, uko) < 1e-10
+    assert_force_parity(fk, fko, "fp64")
+
+
+def test_ewald_contexts_with_different_tables_coexist(gpu, oracle_mod):
+    """A context whose force kernel needs more shared memory (n_kmax = 17, mixed: the one-k-at-a-
+    time kernel) keeps working after a second context with small tables (n_kmax = 5) is made."""
+    p17, s, a_type, r0, v = charged_system(n_kmax=17)
+    p5, _, _, _, _ = charged_system(n_kmax=5)
+    g17 = md.MdSystem(p17, s, a_type, r0, v, precision="mixed")
+    g5 = md.MdSystem(p5, s, a_type, r0, v, precision="mixed")
+    o = oracle_mod.Oracle(p17, s, a_type, r0, v)
+    o.ewald_init()
+    g5.zero_force(); g5.ewald_k()
+    g17.zero_force(); uk = g17.ewald_k()[0]; fk = g17.state()[3]
+    o.zero_force(); uko = o.ewald_k(); fko = o.state()[3]
+    assert rel(uk, uko) < 1e-5
+    assert_force_parity(fk, fko, "mixed")
+    g5.close()
+    g17.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_charged_run_deterministic(gpu, precision):
     """A charged system (slab Ewald + dipolar correction) run twice gives bit-identical states and
