@@ -388,7 +388,8 @@ def main():
     if e2e is not None:
         line["e2e"] = e2e
     if rank == 0 and not args.no_fp64:
-        # spec comparison: the same kind of replicas advanced one at a time in plain FP64
+        # the reference point of the batched mixed step: the same kind of replicas advanced one at
+        # a time in plain FP64
         fv, fk, fn = plain_fp64(reps, p, args.skin, local)
         line["plain_fp64_one_at_a_time"] = {
             "value": fv, "unit": UNIT, "replicas": fk, "particles": int(fn), "steps": 100,
