@@ -182,6 +182,60 @@ def test_charged_nve_energy_excursion_within_3x_fp64_oracle(gpu, oracle_mod):
     assert dg <= 3.0 * max(do, 1e-5 * abs(eo[0]))
 
 
+def test_dpd_statistics_match_oracle(gpu, oracle_mod):
+    """With the DPD noise on, the fused mixed step and the FP64 oracle sample the same process
+    (same Philox stream, same start; the trajectories part after a few hundred steps).  Over 4000
+    steps after 1500 of equilibration (WCA channel, DPD with its own 1.5 sigma cut-off, kT = 1),
+    sampled every 100 steps: kinetic temperature, velocity kurtosis (3 for a Maxwell
+    distribution), brush height (mean distance of the brush beads from their own wall) and the
+    solvent z-profile agree within their statistical errors."""
+    inp = configs.wca_inputs(gamma=5.0, kT=1.0, dt=0.005)
+    inp.flags.dpd_cut_off = 1.5  # DPD_CUT_OFF
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(10.0, 10.0, 0.15, 12, rho=0.7, seed=13)
+    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    threads = max(1, os.cpu_count() or 1)
+    nb, D = s.n_mon * s.n_chain, s.boundary[2]
+    mob = a_type != 1
+    bottom = np.zeros(s.n_part, bool)
+    bottom[: (s.n_chain // 2) * s.n_mon] = True  # the first half of the chains hang from z = 0
+    brush = a_type == 2
+
+    def sample(r, vv):
+        vm = vv[mob]
+        t = np.mean(vm ** 2)
+        k4 = np.mean(vm ** 4) / t ** 2
+        h = np.mean(np.where(bottom[brush], r[brush, 2], D - r[brush, 2]))
+        prof = np.histogram(r[nb:, 2], bins=10, range=(0.0, D))[0].astype(float)
+        return t, k4, h, prof
+
+    g.step(1500)
+    o.step(1500, threads, 0)
+    sg, so = [], []
+    for _ in range(60):
+        g.step(100)
+        o.step(100, threads, 0)
+        sg.append(sample(*g.state()[:2]))
+        so.append(sample(*o.state()[:2]))
+
+    def stat(samples, k):
+        x = np.array([q[k] for q in samples])
+        return x.mean(axis=0), x.std(axis=0) / np.sqrt(len(x) / 4.0)  # blocks of 4 samples as independent
+
+    (tg, etg), (to, eto) = stat(sg, 0), stat(so, 0)
+    (kg, _), (ko, _) = stat(sg, 1), stat(so, 1)
+    (hg, ehg), (ho, eho) = stat(sg, 2), stat(so, 2)
+    (pg, _), (po, _) = stat(sg, 3), stat(so, 3)
+    print("DPD statistics, mixed vs FP64 oracle: <v^2> %.4f / %.4f  kurtosis %.3f / %.3f  brush height "
+          "%.3f / %.3f  profile L1 %.3f" % (tg, to, kg, ko, hg, ho, np.abs(pg - po).sum() / po.sum()))
+    assert abs(tg - 1.0) < 0.05 and abs(to - 1.0) < 0.05
+    assert abs(tg - to) < 4 * np.hypot(etg, eto) + 0.01
+    assert abs(kg - 3.0) < 0.1 and abs(ko - 3.0) < 0.1
+    assert abs(hg - ho) < max(4 * np.hypot(ehg, eho), 0.03 * ho)
+    assert np.abs(pg - po).sum() / po.sum() < 0.06
+
+
 def test_charged_brush_full_size_stays_in_channel(gpu):
     """The full-size charged brush (33,600 particles, 1280 counterions, 8070 k-vectors) for 300
     fused mixed steps under the DPD thermostat: every particle stays in the channel and the
