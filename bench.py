@@ -267,6 +267,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--kernel-steps", type=int, default=20)
+    ap.add_argument("--block", type=int, default=128,
+                    help="threads per block of the pair kernel (32, 64, 128); tuned with --skin auto")
     ap.add_argument("--skin", default="auto",
                     help="list skin in sigma, or 'auto': the whole set timed at 0.5-0.9")
     args = ap.parse_args()
@@ -310,11 +312,17 @@ def main():
         # every replica of this rank: the rebuild rate depends on the size of the batch
         best, rates = tune.tune_skin(p, reps, n_sample=len(reps), steps=100, precision=args.precision,
                                      device=local)
+        blk, brates = tune.tune_block(p, reps, best, n_sample=len(reps), steps=100, precision=args.precision,
+                                      device=local)
         tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
+                 "block_candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in brates.items()},
+                 "block_size": blk,
                  "unit": "G atom-steps/s on the %d replicas of this GPU, 100 steps each" % len(reps)}
         args.skin = best
+        args.block = blk
     args.skin = float(args.skin)
-    g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin)
+    g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin,
+                    block_size=args.block)
 
     def barrier():
         if dist is not None:
@@ -372,6 +380,7 @@ def main():
                        "replicas": args.replicas * world, "particles_per_gpu": n_atoms,
                        "particles_total": n_all, "seed": args.seed,
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
+                       "pair_block": args.block,
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},

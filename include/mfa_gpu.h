@@ -174,7 +174,8 @@ typedef struct mfa_options {
   int32_t nbr_capacity;     /* neighbours per particle; 0 = estimate from density and cut-off  */
   int32_t energy_every;     /* steps between energy reductions in mfa_step (10, as fort.60)     */
   int32_t use_graphs;       /* capture mfa_step sequences as CUDA graphs (default 1)            */
-  int32_t block_size;       /* threads per block of the pair kernel, 0 = built-in choice        */
+  int32_t block_size;       /* threads per block of the pair kernel: 32, 64 or 128; other
+                               values (0) take the built-in 128                                 */
   int32_t profile_from_step;/* mfa_step accumulates z-profiles for steps > this (n_relax)       */
   int32_t kspace_plain_sums;/* 1: mixed-precision k-space sums in plain FP32, without the Kahan
                                compensation across particle tiles and k rows (a precision study;

@@ -529,9 +529,10 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
 
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag, Acc acc,
                  int block, int bonded_mask) {
-  (void)block;
-  int B = 128;
-  int g = (s.N + B - 1) / B;
+  // 32, 64 or 128 threads per block (the kernel is compiled for at most 128); anything else
+  // takes the built-in 128
+  const int B = (block == 32 || block == 64) ? block : 128;
+  const int g = (s.N + B - 1) / B;
   const bool uni = C.scr2_uni_f > 0.f;
   if (s.mixed && !accumulate && bonded_mask) {
     if (uni) {

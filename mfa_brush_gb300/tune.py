@@ -1,4 +1,4 @@
-"""Autotuning of the neighbour-list skin.
+"""Autotuning of the neighbour-list skin and of the pair kernel's block size.
 
 The skin trades the list rebuild (sort + list build, whose frequency falls as the skin grows) for
 the pair kernel (whose lists lengthen with it).  The best value depends on the density, the
@@ -40,5 +40,30 @@ def tune_skin(params, reps, candidates=(0.5, 0.6, 0.7, 0.8, 0.9), n_sample=32, s
         ms = g.event_elapsed(0, 1)
         g.close()
         rates[float(skin)] = n_atoms * max(1, steps // chunk) * chunk / (ms / 1000.0)
+    best = max(rates, key=rates.get)
+    return best, rates
+
+
+def tune_block(params, reps, skin, candidates=(64, 128), n_sample=32, steps=80, warmup=20,
+               precision="mixed", device=0, chunk=10):
+    """Times mfa_step at the given skin with each candidate pair-kernel block size (threads per
+    block); returns (best block size, {block: atom-steps/s})."""
+    sample = sample_replicas(reps, n_sample)
+    systems, a_type, r0, v = configs.concat(sample)
+    n_atoms = int(sum(s.n_part for s in systems))
+    rates = {}
+    for b in candidates:
+        g = md.MdSystem(params, systems, a_type, r0, v, precision=precision, device=device, skin=skin,
+                        block_size=b)
+        for _ in range(max(1, warmup // chunk)):
+            g.step(chunk)
+        g.synchronize()
+        g.event_record(0)
+        for _ in range(max(1, steps // chunk)):
+            g.step(chunk)
+        g.event_record(1)
+        ms = g.event_elapsed(0, 1)
+        g.close()
+        rates[int(b)] = n_atoms * max(1, steps // chunk) * chunk / (ms / 1000.0)
     best = max(rates, key=rates.get)
     return best, rates

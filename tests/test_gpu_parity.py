@@ -353,6 +353,23 @@ def test_charged_run_deterministic(gpu, precision):
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("block", [32, 64])
+def test_pair_block_size_does_not_change_the_trajectory(gpu, block):
+    """The pair kernel's block size (mfa_options.block_size, picked by the tuner) changes only the
+    grouping of threads: each particle's force sums its list in the same order, so 20 fused steps
+    give the same state bit for bit as the built-in 128 threads."""
+    p = configs.wca_params(gamma=5.0)
+    systems, a_type, r0, v = configs.concat(configs.replicas(4, seed=9))
+    out = []
+    for b in (128, block):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", block_size=b)
+        g.step(20)
+        out.append(g.state())
+        g.close()
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
+
+
 def test_state_round_trip_pinned_and_pageable(gpu):
     """mfa_set_state reads page-locked arrays directly and pageable ones through the staging
     buffer; mfa_sync_to_host fills both kinds alike.  Both give the same state, and a round trip
