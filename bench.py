@@ -429,6 +429,10 @@ def main():
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "%d replicas, %d particles, 40 steps (restated reference "
                                           "OpenMP path)" % (len(sample), n)}
+        # the same path on one thread, on the first replica only (a few seconds)
+        c1, _, _ = cpu_sample(sample[:1], p, 20, 2, 1)
+        line["cpu_baseline_1thread"] = {"value": c1, "unit": UNIT, "cores": 1, "kind": "port",
+                                        "sample": "1 replica, %d particles, 20 steps" % sample[0][0].n_part}
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
