@@ -39,17 +39,26 @@ CHUNK = 10
 PAIR_BYTES = {"mixed": 16 + 16 + 16, "fp64": 32 + 32 + 24}
 
 
-def profiled_traffic(precision, n_atoms):
+def profiled_traffic(precision, n_atoms, skin):
     """DRAM bytes of one pair-kernel launch, scaled to n_atoms from the committed ncu summary
-    (`traffic_bytes_per_particle:` line of profiles/k_pair_<precision>_brush_replicas.md)."""
+    (profiles/k_pair_<precision>_brush_replicas.md): the `traffic_bytes_per_particle_skin_S:`
+    line of the profiled skin nearest to `skin`, else `traffic_bytes_per_particle:`.
+    Returns (bytes, the skin of the profile or None)."""
+    per_skin, default = {}, None
     try:
         with open(os.path.join(ROOT, "profiles", "k_pair_%s_brush_replicas.md" % precision)) as f:
             for ln in f:
-                if ln.startswith("traffic_bytes_per_particle:"):
-                    return float(ln.split(":")[1]) * n_atoms
+                if ln.startswith("traffic_bytes_per_particle_skin_"):
+                    k, val = ln.split(":")
+                    per_skin[float(k.rsplit("_", 1)[1])] = float(val)
+                elif ln.startswith("traffic_bytes_per_particle:"):
+                    default = float(ln.split(":")[1])
     except OSError:
-        pass
-    return None
+        return None, None
+    if per_skin:
+        sk = min(per_skin, key=lambda x: abs(x - skin))
+        return per_skin[sk] * n_atoms, sk
+    return (default * n_atoms if default is not None else None), None
 
 
 def peaks():
@@ -364,6 +373,7 @@ def main():
     hbm, peak_kind = peaks()
     t_pair = kt["pair"][0] / 1000.0
     achieved = PAIR_BYTES[args.precision] * n_atoms / t_pair / 1e9 if t_pair > 0 else 0.0
+    traffic, traffic_skin = profiled_traffic(args.precision, n_atoms, args.skin)
 
     # end-to-end through the C ABI with pinned host buffers
     e2e = None
@@ -388,10 +398,11 @@ def main():
             "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": profiled_traffic(args.precision, n_atoms),
+                         "frac": achieved / hbm, "traffic": traffic,
                          "kernel": "k_pair (%s)" % args.precision,
-                         "traffic_source": "ncu DRAM bytes per particle of one full launch at skin 0.6 "
-                                           "(profiles/k_pair_%s_brush_replicas.md), times N" % args.precision,
+                         "traffic_source": "ncu DRAM bytes per particle of one full launch at skin %s "
+                                           "(profiles/k_pair_%s_brush_replicas.md), times N"
+                                           % (traffic_skin, args.precision),
                          "peak_kind": peak_kind},
             "clocks": clocks}
     if e2e is not None:
