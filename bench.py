@@ -319,14 +319,17 @@ def main():
     if args.skin == "auto":
         from mfa_brush_gb300 import tune
         # every replica of this rank: the rebuild rate depends on the size of the batch
-        best, rates = tune.tune_skin(p, reps, n_sample=len(reps), steps=100, precision=args.precision,
-                                     device=local)
-        blk, brates = tune.tune_block(p, reps, best, n_sample=len(reps), steps=100, precision=args.precision,
-                                      device=local)
+        # each candidate warmed up like the timed run (the first steps after the lattice start
+        # are hotter and rebuild more often)
+        best, rates = tune.tune_skin(p, reps, n_sample=len(reps), steps=100, warmup=args.warmup,
+                                     precision=args.precision, device=local)
+        blk, brates = tune.tune_block(p, reps, best, n_sample=len(reps), steps=100, warmup=args.warmup,
+                                      precision=args.precision, device=local)
         tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
                  "block_candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in brates.items()},
                  "block_size": blk,
-                 "unit": "G atom-steps/s on the %d replicas of this GPU, 100 steps each" % len(reps)}
+                 "unit": "G atom-steps/s on the %d replicas of this GPU, 100 steps each after %d "
+                         "warm-up steps" % (len(reps), args.warmup)}
         args.skin = best
         args.block = blk
     args.skin = float(args.skin)
