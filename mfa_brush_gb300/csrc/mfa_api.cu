@@ -315,7 +315,6 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   DA(K.kn, K.nk);
   DA(K.kvec, 3 * K.nk);
   DA(K.kfac, K.nk);
-  DA(K.rho, 2 * K.nk);
   DA(K.mz, 1);
   DA(K.rows, K.nrows);
   DA(K.krow, K.nk);

@@ -290,7 +290,6 @@ __global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, Acc ac
         re += part[h][kl].x;
         im += part[h][kl].y;
       }
-      reinterpret_cast<double2*>(K.rho)[k] = make_double2(re, im);
       const double G = K.kfac[k];
       u += G * (re * re + im * im);
       if constexpr (MIXED) {

@@ -99,7 +99,6 @@ struct KSpace {
   int4* kn;             // [nk] (nx, ny, nz, 0) in the reference's enumeration order
   double* kvec;         // [3*nk]
   double* kfac;         // [nk] exp(-k^2/(4 alpha_c)) / k^2
-  double* rho;          // [2*nk] Re, Im of sum_q q exp(i k.r)
   float2* tabf;         // [ncol][nq] (mixed): X(0..nxm), Y(0..nym), Z(0..nzm) per particle
   double2* tabd;        // [ncol][nq] (fp64)
   int* qtag;            // [nq] tags of the charged particles
