@@ -370,6 +370,27 @@ def test_pair_block_size_does_not_change_the_trajectory(gpu, block):
         assert np.array_equal(x, y)
 
 
+def test_measurement_aids(gpu):
+    """mfa_fp32_fma_peak measures a plausible FP32 FMA throughput (a GB300 has 152 SMs x 128 lanes
+    x 2 FLOP x ~2 GHz = ~80 TFLOP/s nominal); mfa_kspace_info gives the k-set and charge counts of
+    a charged context and zeros for an uncharged one."""
+    import ctypes as C
+    from mfa_brush_gb300 import abi
+    peak = C.c_double(0.0)
+    assert abi.load_library().mfa_fp32_fma_peak(0, C.byref(peak)) == 0
+    assert 10.0 < peak.value < 200.0
+    assert abi.load_library().mfa_fp32_fma_peak(99, C.byref(peak)) == -1  # MFA_ERR_ARG
+    p, s, a_type, r0, v = charged_system()
+    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
+    nk, nq = g.kspace_info()
+    assert nk > 0 and nq == int(np.count_nonzero([p.charge[t - 1] for t in a_type]))
+    g.close()
+    pu = configs.wca_params(gamma=5.0)
+    g = md.MdSystem(pu, s, a_type, r0, v, precision="mixed")
+    assert g.kspace_info() == (0, 0)
+    g.close()
+
+
 def test_state_round_trip_pinned_and_pageable(gpu):
     """mfa_set_state reads page-locked arrays directly and pageable ones through the staging
     buffer; mfa_sync_to_host fills both kinds alike.  Both give the same state, and a round trip

@@ -168,3 +168,14 @@ def test_melt_brush_tables_and_generation(lib):
         d[..., :2] -= L * np.round(d[..., :2] / L)
         assert np.linalg.norm(d, axis=2).max() < 1.5
 
+
+def test_fp32_peak_probe_without_a_device(lib):
+    """mfa_fp32_fma_peak reports MFA_ERR_NO_DEVICE where no GPU is visible, and rejects a null
+    output pointer."""
+    import ctypes as C
+    from mfa_brush_gb300 import md
+    out = C.c_double(0.0)
+    assert lib.mfa_fp32_fma_peak(0, None) == -1  # MFA_ERR_ARG
+    if md.device_count() < 1:
+        assert lib.mfa_fp32_fma_peak(0, C.byref(out)) == -10  # MFA_ERR_NO_DEVICE
+
