@@ -266,7 +266,7 @@ def main():
                     help="brush-replicas: the benchmark; charged-brush: the slab-Ewald channel; "
                          "melt-brush: the 340k-particle melt-in-brush channel")
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=60)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -466,7 +466,7 @@ def run_e2e(g, n_atoms, n_all, args, dist):
     dp = abi.dptr
     abi.check(lib.mfa_sync_to_host(g.ctx, dp(hr), dp(hv), dp(ha), None), g.ctx)
     e = (abi.Energies * g.nrep)()
-    chunks = max(1, min(args.steps, 100) // CHUNK)
+    chunks = max(1, min(args.steps, 300) // CHUNK)
     # one untimed round trip
     abi.check(lib.mfa_set_state(g.ctx, dp(hr), dp(hv), dp(ha)), g.ctx)
     g.step(CHUNK)
