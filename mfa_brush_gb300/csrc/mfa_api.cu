@@ -19,6 +19,8 @@ struct mfa_ctx {
   int device = 0;
   cudaStream_t st = nullptr;
   cudaStream_t st2 = nullptr;  // captures the bodies of conditional graph nodes
+  cudaStream_t stc = nullptr;  // host <-> device copies of mfa_set_state / mfa_sync_to_host
+  cudaEvent_t ev_io[5] = {};   // their ordering against the compute stream
   mfa_params P;
   mfa_options opt;
   std::vector<mfa_system> sys;
@@ -409,7 +411,9 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->stc, cudaStreamNonBlocking));
   for (int k = 0; k < 16; ++k) CK(cudaEventCreate(&ctx->ev[k]));
+  for (int k = 0; k < 5; ++k) CK(cudaEventCreateWithFlags(&ctx->ev_io[k], cudaEventDisableTiming));
   const mfa_flags& F = p->flags;
   if (p->n_type < 1 || p->n_type > MFA_MAX_TYPES) return fail(ctx, MFA_ERR_ARG, "n_type out of range");
   if (F.symmetry != 0) return fail(ctx, MFA_ERR_UNSUPPORTED, "only SYMMETRY 0 (channel) is built");
@@ -776,7 +780,10 @@ int mfa_destroy(mfa_ctx* ctx) {
   for (int k = 0; k < 16; ++k)
     if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
   if (ctx->st) cudaStreamDestroy(ctx->st);
+  for (int k = 0; k < 5; ++k)
+    if (ctx->ev_io[k]) cudaEventDestroy(ctx->ev_io[k]);
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
+  if (ctx->stc) cudaStreamDestroy(ctx->stc);
   delete ctx;
   return MFA_OK;
 }
@@ -1113,41 +1120,27 @@ static int staging(mfa_ctx* ctx, double** out) {
   return MFA_OK;
 }
 
-// Page-locked host arrays (cudaHostAlloc, cudaMallocHost, cudaHostRegister) are read by the
-// scatter kernel of mfa_set_state directly over the host link, which skips the staging copy; the
-// address is used only when the runtime reports page-locked host memory mapped at the same
-// address (unified addressing).  Pageable arrays go through the staging buffer and a copy.
-static bool host_pinned(const void* h) {
-  if (!h) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
-    cudaGetLastError();  // pageable memory on some runtimes: not an error here
-    return false;
-  }
-  return at.type == cudaMemoryTypeHost && at.devicePointer == h;
-}
-
 int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* force) {
   if (!ctx) return MFA_ERR_ARG;
   size_t n3 = 3 * (size_t)ctx->N;
   double* host[4] = {r0, v, a, force};
-  double* dst[4] = {nullptr, nullptr, nullptr, nullptr};
-  bool staged = false;
-  // (always staged: a gather kernel writing to host memory directly measured 3x slower than the
-  // gather into device memory followed by the copy engine)
+  if (!r0 && !v && !a && !force) return mfa_synchronize(ctx);
+  double* buf = nullptr;
+  RET(staging(ctx, &buf));
+  // One array at a time: its gather into the staging buffer (device memory, the compute stream),
+  // then its copy-engine copy to the host (the copy stream) while the next array is gathered.
+  // (A gather kernel writing to host memory directly measured 3x slower than this.)
   for (int k = 0; k < 4; ++k) {
     if (!host[k]) continue;
-    double* buf = nullptr;
-    RET(staging(ctx, &buf));
-    dst[k] = buf + k * n3;
-    staged = true;
+    double* d = buf + k * n3;
+    launch_gather_state(ctx->S, ctx->st, k == 0 ? d : nullptr, k == 1 ? d : nullptr, k == 2 ? d : nullptr,
+                        k == 3 ? d : nullptr);
+    CK(cudaEventRecord(ctx->ev_io[k], ctx->st));
+    CK(cudaStreamWaitEvent(ctx->stc, ctx->ev_io[k], 0));
+    CK(cudaMemcpyAsync(host[k], d, n3 * 8, cudaMemcpyDeviceToHost, ctx->stc));
   }
-  if (!r0 && !v && !a && !force) return mfa_synchronize(ctx);
-  launch_gather_state(ctx->S, ctx->st, dst[0], dst[1], dst[2], dst[3]);
-  if (staged)
-    for (int k = 0; k < 4; ++k)
-      if (host[k] && dst[k] != host[k])
-        CK(cudaMemcpyAsync(host[k], dst[k], n3 * 8, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaEventRecord(ctx->ev_io[4], ctx->stc));
+  CK(cudaStreamWaitEvent(ctx->st, ctx->ev_io[4], 0));
   RET(post_status(ctx));
   return check_status(ctx);
 }
@@ -1156,19 +1149,26 @@ int mfa_set_state(mfa_ctx* ctx, const double* r0, const double* v, const double*
   if (!ctx) return MFA_ERR_ARG;
   size_t n3 = 3 * (size_t)ctx->N;
   const double* host[3] = {r0, v, a};
-  const double* src[3] = {nullptr, nullptr, nullptr};
-  for (int k = 0; k < 3; ++k) {
-    if (!host[k]) continue;
-    if (host_pinned(host[k])) {
-      src[k] = host[k];
-    } else {
-      double* buf = nullptr;
-      RET(staging(ctx, &buf));
-      CK(cudaMemcpyAsync(buf + k * n3, host[k], n3 * 8, cudaMemcpyHostToDevice, ctx->st));
-      src[k] = buf + k * n3;
+  if (r0 || v || a) {
+    double* buf = nullptr;
+    RET(staging(ctx, &buf));
+    // One array at a time: its copy-engine copy into the staging buffer (the copy stream, after
+    // all earlier work of the context), then its scatter into slot order (the compute stream)
+    // while the next array is copied.
+    CK(cudaEventRecord(ctx->ev_io[4], ctx->st));
+    CK(cudaStreamWaitEvent(ctx->stc, ctx->ev_io[4], 0));
+    for (int k = 0; k < 3; ++k) {
+      if (!host[k]) continue;
+      CK(cudaMemcpyAsync(buf + k * n3, host[k], n3 * 8, cudaMemcpyHostToDevice, ctx->stc));
+      CK(cudaEventRecord(ctx->ev_io[k], ctx->stc));
+    }
+    for (int k = 0; k < 3; ++k) {
+      if (!host[k]) continue;
+      const double* d = buf + k * n3;
+      CK(cudaStreamWaitEvent(ctx->st, ctx->ev_io[k], 0));
+      launch_scatter_state(ctx->S, ctx->st, k == 0 ? d : nullptr, k == 1 ? d : nullptr, k == 2 ? d : nullptr);
     }
   }
-  launch_scatter_state(ctx->S, ctx->st, src[0], src[1], src[2]);
   // the lists stay valid unless some particle moved more than skin/2 from the last rebuild
   launch_refresh_views(ctx->S, ctx->C, ctx->st);
   rebuild(ctx, false);

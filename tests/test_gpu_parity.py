@@ -392,8 +392,9 @@ def test_measurement_aids(gpu):
 
 
 def test_state_round_trip_pinned_and_pageable(gpu):
-    """mfa_set_state reads page-locked arrays directly and pageable ones through the staging
-    buffer; mfa_sync_to_host fills both kinds alike.  Both give the same state, and a round trip
+    """mfa_set_state and mfa_sync_to_host move page-locked and pageable host arrays alike, one
+    array at a time through the staging buffer, overlapping each copy with the previous array's
+    scatter (or the next array's gather).  Both give the same state, and a round trip
     of an unchanged state is exact and needs no list rebuild."""
     torch = pytest.importorskip("torch")
     from mfa_brush_gb300 import abi
