@@ -230,6 +230,8 @@ int mfa_write_conf_new(const char* path, const mfa_inputs* in, int32_t n_part,
 int mfa_force_switch_on(mfa_params* p, int64_t n_relax, int64_t n_obser);
 
 /* ---- context --------------------------------------------------------------------------- */
+/* On a failure after the context was made (every status but MFA_ERR_ARG and MFA_ERR_NO_DEVICE),
+   *out still holds it so that mfa_last_error(*out) can say why; release it with mfa_destroy.   */
 int mfa_init(const mfa_params* p, const mfa_system* sys, const int32_t* a_type, const double* r0,
              const double* v, const double* a, const mfa_options* opt, mfa_ctx** out);
 int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sys,
