@@ -255,6 +255,23 @@ def run_single(args):
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": roof,
             "clocks": clocks}
+    if args.precision == "mixed" and not args.no_fp64:
+        # the same system in the plain FP64 mode (the configuration's reference point)
+        g.close()
+        gd = md.MdSystem(p, s, a_type, r0, v, precision="fp64", skin=skin)
+        for _ in range(2):
+            gd.step(CHUNK)
+        gd.synchronize()
+        gd.event_record(0)
+        for _ in range(5):
+            gd.step(CHUNK)
+        gd.event_record(1)
+        fv = n * 5 * CHUNK / (gd.event_elapsed(0, 1) / 1000.0)
+        gd.close()
+        line["plain_fp64"] = {"value": fv, "unit": UNIT, "steps": 5 * CHUNK,
+                              "speedup_of_value": line["value"] / fv}
+        print(json.dumps(line), flush=True)
+        return 0
     print(json.dumps(line), flush=True)
     g.close()
     return 0
