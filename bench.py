@@ -6,7 +6,7 @@ gamma=5, kT=1, dt=0.005), ~4.7M particles, batched in one context, mixed precisi
 bond arithmetic on fixed-point positions, FP64 integration), graph-captured 10-step chunks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision mixed|fp64]
-  python bench.py --workload charged-brush|melt-brush [--steps K] [--warmup W] [--precision mixed|fp64]
+  python bench.py --workload charged-brush|melt-brush|two-liquid [--steps K] [--warmup W] [--precision mixed|fp64]
 
 A step is one full MD step of all replicas.  `value` times K steps with the state resident on the
 device (CUDA events on the library's stream).  `e2e` times the same steps through the C ABI with
@@ -188,6 +188,8 @@ SINGLE = {
                      "counterions, slab Ewald (alpha_c 0.81, 8070 k-vectors, r_c 3) + DPD",
     "melt-brush": "melt in brush 100x100x40, grafting 0.2 per wall, N=50, melt N=20 to 0.85, cosine "
                   "bending k_b=2, LJ 2*2^(1/6) with eps_bm=1.2, brush WCA, DPD",
+    "two-liquid": "two-liquid Poiseuille channel 200x200x50, grafting 0.15, N=30, liquids A/B layered "
+                  "to 0.8, eps_AB=0.5, LJ 2*2^(1/6), f_x=0.01, DPD, z-profiles every step",
 }
 
 
@@ -201,10 +203,13 @@ def run_single(args):
     build.build()
     if args.workload == "charged-brush":
         p, (s, a_type, r0, v) = configs.charged_brush()
-    else:
+    elif args.workload == "melt-brush":
         p, (s, a_type, r0, v) = configs.melt_brush()
+    else:
+        p, (s, a_type, r0, v) = configs.two_liquid_large()
     skin = 0.5 if args.skin == "auto" else float(args.skin)
-    g = md.MdSystem(p, s, a_type, r0, v, precision=args.precision, skin=skin)
+    prof = {"profile_from_step": 0} if args.workload == "two-liquid" else {}
+    g = md.MdSystem(p, s, a_type, r0, v, precision=args.precision, skin=skin, **prof)
     done = 0
     while done < args.warmup:
         g.step(CHUNK)
@@ -233,11 +238,19 @@ def run_single(args):
             nk, nq = g.kspace_info()
             fam, flop = "kspace", 23.0 * nk * nq
             what = "k-space family (k_ks_*), %d k-vectors x %d charged particles" % (nk, nq)
-        else:
+        elif args.workload == "melt-brush":
             npair = len(g.pair_list(0))
             fam, flop = "pair", 2.0 * 40.0 * npair
             what = "k_pair, %d interacting pairs (each evaluated from both sides)" % npair
-        if kt.get(fam, (0, 0))[1]:
+        else:
+            fam, flop, what = None, 0.0, ""
+        if fam is None and kt.get("pair", (0, 0))[1]:
+            # as for the batched replicas: 48 B per particle against the measured copy bandwidth
+            hbm, peak_kind = peaks()
+            achieved = PAIR_BYTES[args.precision] * n / (kt["pair"][0] / 1000.0) / 1e9
+            roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                    "traffic": None, "kernel": "k_pair (%s)" % args.precision, "peak_kind": peak_kind}
+        elif fam and kt.get(fam, (0, 0))[1]:
             achieved = flop / (kt[fam][0] / 1000.0) / 1e12
             roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                     "frac": achieved / peak.value, "traffic": None, "kernel": what,
@@ -279,9 +292,11 @@ def run_single(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="brush-replicas", choices=["brush-replicas", "charged-brush", "melt-brush"],
+    ap.add_argument("--workload", default="brush-replicas",
+                    choices=["brush-replicas", "charged-brush", "melt-brush", "two-liquid"],
                     help="brush-replicas: the benchmark; charged-brush: the slab-Ewald channel; "
-                         "melt-brush: the 340k-particle melt-in-brush channel")
+                         "melt-brush: the 340k-particle melt-in-brush channel; two-liquid: the "
+                         "1.6M-particle two-liquid Poiseuille channel with z-profiles")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=60)

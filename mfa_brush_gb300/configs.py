@@ -397,6 +397,15 @@ def melt_brush(L=100.0, D=40.0, sigma_g=0.2, n_mon=50, n_mon_d=20, rho=0.85, see
     return p, (s, a_type, r0, v)
 
 
+def two_liquid_large(seed=3):
+    """The large two-liquid Poiseuille channel: 200 x 200 x 50, brushes at grafting density 0.15
+    per wall with N = 30, liquids A and B in layered halves to total density 0.8 (1.6 M
+    particles), eps_AB = 0.5, every liquid pair cut at 2 * 2^(1/6) sigma, body force f_x = 0.01,
+    DPD gamma = 5, z-profiles on.  Returns (mfa_params, (System, a_type, r0, v))."""
+    p, _ = md.derive(two_liquid_inputs(f_x=0.01))
+    return p, two_liquid_channel(L=200.0, D=50.0, sigma_g=0.15, n_mon=30, rho=0.8, seed=seed)
+
+
 def small_channel(seed=1):
     """20x20x20 channel, 40 chains of 30 beads per wall (grafting density 0.1), solvent to 0.8."""
     return brush_channel(20.0, 20.0, 0.1, 30, rho=0.8, seed=seed)
