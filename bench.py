@@ -117,6 +117,16 @@ def make_workload(seed, n_rep):
     return configs.wca_params(gamma=5.0, kT=1.0, dt=0.005), reps
 
 
+def oracle_params(**kw):
+    """The derived tables of the WCA brush model from the oracle's own restatement of
+    init_params.f90 (the CPU legs use no part of the library)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from mfa_brush_gb300 import configs
+    oracle.build()
+    return oracle.derive_params(configs.wca_inputs(**kw))[0]
+
+
 def cpu_sample(reps, p, steps, warmup, threads):
     """Restated reference CPU path on the given replicas: (atom-steps/s, atom-steps, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -133,6 +143,24 @@ def cpu_sample(reps, p, steps, warmup, threads):
         tot_n += s.n_part * steps
         o.close()
     return tot_n / tot_t, tot_n, tot_t
+
+
+def config1_cpu(steps_all, steps_one):
+    """The plain FP64 reference-scale channel (20 x 20 x 20, explicit wall beads on a 1 sigma
+    lattice, 40 chains of 30 beads per wall, solvent to 0.8, DPD with its own 1 sigma cut-off) on
+    the restated reference CPU path: all host cores and one thread."""
+    from mfa_brush_gb300 import configs
+    p = oracle_params(gamma=5.0, kT=1.0, dt=0.005, wall=1, dpd_cut_off=1.0)
+    rep = configs.explicit_wall_channel(seed=1)
+    threads = os.cpu_count() or 1
+    va, _, _ = cpu_sample([rep], p, steps_all, 10, threads)
+    v1, _, _ = cpu_sample([rep], p, steps_one, 5, 1)
+    return {"workload": "20x20x20 channel, explicit wall beads, 40 chains of 30 per wall, solvent to 0.8 "
+                        "(%d particles, %d mobile), WCA + FENE + DPD (own 1 sigma cut-off), FP64"
+                        % (rep[0].n_part, rep[0].n_mon_tot),
+            "all_cores": {"value": va, "unit": UNIT, "cores": threads, "steps": steps_all},
+            "one_thread": {"value": v1, "unit": UNIT, "cores": 1, "steps": steps_one},
+            "kind": "port"}
 
 
 def plain_fp64(reps, p, skin, device, every=16, steps=100, warmup=20):
@@ -157,26 +185,28 @@ def plain_fp64(reps, p, skin, device, every=16, steps=100, warmup=20):
 
 
 def run_reference(args, rank, world):
+    """The restated reference CPU path (the oracle's OpenMP loop, all host threads) on this arm's
+    workload: every replica of the set, each advanced `steps` timed steps after `warmup`
+    untimed ones (at most 20 and 3, so the run stays within a few minutes), with tables derived
+    by the oracle itself."""
     if rank != 0:
         return 0
+    from mfa_brush_gb300 import configs
     threads = os.cpu_count() or 1
-    p, reps = make_workload(args.seed, args.replicas)
-    # bounded sample: the first replicas up to ~80k particles, so K steps finish in a few minutes
-    sample, n = [], 0
-    for r in reps:
-        if n > 80000:
-            break
-        sample.append(r)
-        n += r[0].n_part
-    v, an, t = cpu_sample(sample, p, args.steps, args.warmup, threads)
-    desc = "%d of %d replicas (%d particles), %d timed steps after %d warm-up" % (
-        len(sample), len(reps), n, args.steps, args.warmup)
+    p = oracle_params(gamma=5.0, kT=1.0, dt=0.005)
+    reps = configs.replicas(args.replicas, args.seed)
+    steps, warm = min(args.steps, 20), min(args.warmup, 3)
+    v, an, t = cpu_sample(reps, p, steps, warm, threads)
+    n = int(sum(r[0].n_part for r in reps))
+    desc = "all %d replicas (%d particles), %d timed steps each after %d warm-up, one replica at a time" % (
+        len(reps), n, steps, warm)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps,
+            "steps": steps, "warmup": warm, "ms_per_step": 1000 * t / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded brush channels)",
-            "config": {"workload": "256 uneven brush-channel replicas (sample)", "replicas": len(sample),
-                       "particles": n, "precision": "fp64", "l2_flush": "inputs larger than L2"},
+            "config": {"workload": "256 uneven brush-channel replicas, WCA+FENE+DPD", "replicas": len(reps),
+                       "particles": n, "timed_steps": steps, "seed": args.seed, "precision": "fp64",
+                       "l2_flush": "inputs larger than L2"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -471,14 +501,16 @@ def main():
                 break
             sample.append(r)
             n += r[0].n_part
-        cv, an, ct = cpu_sample(sample, p, 40, 5, threads)
+        po = oracle_params(gamma=5.0, kT=1.0, dt=0.005)
+        cv, an, ct = cpu_sample(sample, po, 40, 5, threads)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "%d replicas, %d particles, 40 steps (restated reference "
                                           "OpenMP path)" % (len(sample), n)}
         # the same path on one thread, on the first replica only (a few seconds)
-        c1, _, _ = cpu_sample(sample[:1], p, 20, 2, 1)
+        c1, _, _ = cpu_sample(sample[:1], po, 20, 2, 1)
         line["cpu_baseline_1thread"] = {"value": c1, "unit": UNIT, "cores": 1, "kind": "port",
                                         "sample": "1 replica, %d particles, 20 steps" % sample[0][0].n_part}
+        line["cpu_baseline_config1"] = config1_cpu(2000, 400)
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()

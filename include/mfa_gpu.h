@@ -223,7 +223,9 @@ int mfa_derive_params(const mfa_inputs* in, mfa_params* out, mfa_system* sys_out
 /* init_config.f90:109-208: conf_old reader (types, positions, velocities, accelerations). */
 int mfa_read_conf_old(const char* path, int32_t n_part, int32_t* a_type, double* r0, double* v,
                       double* a);
-/* store_config.f90:14-63 (case 2, implicit walls): conf_new writer. */
+/* store_config.f90:14-63 (case 2): conf_new writer.  With in->flags.wall == 1 the explicit wall
+   beads (the particles after the mobile ones) are written as the r_wall_equi block
+   (store_config.f90:47-52); the top/bottom wall block is zero (the walls do not move).        */
 int mfa_write_conf_new(const char* path, const mfa_inputs* in, int32_t n_part,
                        const int32_t* a_type, const double* r0, const double* v, const double* a);
 /* init_force_switch_on.f90:12-28: sets r_2_min_init/r_2_min_time of p (used when s_time == 1). */
@@ -281,11 +283,17 @@ int mfa_profiles_accumulate(mfa_ctx* ctx);
 
 /* ---- fused step ------------------------------------------------------------------------
  * Runs nsteps complete md_main steps (positions, lists, all forces, velocities, energies every
- * energy_every steps, profiles) on the device; graph-captured when opt.use_graphs.           */
+ * energy_every steps, profiles) on the device; graph-captured when opt.use_graphs.
+ * Each call first looks, without waiting, at the status words that the previous call copied to
+ * the host (once that copy has arrived): a list count past 85 % of the capacity raises the
+ * capacity before the new steps.  If the lists of an earlier rebuild overflowed, the capacity is
+ * raised, the lists are rebuilt and the call returns MFA_ERR_NLIST_OVERFLOW without running steps
+ * (the steps since that rebuild ran on truncated lists); a later call continues normally.     */
 int mfa_step(mfa_ctx* ctx, int32_t nsteps);
 /* Neighbour-list capacity (entries per particle) and the largest count seen at the rebuilds so
    far.  When the largest count passes 85 % of the capacity, the next mfa_step or
-   mfa_verlet_positions raises the capacity by half (up to its maximum) and rebuilds the lists. */
+   mfa_verlet_positions raises the capacity by half (up to its maximum) and rebuilds the lists;
+   the overflow status of the old capacity is cleared by that rebuild.                         */
 int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count);
 /* Size of the reciprocal-space sum: k-vectors of the reference's k-set (ewald_k.f90:47-124) and
    charged particles; both 0 for an uncharged context.                                         */
@@ -324,9 +332,12 @@ int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_
 /* No counterpart in the reference.  mfa_pair_list that takes no device memory from the
    allocator: for callers that cannot allocate device memory at the point of the call (a host
    program that has handed the device's memory to another component or pool).  The pairs are
-   staged in a fixed device array of MFA_PAIR_LIST_STATIC_MAX pairs; cap above that returns
-   MFA_ERR_CAPACITY.  The first call on a device looks the array up (make it before any stream
-   capture); calls that overlap on one device share the array and race.                      */
+   staged in a fixed device array of MFA_PAIR_LIST_STATIC_MAX pairs (2 MiB, held on every device
+   that loads the library until exit); cap above that returns MFA_ERR_CAPACITY.  The first call
+   on a context looks the array's device address up (make it before any stream capture; a
+   context made after a device reset looks it up again).  The call makes the context's device
+   current and restores the caller's current device before it returns.  Calls that overlap on
+   one device share the array and race.                                                       */
 #define MFA_PAIR_LIST_STATIC_MAX 262144
 int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n);
 

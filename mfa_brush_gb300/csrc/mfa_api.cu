@@ -5,7 +5,6 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
-#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -41,7 +40,9 @@ struct mfa_ctx {
   KSpace K;
   bool kspace = false;
   unsigned* h_status = nullptr;  // pinned: [0] status bits, [1] largest list count seen
+  cudaEvent_t ev_status = nullptr;  // recorded after each copy of the status words into h_status
   bool grow_pending = false;     // the list capacity is to be raised before the next step
+  bool overflow_reported = false;  // the current list overflow was returned to the caller already
   long long* h_rebuilds = nullptr;
   long long* d_rebuilds = nullptr;
   long long last_rebuilds = 0;
@@ -53,6 +54,10 @@ struct mfa_ctx {
   std::vector<void*> allocs;
   double* stage = nullptr;  // 4 x 3N doubles for host <-> device state movement, made on first use
   double* obs = nullptr;    // [nrep][9] of mfa_observe, made on first use
+  // device addresses of the file-scope scratch of mfa_pair_list_static, looked up at the first
+  // call of that entry point on this context (with the context's device current)
+  int* static_pairs = nullptr;
+  unsigned long long* static_count = nullptr;
   std::string err;
   double rl_max = 0.;
 };
@@ -85,7 +90,10 @@ int dalloc(mfa_ctx* ctx, T** p, size_t n) {
   void* q = nullptr;
   if (n == 0) n = 1;
   cudaError_t e = cudaMalloc(&q, n * sizeof(T));
-  if (e != cudaSuccess) return fail(ctx, MFA_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // an allocation failure is not sticky: later launch checks must not see it
+    return fail(ctx, MFA_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
   ctx->allocs.push_back(q);
   *p = (T*)q;
   return MFA_OK;
@@ -99,22 +107,49 @@ int dalloc(mfa_ctx* ctx, T** p, size_t n) {
 
 Acc acc_of(double* a, int nrep) { return Acc{a, nrep}; }
 
+// The list capacity is raised before the next step when the largest list count of the rebuilds
+// so far has passed 85 % of it (or the lists overflowed), so that a density fluctuation later in
+// the run does not overflow them.
+void note_list_count(mfa_ctx* ctx) {
+  if (ctx->h_status[1] * 20u > (unsigned)ctx->S.nbr_cap * 17u && ctx->S.nbr_cap < NL_CAP_MAX)
+    ctx->grow_pending = true;
+}
+
 int check_status(mfa_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->st));
   unsigned s = ctx->h_status[0];
-  // a list count past 85 % of the capacity: raise the capacity before the next step, so that a
-  // density fluctuation later in the run does not overflow it
-  if (ctx->h_status[1] * 20u > (unsigned)ctx->S.nbr_cap * 17u && ctx->S.nbr_cap < NL_CAP_MAX)
-    ctx->grow_pending = true;
+  note_list_count(ctx);
   if (s & ST_NAN) return fail(ctx, MFA_ERR_NAN, "non-finite position detected");
   if (s & ST_OUT_OF_BOX) return fail(ctx, MFA_ERR_OUT_OF_BOX, "a particle left the channel");
-  if (s & ST_NLIST_OVERFLOW) return fail(ctx, MFA_ERR_NLIST_OVERFLOW, "neighbour list capacity exceeded");
+  if (s & ST_NLIST_OVERFLOW) {
+    ctx->overflow_reported = true;
+    return fail(ctx, MFA_ERR_NLIST_OVERFLOW, "neighbour list capacity exceeded");
+  }
   return MFA_OK;
 }
 
 int post_status(mfa_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->h_status, ctx->S.status, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaEventRecord(ctx->ev_status, ctx->st));
   return MFA_OK;
+}
+
+// Non-blocking look at the status words of the last post_status: when that copy has arrived (no
+// copy into h_status is then in flight), a list count past 85 % of the capacity schedules the
+// growth, and an overflow of an earlier rebuild is reported.  When it has not arrived yet, the
+// next call looks again.  Lets a caller that only ever calls mfa_step get the growth too.
+int poll_status(mfa_ctx* ctx) {
+  const cudaError_t q = cudaEventQuery(ctx->ev_status);
+  if (q == cudaErrorNotReady) return MFA_OK;
+  CK(q);
+  note_list_count(ctx);
+  if (ctx->h_status[0] & ST_NLIST_OVERFLOW) return MFA_ERR_NLIST_OVERFLOW;
+  return MFA_OK;
+}
+
+__global__ void k_clear_overflow(unsigned* status) {
+  atomicAnd(status, ~ST_NLIST_OVERFLOW);
+  status[1] = 0u;
 }
 
 __global__ void k_count_rebuild(int* flag, long long* n) {
@@ -414,6 +449,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaStreamCreateWithFlags(&ctx->stc, cudaStreamNonBlocking));
   for (int k = 0; k < 16; ++k) CK(cudaEventCreate(&ctx->ev[k]));
   for (int k = 0; k < 5; ++k) CK(cudaEventCreateWithFlags(&ctx->ev_io[k], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->ev_status, cudaEventDisableTiming));
   const mfa_flags& F = p->flags;
   if (p->n_type < 1 || p->n_type > MFA_MAX_TYPES) return fail(ctx, MFA_ERR_ARG, "n_type out of range");
   if (F.symmetry != 0) return fail(ctx, MFA_ERR_UNSUPPORTED, "only SYMMETRY 0 (channel) is built");
@@ -782,6 +818,7 @@ int mfa_destroy(mfa_ctx* ctx) {
   if (ctx->st) cudaStreamDestroy(ctx->st);
   for (int k = 0; k < 5; ++k)
     if (ctx->ev_io[k]) cudaEventDestroy(ctx->ev_io[k]);
+  if (ctx->ev_status) cudaEventDestroy(ctx->ev_status);
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
   if (ctx->stc) cudaStreamDestroy(ctx->stc);
   delete ctx;
@@ -825,9 +862,11 @@ static int read_call_slot(mfa_ctx* ctx, int slot, double* out, double add_self) 
 
 static int grow_lists(mfa_ctx* ctx);
 
+static int prepare_step(mfa_ctx* ctx);
+
 int mfa_verlet_positions(mfa_ctx* ctx) {
   if (!ctx) return MFA_ERR_ARG;
-  if (ctx->grow_pending) RET(grow_lists(ctx));
+  RET(prepare_step(ctx));
   launch_integrate(ctx->S, ctx->C, ctx->st, 0, false, false, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 1;
   rebuild(ctx, false);
@@ -993,9 +1032,38 @@ static int grow_lists(mfa_ctx* ctx) {
   S.nbr_cap = newcap;
   for (auto& g : ctx->graphs) cudaGraphExecDestroy(g.second.first);
   ctx->graphs.clear();
-  CK(cudaMemsetAsync(S.status + 1, 0, sizeof(unsigned), ctx->st));
+  // the overflow of the old capacity is over once the lists are rebuilt with the new one (the
+  // rebuild sets the bit again if they still do not fit); the other status bits stay
+  k_clear_overflow<<<1, 1, 0, ctx->st>>>(S.status);
+  ctx->h_status[0] &= ~ST_NLIST_OVERFLOW;
   ctx->h_status[1] = 0;
+  ctx->overflow_reported = false;
   rebuild(ctx, true);
+  return MFA_OK;
+}
+
+// Start of mfa_step / mfa_verlet_positions: the status of earlier calls (when it has arrived)
+// schedules a capacity growth; the growth runs before any new step.  An overflow seen here that no
+// status-returning call has reported yet means that the steps since that rebuild ran on truncated
+// lists: the capacity is raised, the lists rebuilt, and the call returns MFA_ERR_NLIST_OVERFLOW
+// without running steps.  At the largest capacity an overflow cannot be repaired and is returned
+// on every call.
+static int prepare_step(mfa_ctx* ctx) {
+  const int p = poll_status(ctx);
+  if (p != MFA_OK && p != MFA_ERR_NLIST_OVERFLOW) return p;
+  const bool over = p == MFA_ERR_NLIST_OVERFLOW;
+  if (over && ctx->S.nbr_cap >= NL_CAP_MAX)
+    return fail(ctx, MFA_ERR_NLIST_OVERFLOW,
+                "neighbour lists overflow at the largest capacity (" + std::to_string(NL_CAP_MAX) + ")");
+  const bool report = over && !ctx->overflow_reported;
+  if (over) ctx->grow_pending = true;
+  const int cap0 = ctx->S.nbr_cap;
+  if (ctx->grow_pending) RET(grow_lists(ctx));
+  if (report)
+    return fail(ctx, MFA_ERR_NLIST_OVERFLOW,
+                "neighbour lists of an earlier rebuild were truncated (capacity " + std::to_string(cap0) +
+                    "); the steps since then used them; capacity now " + std::to_string(ctx->S.nbr_cap) +
+                    " and the lists rebuilt");
   return MFA_OK;
 }
 
@@ -1064,7 +1132,7 @@ int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged) {
 int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
   if (!ctx) return MFA_ERR_ARG;
   if (nsteps <= 0) return MFA_OK;
-  if (ctx->grow_pending) RET(grow_lists(ctx));
+  RET(prepare_step(ctx));
   const long long s0 = ctx->sys[0].s_time + ctx->host_steps;
   bool prof = ctx->P.flags.profiles && (ctx->host_steps >= ctx->opt.profile_from_step);
   if (ctx->P.flags.profiles && !prof && ctx->host_steps + nsteps > ctx->opt.profile_from_step) {
@@ -1291,8 +1359,16 @@ int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_
   if (!ctx || rep < 0 || rep >= ctx->nrep || !n || cap < 0) return MFA_ERR_ARG;
   int* dp = nullptr;
   unsigned long long* dc = nullptr;
-  CK(cudaMallocAsync(&dp, sizeof(int) * 2 * std::max<int64_t>(cap, 1), ctx->st));
-  CK(cudaMallocAsync(&dc, sizeof(unsigned long long), ctx->st));
+  cudaError_t ea = cudaMallocAsync(&dp, sizeof(int) * 2 * std::max<int64_t>(cap, 1), ctx->st);
+  if (ea == cudaSuccess) {
+    ea = cudaMallocAsync(&dc, sizeof(unsigned long long), ctx->st);
+    if (ea != cudaSuccess) cudaFreeAsync(dp, ctx->st);
+  }
+  if (ea != cudaSuccess) {
+    cudaGetLastError();  // not sticky: later launch checks must not see it
+    return fail(ctx, MFA_ERR_ALLOC, std::string("pair-list scratch (cudaMallocAsync): ") + cudaGetErrorString(ea) +
+                                        "; mfa_pair_list_static takes no device memory");
+  }
   CK(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), ctx->st));
   launch_pair_list(ctx->S, ctx->C, ctx->st, rep, dp, cap, dc);
   ctx->launches += 1;
@@ -1310,44 +1386,28 @@ int mfa_pair_list(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_
 
 // ---- mfa_pair_list without device allocation -----------------------------------------------
 // Same result as mfa_pair_list, staged in file-scope device arrays instead of memory taken from
-// the allocator: MFA_PAIR_LIST_STATIC_MAX pairs and one counter.  Their device addresses are
-// looked up once per device, on the first call made with that device (the lookup may load this
-// module, so the first call must come before any stream capture).  Every call shares the same
-// scratch: two calls that overlap on one device race.
+// the allocator: MFA_PAIR_LIST_STATIC_MAX pairs and one counter.  The driver places them on each
+// device when it loads this module; every device that loads the library holds them until exit.
+// Host code must not hand the array names to a kernel (on the host they are stand-ins, not device
+// addresses): their device addresses are looked up with cudaGetSymbolAddress at the first call on
+// a context, with the context's device current, and kept in the context.  That first call may load
+// the module, so it must come before any stream capture.  A context made after a device reset
+// looks them up again.  Every call shares the same scratch and finds the last call's contents in
+// it: the counter is cleared on each call, and two calls that overlap on one device race.
 static __device__ __align__(256) int g_static_pairs[2 * MFA_PAIR_LIST_STATIC_MAX];
 static __device__ __align__(256) unsigned long long g_static_count;
 
-namespace {
-constexpr int kStaticMaxDevices = 64;
-std::mutex g_static_mu;
-int* g_static_pairs_at[kStaticMaxDevices] = {};
-unsigned long long* g_static_count_at[kStaticMaxDevices] = {};
-}  // namespace
-
-int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n) {
-  if (!ctx || rep < 0 || rep >= ctx->nrep || !n || cap < 0) return MFA_ERR_ARG;
-  if (cap > MFA_PAIR_LIST_STATIC_MAX)
-    return fail(ctx, MFA_ERR_CAPACITY,
-                "cap above MFA_PAIR_LIST_STATIC_MAX (" + std::to_string(MFA_PAIR_LIST_STATIC_MAX) +
-                    " pairs): use mfa_pair_list");
-  const int dev = ctx->device;
-  if (dev < 0 || dev >= kStaticMaxDevices) return fail(ctx, MFA_ERR_ARG, "device index out of range");
-  CK(cudaSetDevice(dev));
-  int* dp = nullptr;
-  unsigned long long* dc = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_pairs_at[dev]) {
-      void* a = nullptr;
-      void* b = nullptr;
-      CK(cudaGetSymbolAddress(&a, g_static_pairs));
-      CK(cudaGetSymbolAddress(&b, g_static_count));
-      g_static_pairs_at[dev] = static_cast<int*>(a);
-      g_static_count_at[dev] = static_cast<unsigned long long*>(b);
-    }
-    dp = g_static_pairs_at[dev];
-    dc = g_static_count_at[dev];
+static int pair_list_static_on_device(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n) {
+  if (!ctx->static_pairs) {
+    void* a = nullptr;
+    void* b = nullptr;
+    CK(cudaGetSymbolAddress(&a, g_static_pairs));
+    CK(cudaGetSymbolAddress(&b, g_static_count));
+    ctx->static_pairs = static_cast<int*>(a);
+    ctx->static_count = static_cast<unsigned long long*>(b);
   }
+  int* dp = ctx->static_pairs;
+  unsigned long long* dc = ctx->static_count;
   CK(cudaMemsetAsync(dc, 0, sizeof(unsigned long long), ctx->st));  // the pair counter starts at zero
   launch_pair_list(ctx->S, ctx->C, ctx->st, rep, dp, cap, dc);
   ctx->launches += 1;
@@ -1361,6 +1421,26 @@ int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap,
     CK(cudaStreamSynchronize(ctx->st));
   }
   return MFA_OK;
+}
+
+int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap, int64_t* n) {
+  if (!ctx || rep < 0 || rep >= ctx->nrep || !n || cap < 0) return MFA_ERR_ARG;
+  if (cap > MFA_PAIR_LIST_STATIC_MAX)
+    return fail(ctx, MFA_ERR_CAPACITY,
+                "cap above MFA_PAIR_LIST_STATIC_MAX (" + std::to_string(MFA_PAIR_LIST_STATIC_MAX) +
+                    " pairs): use mfa_pair_list");
+  // the context's device is made current for the call; the caller's current device is restored
+  int prev = 0;
+  CK(cudaGetDevice(&prev));
+  if (prev != ctx->device) CK(cudaSetDevice(ctx->device));
+  const int rc = pair_list_static_on_device(ctx, rep, pairs, cap, n);
+  if (prev != ctx->device) {
+    const cudaError_t e = cudaSetDevice(prev);
+    if (rc == MFA_OK && e != cudaSuccess)
+      return fail(ctx, MFA_ERR_CUDA, std::string("cudaSetDevice (restoring the caller's device): ") +
+                                         cudaGetErrorString(e));
+  }
+  return rc;
 }
 
 // ---- timing ---------------------------------------------------------------------------------

@@ -492,8 +492,20 @@ int mfa_write_conf_new(const char* path, const mfa_inputs* in, int32_t n_part, c
     std::fprintf(f, "%3d%13.7f%13.7f%13.7f\n", a_type[i], r0[3 * i], r0[3 * i + 1], r0[3 * i + 2]);
   for (int i = 0; i < n_part; ++i) std::fprintf(f, "%15.7f%15.7f%15.7f\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
   for (int i = 0; i < n_part; ++i) std::fprintf(f, "%15.7f%15.7f%15.7f\n", a[3 * i], a[3 * i + 1], a[3 * i + 2]);
-  // wall block of the implicit-wall case (r0_twall, rx_twall(:,1:2), pbc_twall, r0_bwall, pbc_bwall,
-  // r0_spring_twall, s_force_grad): all zero without explicit walls
+  if (in->flags.wall == 1) {
+    // WALL 1 (store_config.f90:47-52): r_wall_equi of every wall bead.  The wall beads follow the
+    // mobile particles and are held fixed here, so their equilibrium positions are their positions.
+    const long long n_mob = (long long)in->n_mon * in->n_chain + (long long)in->n_mon_d * in->n_chain_d +
+                            (long long)in->n_mon_e * in->n_chain_e;
+    if (n_mob > n_part) {
+      std::fclose(f);
+      return MFA_ERR_ARG;
+    }
+    for (long long i = n_mob; i < n_part; ++i)
+      std::fprintf(f, "%15.7f%15.7f%15.7f\n", r0[3 * i], r0[3 * i + 1], r0[3 * i + 2]);
+  }
+  // top/bottom wall block (r0_twall, rx_twall(:,1:2), pbc_twall, r0_bwall, pbc_bwall,
+  // r0_spring_twall, s_force_grad): all zero with walls that do not move
   for (int k = 0; k < 3; ++k) std::fprintf(f, "%15.7f%15.7f%15.7f\n", 0., 0., 0.);
   std::fprintf(f, "%13d%13d%13d\n", 0, 0, 0);
   std::fprintf(f, "%15.7f%15.7f%15.7f\n", 0., 0., 0.);

@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
   __syncthreads();
   const int i = blockIdx.x * NL_BLOCK + threadIdx.x;
   const int w = (i < s.N) ? s.info[i] : 0;
-  int cnt = 0;
+  int cnt = 0, found = 0;  // entries stored, neighbours found (more when the list overflows)
   if (i < s.N && info_mobile(w)) {
     const RepDesc& R = s.reps[info_rep(w)];
     const int ti = info_type(w);
@@ -370,12 +370,13 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
         }
       }
     }
+    found = cnt;
     if (cnt > cap) {
       atomicOr(s.status, ST_NLIST_OVERFLOW);
       cnt = cap;
     }
   }
-  atomicMax(&blk_max, cnt);
+  atomicMax(&blk_max, found);  // the true count, so that the host grows the capacity past it
   __syncthreads();
   if (threadIdx.x == 0) atomicMax(s.status + 1, (unsigned)blk_max);  // largest count, for the host
   const int mx = min(blk_max, NL_STAGE);

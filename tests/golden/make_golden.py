@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures under tests/golden/ from the reference's own run artefacts.
 
-Run once in a container where the reference checkout is mounted (default /root/reference):
+Run once in a container where the reference checkout is mounted:
 
-    python tests/golden/make_golden.py [REFERENCE_DIR]
+    python tests/golden/make_golden.py REFERENCE_DIR
 
 It copies the input deck of the reference's `try/` run (a 27 445-step run of the
 Filled_Channel deck: 300 brush chains x 10 beads + 3000 solvent beads, box 30x20x40) and
@@ -39,9 +39,12 @@ def main(ref):
         shutil.copyfile(os.path.join(ref, "try", name), os.path.join(out, name))
     shutil.copyfile(os.path.join(ref, "inputs", "Filled_Channel", "control_simulation.h"),
                     os.path.join(out, "control_simulation.h"))
-    with open(os.path.join(ref, "try", "conf_old"), "rb") as f, \
-            gzip.GzipFile(os.path.join(out, "conf_old.gz"), "wb", mtime=0) as g:
-        g.write(f.read())
+    # conf_old: the start of the run; conf_new: the restart file that the run wrote
+    # (store_config.f90:14-63), the byte-level fixture of the conf_new writer
+    for name in ("conf_old", "conf_new"):
+        with open(os.path.join(ref, "try", name), "rb") as f, \
+                gzip.GzipFile(os.path.join(out, name + ".gz"), "wb", mtime=0) as g:
+            g.write(f.read())
 
     kat = {"cutoffs": [], "shifts": []}
     with open(os.path.join(ref, "try", "log")) as f:
@@ -77,4 +80,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_DIR")
+    main(sys.argv[1])

@@ -466,6 +466,35 @@ def test_list_capacity_grows_before_it_overflows(gpu):
         assert np.array_equal(x, y)
 
 
+def test_list_overflow_is_cleared_by_the_growth(gpu):
+    """A state whose lists do not fit the capacity is reported (MFA_ERR_NLIST_OVERFLOW).  After the
+    original state is put back, mfa_step alone (no status-reading call in between) raises the
+    capacity, rebuilds the lists and clears the overflow: the status is clean again and the
+    trajectory equals that of a context with ample room."""
+    p = configs.wca_params(gamma=5.0)
+    s, a_type, r0, v = configs.brush_channel(14.0, 12.0, 0.2, 20, seed=71)
+    ref = md.MdSystem(p, s, a_type, r0, v, precision="fp64")
+    cap0, mx0 = ref.list_stats()
+    cap = int(np.ceil(mx0 / 0.85)) + 2  # no growth pending after start-up
+    g = md.MdSystem(p, s, a_type, r0, v, precision="fp64", nbr_capacity=cap)
+    assert g.list_stats() == (cap, mx0)
+    squeezed = np.array(r0, np.float64).reshape(-1, 3).copy()
+    D = s.boundary[2]
+    squeezed[:, 2] = 0.5 * D + 0.5 * (squeezed[:, 2] - 0.5 * D)  # twice the density: more neighbours
+    with pytest.raises(abi.MfaError) as ei:
+        g.set_state(r0=squeezed)
+    assert abi.ERRORS[ei.value.code] == "MFA_ERR_NLIST_OVERFLOW"
+    with pytest.raises(abi.MfaError):  # the rebuild of the original state fits, the overflow is still set
+        g.set_state(r0=r0)
+    for _ in range(3):
+        g.step(10)  # the first call raises the capacity and rebuilds before its steps
+    ref.step(30)
+    cap1, mx1 = g.list_stats()  # would raise if the overflow bit were still set
+    assert cap1 > cap and mx1 <= cap1
+    for x, y in zip(g.state(), ref.state()):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_force_switch_on_ramp(gpu, try_deck, oracle_mod, precision):
     """FORCE_SWITCH_ON from s_time = 1 (init_force_switch_on.f90:12-28, fluid_fluid.f90:35-42):

@@ -67,6 +67,46 @@ def test_conf_round_trip(try_deck, tmp_path):
     assert np.abs(r2 - r0).max() < 5.1e-8 and np.abs(v2 - v).max() < 5.1e-8 and np.abs(a2 - a).max() < 5.1e-8
 
 
+def test_conf_new_writer_reproduces_the_reference_file(try_deck, tmp_path):
+    """The restart file that the reference's try/ run wrote (store_config.f90:14-63, implicit
+    walls), read and written back by the library: byte for byte the same file."""
+    import gzip
+
+    from conftest import GOLDEN
+    from mfa_brush_gb300 import md
+    inp, p, s, _, _, _, _ = try_deck
+    with gzip.open(os.path.join(GOLDEN, "try", "conf_new.gz"), "rb") as g:
+        ref = g.read()
+    src = tmp_path / "conf_new_ref"
+    src.write_bytes(ref)
+    t, r, v, a = md.read_conf_old(str(src), s.n_part)
+    out = tmp_path / "conf_new"
+    md.write_conf_new(str(out), inp, t, r, v, a)
+    assert out.read_bytes() == ref
+
+
+def test_conf_new_explicit_walls_round_trip(tmp_path):
+    """WALL 1: the wall beads' equilibrium positions (store_config.f90:47-52) follow the
+    accelerations, one line per wall bead, before the eight lines of the top/bottom wall block;
+    the file reads back with the same types and positions."""
+    from mfa_brush_gb300 import configs, md
+    inp = configs.wca_inputs(wall=1, dpd_cut_off=1.0)
+    s, a_type, r0, v = configs.explicit_wall_channel(seed=2)
+    inp.n_mon, inp.n_chain = s.n_mon, s.n_chain
+    inp.n_mon_d, inp.n_chain_d = s.n_mon_d, s.n_chain_d
+    n_wall = s.n_part - s.n_mon_tot
+    assert n_wall > 0
+    a = np.zeros_like(r0)
+    path = tmp_path / "conf_new"
+    md.write_conf_new(str(path), inp, a_type, r0, v, a)
+    lines = path.read_text().splitlines()
+    assert len(lines) == 4 + 3 * s.n_part + n_wall + 8
+    walls = np.array([[float(x) for x in ln.split()] for ln in lines[4 + 3 * s.n_part:4 + 3 * s.n_part + n_wall]])
+    assert np.abs(walls - r0[s.n_mon_tot:]).max() < 5.1e-8
+    t2, r2, _, _ = md.read_conf_old(str(path), s.n_part)
+    assert np.array_equal(t2, a_type) and np.abs(r2 - r0).max() < 5.1e-8
+
+
 def test_unsupported_flags_are_rejected(try_deck):
     import ctypes as C
     from mfa_brush_gb300 import abi, md

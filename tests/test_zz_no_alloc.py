@@ -71,3 +71,43 @@ def test_static_pair_list_limits(gpu, try_deck):
     # and the scratch still works afterwards
     rc, got, n = static_pairs(g, 0, STATIC_MAX)
     assert rc == abi.MFA_OK and as_set(got) == as_set(ref)
+
+
+def test_static_pair_list_takes_no_device_memory(gpu, try_deck):
+    """The case the entry point exists for: another component of the host program holds nearly all
+    of the device's free memory.  The allocating export then cannot get its scratch and says so
+    (MFA_ERR_ALLOC); the static one still returns the same pairs, on two calls in a row, and the
+    device's free memory is the same before and after them."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    inp, p, s, a_type, r0, v, a = try_deck
+    g = md.MdSystem(p, s, a_type, r0, v, a, precision="mixed")
+    ref = g.pair_list(0)
+    rc, _, _ = static_pairs(g, 0, len(ref))  # first call on the context: the address lookup
+    assert rc == abi.MFA_OK
+    free, _ = torch.cuda.mem_get_info(0)
+    try:
+        hold = torch.empty(free - (192 << 20), dtype=torch.uint8, device="cuda:0")
+    except RuntimeError:
+        pytest.skip("could not take the device's free memory")
+    try:
+        pairs = np.zeros((len(ref) + 1, 2), np.int32)
+        n = abi.i64(0)
+        big = 64 << 20  # 64 Mi pairs: 512 MiB of scratch, more than is left
+        rc = g.lib.mfa_pair_list(g.ctx, 0, abi.iptr(pairs), big, C.byref(n))
+        assert abi.ERRORS.get(rc) == "MFA_ERR_ALLOC"
+        f0, _ = torch.cuda.mem_get_info(0)
+        for _ in range(2):
+            rc, got, n = static_pairs(g, 0, STATIC_MAX)
+            assert rc == abi.MFA_OK and n == len(ref)
+            assert as_set(got) == as_set(ref)
+        f1, _ = torch.cuda.mem_get_info(0)
+        assert f1 == f0
+    finally:
+        del hold
+        torch.cuda.empty_cache()
+    # the context goes on working once the memory is back
+    g.step(10)
+    rc, got, n = static_pairs(g, 0, STATIC_MAX)
+    assert rc == abi.MFA_OK and as_set(got) == as_set(g.pair_list(0))
