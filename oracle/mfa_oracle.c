@@ -306,7 +306,30 @@ typedef struct orc_sys {
   int hist;
   double *dens, *vp, *vp2;
   int64_t n_obs;
+  /* virial W_ab = minus the derivative of the energy under the strain r_a -> r_a + e r_b (box,
+     walls and positions deformed together).  For the pair, bond, angle and wall terms that is the
+     sum over the terms of F_a r_b (F on a particle, r its position relative to the other
+     particles of the term, or to the wall plane); the k-space and slab-dipole energies depend on
+     the volume as well.  Groups: 0 pair (LJ + DPD + real-space Coulomb), 1 FENE, 2 bending (brush
+     and melt), 3 orientation, 4 walls (zz), 5 k-space, 6 slab dipole; each routine sets its own
+     group (bending and melt bending share theirs, cleared with the forces) */
+  double vir[7][9];
+  /* per-particle force scale: the sum of the magnitudes of every force term acting on the
+     particle (NULL unless enabled by orc_track_force_scale) */
+  double* fscale;
 } orc_sys;
+
+static inline void fsc(const orc_sys* o, int i0, const double* f) {
+  if (o->fscale) o->fscale[i0] += sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+}
+static inline void fsc_mag(const orc_sys* o, int i0, double m) {
+  if (o->fscale) o->fscale[i0] += fabs(m);
+}
+/* W_ab += f_a r_b */
+static inline void vir_add(double* w, const double* f, const double* r) {
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) w[3 * a + b] += f[a] * r[b];
+}
 
 static int get_cell(const orc_sys* o, const double* r) {
   /* cell_list.f90:186-213 with per-axis clamping (see header) */
@@ -506,7 +529,7 @@ void orc_destroy(orc_sys* o) {
   free(o->a_type); free(o->r0); free(o->v); free(o->a); free(o->force); free(o->ext_force);
   free(o->mass); free(o->inv_mass); free(o->q); free(o->r_nei); free(o->l_nei);
   free(o->part_in_cell); free(o->cell_neigh_ls); free(o->kv); free(o->k2); free(o->ik2);
-  free(o->dens); free(o->vp); free(o->vp2);
+  free(o->dens); free(o->vp); free(o->vp2); free(o->fscale);
   free(o);
 }
 
@@ -588,7 +611,30 @@ void orc_get_energies(const orc_sys* o, double* e) {
   e[4] = o->v_bend; e[5] = o->v_bend_melt; e[6] = o->v_or; e[7] = o->v_coul; e[8] = o->t_fluid;
 }
 
-void orc_zero_force(orc_sys* o) { memset(o->force, 0, (size_t)3 * o->n * 8); }
+void orc_zero_force(orc_sys* o) {
+  memset(o->force, 0, (size_t)3 * o->n * 8);
+  if (o->fscale) memset(o->fscale, 0, (size_t)o->n * 8);
+  memset(o->vir, 0, sizeof o->vir);
+}
+
+/* Per-particle force scale (test aid: the conditioning of each particle's force sum). */
+void orc_track_force_scale(orc_sys* o, int on) {
+  free(o->fscale);
+  o->fscale = on ? (double*)calloc((size_t)o->n, 8) : NULL;
+}
+void orc_get_force_scale(const orc_sys* o, double* out) {
+  if (o->fscale) memcpy(out, o->fscale, (size_t)o->n * 8);
+  else memset(out, 0, (size_t)o->n * 8);
+}
+/* out[9 g + 3 a + b] = W_ab of group g (7 groups, see orc_sys::vir) */
+void orc_get_virial(const orc_sys* o, double* out) { memcpy(out, o->vir, sizeof o->vir); }
+/* Kinetic tensor sum m v_a v_b over the mobile particles (viscosity.f90:20-27). */
+void orc_kinetic_tensor(const orc_sys* o, double* out) {
+  for (int k = 0; k < 9; ++k) out[k] = 0.;
+  for (int i = 0; i < o->nm; ++i)
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) out[3 * a + b] += o->mass[i] * o->v[3 * i + a] * o->v[3 * i + b];
+}
 
 /* ------------------------------------------------------------------------------------------
  * Pair interaction of fluid_fluid.f90:97-261 / 276-436 for the ordered pair (i, j), 1-based.
@@ -596,7 +642,7 @@ void orc_zero_force(orc_sys* o) { memset(o->force, 0, (size_t)3 * o->n * 8); }
  * i and j, and the LJ reaction on j.  Returns nothing; energies via pointers.
  * ---------------------------------------------------------------------------------------- */
 static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* force_tmp,
-                           double* v_ff, double* v_coul) {
+                           double* v_ff, double* v_coul, double* w) {
   const mfa_params* p = &o->p;
   int ti = o->a_type[i - 1] - 1, tj = o->a_type[j - 1] - 1;
   double r_cut2 = p->range_2[IDX(ti, tj)];
@@ -625,6 +671,12 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
       fi[d] -= rd * dr[d];
       force_tmp[3 * (j - 1) + d] += rd * dr[d];
     }
+    {
+      double f[3] = {-rd * dr[0], -rd * dr[1], -rd * dr[2]};
+      vir_add(w, f, dr);
+      fsc(o, i - 1, f);
+      fsc(o, j - 1, f);
+    }
     int wall_pair = p->flags.wall == 1 && (ti == p->n_type - 1 || tj == p->n_type - 1);
     if (dpd && p->r_cut_dpd_2 == 0. && !wall_pair) { /* DPD inside the LJ range (dpd_forces.f90:45-53) */
       double w_r, w_d;
@@ -638,12 +690,19 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
       for (int d = 0; d < 3; ++d) ev[d] = dr[d] * inv_sqrt_r_2;
       for (int d = 0; d < 3; ++d) dv[d] = o->v[3 * (i - 1) + d] - o->v[3 * (j - 1) + d];
       double rdot = dv[0] * ev[0] + dv[1] * ev[1] + dv[2] * ev[2];
+      double fij[3];
       for (int d = 0; d < 3; ++d) {
         double fr = p->sig * w_r * g * ev[d];
         double fd = -1. * p->friction1 * w_d * rdot * ev[d];
         force_tmp[3 * (i - 1) + d] += fr + fd;
         force_tmp[3 * (j - 1) + d] -= fr + fd;
+        fij[d] = fr + fd;
       }
+      vir_add(w, fij, dr);
+      fsc_mag(o, i - 1, p->sig * w_r * g);
+      fsc_mag(o, j - 1, p->sig * w_r * g);
+      fsc_mag(o, i - 1, p->friction1 * w_d * rdot);
+      fsc_mag(o, j - 1, p->friction1 * w_d * rdot);
     }
   }
   /* real-space Ewald (ewald_real.f90:15-33) */
@@ -657,11 +716,16 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
       *v_coul += qq * erfcv * inv_r;
       double fs = qq * p->sqrt_alpha * p->inv_sqrt_pi * 2. * exp(-p->alpha_c * rc2) * inv_r +
                   qq * erfcv * inv_r * inv_r;
+      double fcv[3];
       for (int d = 0; d < 3; ++d) {
         double fc = fs * dr[d] * inv_r;
         force_tmp[3 * (i - 1) + d] += fc;
         if (!(p->compat & MFA_COMPAT_EWALD_I_ONLY)) force_tmp[3 * (j - 1) + d] -= fc;
+        fcv[d] = fc;
       }
+      vir_add(w, fcv, dr);
+      fsc(o, i - 1, fcv);
+      fsc(o, j - 1, fcv);
     }
   }
   /* DPD with its own cut-off (fluid_fluid.f90:217-258): heads excluded */
@@ -681,12 +745,19 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
       for (int d = 0; d < 3; ++d) ev[d] = dr[d] * isr;
       for (int d = 0; d < 3; ++d) dv[d] = o->v[3 * (i - 1) + d] - o->v[3 * (j - 1) + d];
       double rdot = dv[0] * ev[0] + dv[1] * ev[1] + dv[2] * ev[2];
+      double fij[3];
       for (int d = 0; d < 3; ++d) {
         double fr = p->sig * w_r * g * ev[d];
         double fd = -1. * p->friction1 * w_d * rdot * ev[d];
         force_tmp[3 * (i - 1) + d] += fr + fd;
         force_tmp[3 * (j - 1) + d] -= fr + fd;
+        fij[d] = fr + fd;
       }
+      vir_add(w, fij, dr);
+      fsc_mag(o, i - 1, p->sig * w_r * g);
+      fsc_mag(o, j - 1, p->sig * w_r * g);
+      fsc_mag(o, i - 1, p->friction1 * w_d * rdot);
+      fsc_mag(o, j - 1, p->friction1 * w_d * rdot);
     }
   }
 }
@@ -704,15 +775,17 @@ static void switch_on_r2min(orc_sys* o) {
 void orc_fluid_fluid(orc_sys* o) {
   switch_on_r2min(o);
   double vff = 0., vc = 0.;
+  double* w = o->vir[0];
+  memset(w, 0, 9 * sizeof(double));
   for (int ic = 1; ic <= o->nct; ++ic) {
     for (int i = o->part_in_cell[ic]; i != 0; i = o->r_nei[i]) {
       double fi[3] = {0, 0, 0};
       for (int jd = 0; jd < o->n_nei; ++jd) {
         int jc = o->cell_neigh_ls[(size_t)(ic - 1) * o->n_nei + jd];
-        for (int j = o->part_in_cell[jc]; j != 0; j = o->r_nei[j]) pair_ij(o, i, j, fi, o->force, &vff, &vc);
+        for (int j = o->part_in_cell[jc]; j != 0; j = o->r_nei[j]) pair_ij(o, i, j, fi, o->force, &vff, &vc, w);
       }
       for (int j = o->part_in_cell[ic]; j != 0; j = o->r_nei[j])
-        if (i < j) pair_ij(o, i, j, fi, o->force, &vff, &vc);
+        if (i < j) pair_ij(o, i, j, fi, o->force, &vff, &vc, w);
       for (int d = 0; d < 3; ++d) o->force[3 * (i - 1) + d] += fi[d];
     }
   }
@@ -725,8 +798,13 @@ void orc_fluid_fluid(orc_sys* o) {
 /* The reference's OpenMP CPU path (fluid_fluid.f90:65-70,475-476): cells in static chunks of
  * 10, each thread a private force array, reduced at the end.  This is the timed CPU baseline. */
 void orc_fluid_fluid_omp(orc_sys* o, int nthreads) {
+  if (o->fscale) {  /* the force-scale accumulation is serial */
+    orc_fluid_fluid(o);
+    return;
+  }
   switch_on_r2min(o);
   double vff = 0., vc = 0.;
+  memset(o->vir[0], 0, 9 * sizeof(double));
 #ifdef _OPENMP
   if (nthreads < 1) nthreads = omp_get_max_threads();
   int nth = nthreads;
@@ -736,19 +814,22 @@ void orc_fluid_fluid_omp(orc_sys* o, int nthreads) {
   {
     int t = omp_get_thread_num();
     double* ft = priv + n3 * t;
+    double wt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma omp for schedule(static, 10)
     for (int ic = 1; ic <= o->nct; ++ic) {
       for (int i = o->part_in_cell[ic]; i != 0; i = o->r_nei[i]) {
         double fi[3] = {0, 0, 0};
         for (int jd = 0; jd < o->n_nei; ++jd) {
           int jc = o->cell_neigh_ls[(size_t)(ic - 1) * o->n_nei + jd];
-          for (int j = o->part_in_cell[jc]; j != 0; j = o->r_nei[j]) pair_ij(o, i, j, fi, ft, &vff, &vc);
+          for (int j = o->part_in_cell[jc]; j != 0; j = o->r_nei[j]) pair_ij(o, i, j, fi, ft, &vff, &vc, wt);
         }
         for (int j = o->part_in_cell[ic]; j != 0; j = o->r_nei[j])
-          if (i < j) pair_ij(o, i, j, fi, ft, &vff, &vc);
+          if (i < j) pair_ij(o, i, j, fi, ft, &vff, &vc, wt);
         for (int d = 0; d < 3; ++d) ft[3 * (i - 1) + d] += fi[d];
       }
     }
+#pragma omp critical
+    for (int k = 0; k < 9; ++k) o->vir[0][k] += wt[k];
 #pragma omp for schedule(static)
     for (size_t k = 0; k < n3; ++k) {
       double s = 0.;
@@ -827,6 +908,7 @@ void orc_fluid_wall(orc_sys* o) {
   const mfa_params* p = &o->p;
   double vfw = 0.;
   double D = o->s.boundary[2];
+  memset(o->vir[4], 0, 9 * sizeof(double));
   if (p->flags.wall == 2) {
     for (int i = 0; i < o->nm; ++i) {
       int t = o->a_type[i] - 1;
@@ -835,13 +917,21 @@ void orc_fluid_wall(orc_sys* o) {
       double rd = p->sigma_wall[t] * inv_z;
       double aw = fabs(p->a_wall[t]), sw = p->sigma_wall[t];
       vfw += aw * ipow(rd, 9) - p->a_w * ipow(rd, 3);
+      const double f0 = o->force[3 * i + 2];
       o->force[3 * i + 2] += 9. * aw * ipow(sw, 9) * ipow(inv_z, 10);
       o->force[3 * i + 2] -= 3. * p->a_wall[t] * ipow(sw, 3) * ipow(inv_z, 4);
+      const double fb = o->force[3 * i + 2] - f0;  /* the bottom wall's force */
       inv_z = 1. / (D - z);
       rd = sw * inv_z;
       vfw += aw * ipow(rd, 9) - p->a_w * ipow(rd, 3);
+      const double f1 = o->force[3 * i + 2];
       o->force[3 * i + 2] -= 9. * aw * ipow(sw, 9) * ipow(inv_z, 10);
       o->force[3 * i + 2] += 3 * p->a_wall[t] * ipow(sw, 3) * ipow(inv_z, 4);
+      const double ft = o->force[3 * i + 2] - f1;   /* the top wall's */
+      /* each wall's force times the distance vector from the wall plane */
+      o->vir[4][8] += fb * z + ft * (z - D);
+      fsc_mag(o, i, fb);
+      fsc_mag(o, i, ft);
     }
   }
   o->v_fw = vfw;
@@ -873,6 +963,10 @@ static double fene_bond(orc_sys* o, int ip, int jp, int z_pbc) {
     o->force[3 * ip + d] -= rd * dr[d];
     o->force[3 * jp + d] += rd * dr[d];
   }
+  double f[3] = {-rd * dr[0], -rd * dr[1], -rd * dr[2]};  /* on ip; dr = r_ip - r_jp */
+  vir_add(o->vir[1], f, dr);
+  fsc(o, ip, f);
+  fsc(o, jp, f);
   return pot;
 }
 
@@ -880,6 +974,7 @@ static double fene_bond(orc_sys* o, int ip, int jp, int z_pbc) {
 void orc_intra_molec(orc_sys* o) {
   const mfa_system* s = &o->s;
   double vb = 0., vd = 0., ve = 0.;
+  memset(o->vir[1], 0, 9 * sizeof(double));
   for (int c = 1; c <= s->n_chain; ++c)
     for (int m = 1; m <= s->n_mon - 1; ++m) {
       int ip = (c - 1) * s->n_mon + m;
@@ -952,12 +1047,20 @@ static double bend_term(orc_sys* o, int ia, int ib, int ic, const double* r_prev
     fmod = k_b * da;
     e = .5 * fmod * da;
   }
+  double fa[3], fc[3], fm[3], mrp[3];
   for (int j = 0; j < 3; ++j) {
     double fb0 = fmod * dp[j], fb1 = fmod * dn[j];
     o->force[3 * ia + j] += fb0;
     o->force[3 * ib + j] += -fb0 - fb1;
     o->force[3 * ic + j] += fb1;
+    fa[j] = fb0; fc[j] = fb1; fm[j] = -fb0 - fb1; mrp[j] = -r_prev[j];
   }
+  /* sum_k F_k (x) (r_k - r_b): r_a - r_b = -r_prev, r_c - r_b = r_next */
+  vir_add(o->vir[2], fa, mrp);
+  vir_add(o->vir[2], fc, r_next);
+  fsc(o, ia, fa);
+  fsc(o, ib, fm);
+  fsc(o, ic, fc);
   return e;
 }
 
@@ -981,6 +1084,7 @@ static double bend_chains(orc_sys* o, int beg, int n_chains, int n_mon) {
 
 /* bending(1) (bending.f90:19-121) */
 void orc_bending(orc_sys* o) { o->v_bend = bend_chains(o, 0, o->s.n_chain, o->s.n_mon); }
+/* the bending group of the virial holds brush and melt bending; cleared with the forces */
 /* bending_melt(1) (bending_melt.f90:22-108; the second index there lacks the `beg` offset, a
  * reference defect not reproduced: the consecutive melt bond is used). */
 void orc_bending_melt(orc_sys* o) {
@@ -990,6 +1094,7 @@ void orc_bending_melt(orc_sys* o) {
 /* orientation(1) (orientation.f90:24-88) */
 void orc_orientation(orc_sys* o) {
   double v = 0.;
+  memset(o->vir[3], 0, 9 * sizeof(double));
   const double D = o->s.boundary[2];
   for (int l = 0; l < o->s.n_chain; ++l) {
     int h = l * o->s.n_mon; /* head, 0-based */
@@ -1024,18 +1129,26 @@ void orc_orientation(orc_sys* o) {
     double da = ((cos_a >= 1.0) ? 0. : acos(cos_a)) - o->p.alpha_or;
     double fm = o->p.k_or * da;
     v += .5 * fm * da;
+    double f1[3];
     for (int j = 0; j < 3; ++j) {
       o->force[3 * h + j] -= fm * dn[j];
       o->force[3 * (h + 1) + j] += fm * dn[j];
+      f1[j] = fm * dn[j];
     }
+    /* forces on the head and bead 1 only: F_1 (x) (r_1 - r_h) */
+    vir_add(o->vir[3], f1, r_next);
+    fsc(o, h, f1);
+    fsc(o, h + 1, f1);
   }
   o->v_or = v;
 }
 
 /* constant_force(1) (constant_force.f90:17-21) */
 void orc_constant_force(orc_sys* o) {
-  for (int i = 0; i < o->nm; ++i)
+  for (int i = 0; i < o->nm; ++i) {
     for (int d = 0; d < 3; ++d) o->force[3 * i + d] += o->ext_force[3 * i + d];
+    fsc(o, i, &o->ext_force[3 * i]);
+  }
 }
 
 /* ewald_k(0) (ewald_k.f90:37-124) */
@@ -1094,8 +1207,18 @@ double orc_ewald_k(orc_sys* o) {
     }
   }
   double u = 0.;
-  for (int k = 0; k < nk; ++k) u += o->ik2[k] * exp(-o->k2[k] * o->fac_alpha) * (re[k] * re[k] + im[k] * im[k]);
+  memset(o->vir[5], 0, 9 * sizeof(double));
+  for (int k = 0; k < nk; ++k) {
+    const double uk = o->ik2[k] * exp(-o->k2[k] * o->fac_alpha) * (re[k] * re[k] + im[k] * im[k]);
+    u += uk;
+    /* reciprocal-space virial: u_k (delta_ab - 2 k_a k_b (1/k^2 + 1/(4 alpha_c))) */
+    const double c = 2. * (o->ik2[k] + o->fac_alpha);
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+        o->vir[5][3 * a + b] += uk * ((a == b ? 1. : 0.) - c * o->kv[3 * k + a] * o->kv[3 * k + b]);
+  }
   u = u * 4. * pi * o->inv_V_k;
+  for (int k = 0; k < 9; ++k) o->vir[5][k] *= 4. * pi * o->inv_V_k;
   for (int i = 0; i < o->nm; ++i) {
     if (o->q[i] == 0.) continue;
     double fk[3] = {0, 0, 0};
@@ -1104,7 +1227,12 @@ double orc_ewald_k(orc_sys* o) {
       double s = o->ik2[k] * exp(-o->k2[k] * o->fac_alpha) * (cos(ph) * im[k] - sin(ph) * re[k]);
       for (int d = 0; d < 3; ++d) fk[d] += o->kv[3 * k + d] * s;
     }
-    for (int d = 0; d < 3; ++d) o->force[3 * i + d] += -8. * pi * o->q[i] * fk[d] * o->inv_V_k;
+    double fkv[3];
+    for (int d = 0; d < 3; ++d) {
+      fkv[d] = -8. * pi * o->q[i] * fk[d] * o->inv_V_k;
+      o->force[3 * i + d] += fkv[d];
+    }
+    fsc(o, i, fkv);
   }
   free(re);
   free(im);
@@ -1117,8 +1245,17 @@ double orc_dipolar_correction(orc_sys* o) {
   const double pi = ref_pi();
   double mz = 0.;
   for (int i = 0; i < o->nm; ++i) mz += o->q[i] * (o->r0[3 * i + 2] - o->lz_half);
-  for (int i = 0; i < o->nm; ++i) o->force[3 * i + 2] -= 4. * pi * o->q[i] * mz * o->inv_V_k;
+  for (int i = 0; i < o->nm; ++i) {
+    o->force[3 * i + 2] -= 4. * pi * o->q[i] * mz * o->inv_V_k;
+    fsc_mag(o, i, 4. * pi * o->q[i] * mz * o->inv_V_k);
+  }
   double u = 2. * pi * mz * mz * o->inv_V_k;
+  /* minus the strain derivative of u (M_z scales with z, the volume with each axis):
+     diag(u, u, -u) */
+  memset(o->vir[6], 0, 9 * sizeof(double));
+  o->vir[6][0] = u;
+  o->vir[6][4] = u;
+  o->vir[6][8] = -u;
   o->v_coul += u;
   return u;
 }

@@ -72,6 +72,10 @@ def lib():
             "orc_observe": (None, [vp, dp]),
             "orc_pair_gauss": (C.c_double, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32]),
             "orc_philox": (None, [C.c_uint64, C.c_int64, C.c_uint32, C.c_uint32, P(C.c_uint32)]),
+            "orc_track_force_scale": (None, [vp, C.c_int]),
+            "orc_get_force_scale": (None, [vp, dp]),
+            "orc_get_virial": (None, [vp, dp]),
+            "orc_kinetic_tensor": (None, [vp, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -88,6 +92,8 @@ def _d(a):
 def _i(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int32))
 
+
+VIRIAL_GROUPS = ("pair", "fene", "bend", "orientation", "wall", "kspace", "dipole")
 
 ENERGY_KEYS = ("v_fluid_fluid", "v_fluid_wall", "v_wall_wall", "v_intra_molec", "v_bend", "v_bend_melt",
                "v_or", "v_coul", "t_fluid")
@@ -140,6 +146,27 @@ class Oracle:
         # orc_<routine>(handle) pass-throughs: fluid_fluid, fluid_wall, intra_molec, ...
         f = getattr(lib(), "orc_" + name)
         return lambda *a: f(self.h, *a)
+
+    def track_force_scale(self, on=True):
+        """From the next force evaluation on, sum per particle the magnitudes of every force term
+        acting on it (the conditioning of its force sum); serial pair loop."""
+        self.L.orc_track_force_scale(self.h, 1 if on else 0)
+
+    def force_scale(self):
+        out = np.zeros(self.n)
+        self.L.orc_get_force_scale(self.h, _d(out))
+        return out
+
+    def virial(self):
+        """W_ab = sum of F_a r_b per term group of the last force evaluation (3x3 arrays)."""
+        out = np.zeros(7 * 9)
+        self.L.orc_get_virial(self.h, _d(out))
+        return {g: out[9 * k:9 * k + 9].reshape(3, 3) for k, g in enumerate(VIRIAL_GROUPS)}
+
+    def kinetic_tensor(self):
+        out = np.zeros(9)
+        self.L.orc_kinetic_tensor(self.h, _d(out))
+        return out.reshape(3, 3)
 
     def observe(self):
         """observation.f90 quantities (see orc_observe)."""

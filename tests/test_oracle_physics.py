@@ -131,3 +131,91 @@ def test_explicit_walls_cell_traversal_matches_n2(oracle_mod):
     o.fluid_fluid()
     e_cell, e_n2 = o.energies()["v_fluid_fluid"], o.check_fluid_fluid()
     assert abs(e_cell - e_n2) <= 1e-12 * max(1.0, abs(e_n2))
+
+
+def strained(r0, s, a, b, eps):
+    """Positions and box under the strain r_a -> r_a + eps r_b: for a == b the axis and its box
+    length (or the channel width, walls included) are scaled by 1 + eps."""
+    from mfa_brush_gb300 import abi
+    r = np.array(r0, np.float64).copy()
+    s2 = abi.System.from_buffer_copy(s)
+    if a == b:
+        r[:, a] *= 1.0 + eps
+        s2.boundary[a] = s.boundary[a] * (1.0 + eps)
+    else:
+        r[:, a] += eps * r[:, b]
+    return r, s2
+
+
+@pytest.mark.parametrize("group,which,key", [("pair", "fluid_fluid", "v_fluid_fluid"),
+                                             ("fene", "intra_molec", "v_intra_molec"),
+                                             ("bend", "bending", "v_bend"),
+                                             ("orientation", "orientation", "v_or"),
+                                             ("wall", "fluid_wall", "v_fluid_wall")])
+def test_virial_is_minus_the_strain_derivative(oracle_mod, group, which, key):
+    """W_ab of each group is -dU/de under r_a -> r_a + e r_b (central differences): the diagonal
+    with the box (or the channel width, walls included) scaled, and the x-z and y-z shears."""
+    p, s, a_type, r0, v = small_system(oracle_mod)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    o.zero_force()
+    getattr(o, which)()
+    W = o.virial()[group]
+    h = 1e-6
+    for a, b in ((0, 0), (1, 1), (2, 2), (0, 2), (1, 2)):
+        E = []
+        for e in (h, -h):
+            r, s2 = strained(r0, s, a, b, e)
+            o2 = oracle_mod.Oracle(p, s2, a_type, r, v)
+            o2.zero_force()
+            getattr(o2, which)()
+            E.append(o2.energies()[key])
+            o2.close()
+        fd = -(E[0] - E[1]) / (2 * h)
+        assert abs(fd - W[a, b]) <= 1e-5 * max(1.0, np.abs(W).max()), (group, a, b, fd, W[a, b])
+    if group != "orientation":  # central or rotation-invariant terms: a symmetric tensor
+        assert np.abs(W - W.T).max() <= 1e-9 * max(1.0, np.abs(W).max())
+
+
+def test_ewald_virial_is_minus_the_strain_derivative(oracle_mod):
+    """The same for the charged brush (slab Ewald): real-space Coulomb (pair group), the
+    reciprocal sum and the slab dipole term, each a function of the box as well."""
+    from mfa_brush_gb300 import md
+    inp = configs.wca_inputs(gamma=1.0, thermostat=1)
+    inp.flags.system = 3
+    inp.charge[1], inp.charge[2] = -1.0, 1.0
+    inp.alpha_c, inp.n_kmax, inp.rc_coul = 0.81, 5, 3.0
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.brush_channel(10.0, 10.0, 0.08, 10, rho=0.5, seed=21)
+    rng = np.random.default_rng(2)
+    r0 = r0 + rng.normal(0, 0.05, r0.shape)
+    # a rectangular box (y stretched by 3 %): in the square one several k-vectors sit exactly on
+    # the |k| <= k_c boundary of the k-set rule, and a strain of 1e-6 moves them in or out
+    r0[:, 1] *= 1.03
+    s.boundary[1] *= 1.03
+
+    def energies(sys_, r):
+        o = oracle_mod.Oracle(p, sys_, a_type, r, v)
+        nk = o.ewald_init()
+        o.zero_force()
+        o.fluid_fluid()
+        e = o.energies()
+        u_real = e["v_fluid_fluid"] + e["v_coul"]  # LJ and real-space Coulomb (self term: a constant)
+        u_k = o.ewald_k()
+        u_d = o.dipolar_correction()
+        w = o.virial()
+        o.close()
+        return nk, {"pair": u_real, "kspace": u_k, "dipole": u_d}, w
+
+    nk0, _, W = energies(s, r0)
+    h = 1e-6
+    for a, b in ((0, 0), (1, 1), (2, 2), (0, 2), (1, 2)):
+        (nk1, ep, _), (nk2, em, _) = (energies(*strained(r0, s, a, b, e)[::-1]) for e in (h, -h))
+        assert nk1 == nk2 == nk0
+        # the reciprocal-space formula is the derivative under a deformation of the whole cell;
+        # a shear of the positions alone in an orthorhombic box is not one, so the k-space term
+        # is checked on the diagonal (box scalings) and for symmetry
+        for g in (("pair", "kspace", "dipole") if a == b else ("pair", "dipole")):
+            fd = -(ep[g] - em[g]) / (2 * h)
+            assert abs(fd - W[g][a, b]) <= 1e-5 * max(1.0, np.abs(W[g]).max()), (g, a, b, fd, W[g][a, b])
+    for g in ("pair", "kspace", "dipole"):
+        assert np.abs(W[g] - W[g].T).max() <= 1e-9 * max(1.0, np.abs(W[g]).max())
