@@ -204,6 +204,25 @@ typedef struct mfa_observables {
                                observation.f90:324-327)                                          */
 } mfa_observables;
 
+/* Virial and pressure tensors of one replica (the reference's press_tensor, fluid_fluid.f90:156-166,
+   dpd_forces.f90:118-127, intra_molec.f90:60-67, viscosity.f90:20-33, obser_out.f90:309-318).
+   Every tensor is row-major, w[3 a + b].  A group's virial is minus the derivative of its energy
+   under the strain r_a -> r_a + e r_b of positions and box: for pair, bond and angle terms the sum
+   over the terms of F_a (r_i - r_j)_b with F the force on particle i (the sign of the reference's
+   pair term; its brush-bond term, intra_molec.f90:64, has the opposite sign, which is not
+   reproduced), for the walls each wall's force times the distance from its plane, for the
+   reciprocal-space and slab-dipole energies the derivative of their volume-dependent sums.
+   The pair group holds LJ, DPD (random and dissipative) and real-space Coulomb; the body force
+   of POISEUILLE has no virial.                                                              */
+typedef struct mfa_virial {
+  int64_t step;             /* absolute step of the record                                      */
+  double pair[9], fene[9], bend[9], bend_melt[9], orientation[9], wall[9], kspace[9], dipole[9];
+  double total[9];          /* sum of the groups                                                */
+  double kinetic[9];        /* sum of m v_a v_b over the mobile particles (viscosity.f90:20-27) */
+  double volume;            /* Lx Ly D                                                          */
+  double pressure[9];       /* (kinetic + total) / volume                                       */
+} mfa_virial;
+
 typedef struct mfa_ctx mfa_ctx;
 
 /* ---- library / device ------------------------------------------------------------------ */
@@ -307,6 +326,10 @@ int mfa_sync_to_host(mfa_ctx* ctx, double* r0, double* v, double* a, double* for
 int mfa_set_state(mfa_ctx* ctx, const double* r0, const double* v, const double* a);
 /* Energies of the last energy record, one mfa_energies per replica. */
 int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out);
+/* Virial and pressure tensors of the last energy record, one mfa_virial per replica: the forces
+   and velocities of the record's step (mfa_step every energy_every steps), or the per-routine
+   calls since the last mfa_verlet_velocities (each call replaces its own group).               */
+int mfa_get_virial(mfa_ctx* ctx, mfa_virial* out);
 /* Observation quantities of every replica (one mfa_observables each) on the current state; the
    head forces are those of the last energy record (mfa_step every energy_every steps, or the
    last mfa_verlet_velocities call).                                                           */

@@ -108,6 +108,22 @@ class Observables(C.Structure):
                 "momentum": list(self.momentum), "f_heads": [list(self.f_heads[0]), list(self.f_heads[1])]}
 
 
+VIRIAL_GROUPS = ("pair", "fene", "bend", "bend_melt", "orientation", "wall", "kspace", "dipole")
+
+
+class Virial(C.Structure):
+    _fields_ = ([("step", i64)] + [(g, f64 * 9) for g in VIRIAL_GROUPS] +
+                [("total", f64 * 9), ("kinetic", f64 * 9), ("volume", f64), ("pressure", f64 * 9)])
+
+    def as_dict(self):
+        """3x3 arrays (row-major w[3 a + b] = sum of F_a r_b), plus step and volume."""
+        import numpy as np
+        d = {"step": self.step, "volume": self.volume}
+        for k in VIRIAL_GROUPS + ("total", "kinetic", "pressure"):
+            d[k] = np.array(list(getattr(self, k))).reshape(3, 3)
+        return d
+
+
 P = C.POINTER
 vp = C.c_void_p
 dp = P(f64)
@@ -154,6 +170,7 @@ SIGNATURES = {
     "mfa_get_energies": (i32, [vp, P(Energies)]),
     "mfa_get_profiles": (i32, [vp, i32, dp, dp, dp, P(i64)]),
     "mfa_observe": (i32, [vp, P(Observables)]),
+    "mfa_get_virial": (i32, [vp, P(Virial)]),
     "mfa_list_stats": (i32, [vp, ip, ip]),
     "mfa_kspace_info": (i32, [vp, ip, ip]),
     "mfa_reset_profiles": (i32, [vp]),

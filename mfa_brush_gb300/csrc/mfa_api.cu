@@ -241,6 +241,38 @@ void fill_energies(const mfa_ctx* ctx, const double* acc, int rep, mfa_energies*
   e->inv_n = ctx->hreps[rep].inv_n;
 }
 
+// Virial tensors of record `acc` for replica `rep`: the symmetric groups hold xx yy zz xy xz yz
+// and are mirrored here; the orientation group is a full tensor; the slab-dipole group follows from
+// its energy u: diag(u, u, -u).
+void fill_virial(const mfa_ctx* ctx, const double* acc, int rep, mfa_virial* o) {
+  const int R = ctx->nrep;
+  auto A = [&](int slot) { return acc[(size_t)slot * R + rep]; };
+  std::memset(o, 0, sizeof *o);
+  o->step = ctx->sys[rep].s_time + ctx->host_steps;
+  double* grp[NVIR] = {o->pair, o->fene, o->bend, o->bend_melt, o->orientation, o->wall, o->kspace, o->dipole};
+  for (int g = 0; g < NVIR; ++g) {
+    double* w = grp[g];
+    for (int c = 0; c < 9; ++c) w[c] = A(O_VIR + 9 * g + c);
+    if (g != V_OR)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < a; ++b) w[3 * a + b] = w[3 * b + a];
+  }
+  const bool charged = ctx->P.flags.system == 2 || ctx->P.flags.system == 3;
+  const double ud = charged ? A(O_VDIP) : 0.;
+  std::memset(o->dipole, 0, sizeof o->dipole);
+  o->dipole[0] = o->dipole[4] = ud;
+  o->dipole[8] = -ud;
+  for (int c = 0; c < 9; ++c) o->kinetic[c] = A(O_KIN + c);
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < a; ++b) o->kinetic[3 * a + b] = o->kinetic[3 * b + a];
+  const double* L = ctx->sys[rep].boundary;
+  o->volume = L[0] * L[1] * L[2];
+  for (int c = 0; c < 9; ++c) {
+    for (int g = 0; g < NVIR; ++g) o->total[c] += grp[g][c];
+    o->pressure[c] = (o->kinetic[c] + o->total[c]) / o->volume;
+  }
+}
+
 // ewald_k(0) (ewald_k.f90:37-124): the k-vectors in the reference's enumeration order, G(k),
 // and the list of charged particles (replica 0).
 int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
@@ -361,7 +393,7 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   DA(K.fwin, K.nkchunks);
   DA(K.rho_part, (size_t)K.npchunks * 2 * K.nk);
   DA(K.fpart, (size_t)K.nkchunks * std::max(K.nq, 1) * 3);
-  DA(K.red_part, 2 * KS_RED_MAX);
+  DA(K.red_part, 8 * KS_RED_MAX);
   DA(K.ticket, 2);
   DA(K.qtag, K.nq);
   DA(K.qval, K.nq);
@@ -843,10 +875,12 @@ int mfa_n_particles(const mfa_ctx* ctx, int64_t* n_total, int32_t* n_rep) {
 }
 
 // ---- per-routine drop-ins -------------------------------------------------------------------
-static int zero_call_slot(mfa_ctx* ctx, int slot) {
-  CK(cudaMemsetAsync(ctx->acc_call + (size_t)slot * ctx->nrep, 0, sizeof(double) * ctx->nrep, ctx->st));
+static int zero_call_slot(mfa_ctx* ctx, int slot, int n = 1) {
+  CK(cudaMemsetAsync(ctx->acc_call + (size_t)slot * ctx->nrep, 0, sizeof(double) * ctx->nrep * n, ctx->st));
   return MFA_OK;
 }
+// the 9 virial slots of a group (each drop-in replaces its own group)
+static int zero_call_group(mfa_ctx* ctx, int group) { return zero_call_slot(ctx, O_VIR + 9 * group, 9); }
 
 static int read_call_slot(mfa_ctx* ctx, int slot, double* out, double add_self) {
   if (!out) return MFA_OK;
@@ -895,7 +929,8 @@ int mfa_zero_force(mfa_ctx* ctx) {
 int mfa_fluid_fluid(mfa_ctx* ctx, double* v_ff, double* v_coul) {
   if (!ctx) return MFA_ERR_ARG;
   int r;
-  if ((r = zero_call_slot(ctx, O_VFF)) || (r = zero_call_slot(ctx, O_VCOUL))) return r;
+  if ((r = zero_call_slot(ctx, O_VFF)) || (r = zero_call_slot(ctx, O_VCOUL)) || (r = zero_call_group(ctx, V_PAIR)))
+    return r;
   launch_pair(ctx->S, ctx->C, ctx->st, true, true, acc_of(ctx->acc_call, ctx->nrep), ctx->opt.block_size);
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -910,7 +945,7 @@ int mfa_fluid_fluid(mfa_ctx* ctx, double* v_ff, double* v_coul) {
 int mfa_fluid_wall(mfa_ctx* ctx, int32_t wall_type, double* v_fw) {
   if (!ctx) return MFA_ERR_ARG;
   int r;
-  if ((r = zero_call_slot(ctx, O_VFW))) return r;
+  if ((r = zero_call_slot(ctx, O_VFW)) || (r = zero_call_group(ctx, V_WALL))) return r;
   if (wall_type == 2 && ctx->C.wall == 2) {
     launch_wall(ctx->S, ctx->C, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
     ctx->launches += 1;
@@ -930,7 +965,8 @@ int mfa_wall_wall(mfa_ctx* ctx, int32_t wall_type, double* v_ww) {
 
 static int bonded_call(mfa_ctx* ctx, int mask, int slot, double* out) {
   int r;
-  if ((r = zero_call_slot(ctx, slot))) return r;
+  const int group = mask == 1 ? V_FENE : mask == 2 ? V_BEND : mask == 4 ? V_BENDM : V_OR;
+  if ((r = zero_call_slot(ctx, slot)) || (r = zero_call_group(ctx, group))) return r;
   launch_bonded(ctx->S, ctx->C, ctx->st, mask, true, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -956,7 +992,7 @@ int mfa_ewald_k(mfa_ctx* ctx, int32_t mode, double* v) {
   if (mode == 0) return MFA_OK;
   if (!ctx->kspace) return fail(ctx, MFA_ERR_STATE, "ewald_k: not a charged system");
   int r;
-  if ((r = zero_call_slot(ctx, O_VCOULK))) return r;
+  if ((r = zero_call_slot(ctx, O_VCOULK)) || (r = zero_call_group(ctx, V_KSPACE))) return r;
   launch_kspace(ctx->S, ctx->C, ctx->K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 4;
   CK(cudaGetLastError());
@@ -986,9 +1022,8 @@ int mfa_constant_force(mfa_ctx* ctx, int32_t mode) {
 int mfa_verlet_velocities(mfa_ctx* ctx, mfa_energies* e) {
   if (!ctx) return MFA_ERR_ARG;
   int r;
-  if ((r = zero_call_slot(ctx, O_TFLUID))) return r;
-  for (int k = 0; k < 6; ++k)
-    if ((r = zero_call_slot(ctx, O_FH + k))) return r;
+  if ((r = zero_call_slot(ctx, O_TFLUID)) || (r = zero_call_slot(ctx, O_FH, 6)) || (r = zero_call_slot(ctx, O_KIN, 9)))
+    return r;
   launch_integrate(ctx->S, ctx->C, ctx->st, 1, false, true, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 1;
   CK(cudaGetLastError());
@@ -1252,6 +1287,18 @@ int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out) {
   int r = check_status(ctx);
   if (r) return r;
   for (int k = 0; k < ctx->nrep; ++k) fill_energies(ctx, h.data(), k, &out[k]);
+  return MFA_OK;
+}
+
+int mfa_get_virial(mfa_ctx* ctx, mfa_virial* out) {
+  if (!ctx || !out) return MFA_ERR_ARG;
+  std::vector<double> h(NOBS * ctx->nrep);
+  const double* src = ctx->last_source == 2 ? ctx->acc_call : ctx->rec;
+  CK(cudaMemcpyAsync(h.data(), src, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (r) return r;
+  for (int k = 0; k < ctx->nrep; ++k) fill_virial(ctx, h.data(), k, &out[k]);
   return MFA_OK;
 }
 

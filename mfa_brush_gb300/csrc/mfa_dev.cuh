@@ -21,9 +21,15 @@ namespace mfa {
 
 constexpr int MAXT = 6;
 constexpr int NPAIR = MAXT * MAXT;
-constexpr int NOBS = 17;  // per-replica accumulator slots (energies, head forces)
+// per-replica accumulator slots: energies, head forces, the virial tensor of each term group and the
+// kinetic tensor
 enum Obs { O_VFF = 0, O_VFW, O_VWW, O_VINTRA, O_VBEND, O_VBENDM, O_VOR, O_VCOUL, O_TFLUID, O_VCOULK, O_VDIP,
-           O_FH = 11 /* 6 slots: -sum of head forces, chains 1..n_chain/2 (xyz) then the others */ };
+           O_FH = 11,  /* 6 slots: -sum of head forces, chains 1..n_chain/2 (xyz) then the others */
+           O_VIR = 17, /* NVIR groups x 9 slots: W_ab = sum of F_a r_b at slot O_VIR + 9 g + 3 a + b */
+           O_KIN = O_VIR + 9 * 8, /* 9 slots: sum of m v_a v_b over the mobile particles */
+           NOBS = O_KIN + 9 };
+// virial groups (the terms whose forces they sum)
+enum VirGroup { V_PAIR = 0, V_FENE, V_BEND, V_BENDM, V_OR, V_WALL, V_KSPACE, V_DIP, NVIR };
 
 // status bits
 constexpr unsigned ST_NLIST_OVERFLOW = 1u, ST_OUT_OF_BOX = 2u, ST_NAN = 4u;

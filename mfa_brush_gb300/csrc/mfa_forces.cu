@@ -7,10 +7,12 @@
 //            momentum is conserved exactly in exact arithmetic.  Energies are halved per visit
 //            (a fixed wall bead has no list: its pairs count in full).
 //            MIXED: positions are fixed-point int4 (the int32 difference is the x,y minimum image),
-//            all pair arithmetic is FP32, the per-particle sum is FP32 (the FP32 force array of
-//            the fused step, or added to the FP64 force).  In the fused mixed step the particle's
-//            bonded terms are evaluated by the same thread (BONDED), and with a single cut-off
-//            for every type pair the screening compares against one constant (UNI).
+//            all pair arithmetic is FP32.  In the fused mixed step the FP32 partial sums over each
+//            batch of kept pairs go into an FP64 per-particle total, with the particle's bonded
+//            terms (evaluated by the same thread), its 9-3 wall force and the body force; in the
+//            drop-in the FP32 sum is added to the FP64 force.  With a single cut-off for every
+//            type pair the screening compares against one constant (UNI).  With energies, the
+//            pair, bond, angle and wall virial is summed as well.
 // k_bonded : intra_molec.f90:16-188 (FENE), bending.f90:19-121 / bending_melt.f90:22-108 and
 //            orientation.f90:24-88.  Owner computes: the thread of bead m evaluates every bond,
 //            angle and orientation term that acts on m (terms centred on m-1, m, m+1) and adds
@@ -144,12 +146,28 @@ __device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, cons
   }
 }
 
+// Virial partials of the bonded terms of one particle (EFLAG kernels): FENE, brush and melt
+// bending as symmetric tensors (xx yy zz xy xz yz), orientation as a full one (row-major).
+template <typename T>
+struct BondVir {
+  T fene[6], bend[6], bendm[6], orient[9];
+  __device__ void zero() {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) fene[c] = bend[c] = bendm[c] = 0;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) orient[c] = 0;
+  }
+};
+
 // Bonded force on the mobile particle i (owner computes, see k_bonded); adds to F[3] and, for the
-// terms that i owns, to e[4] = {FENE, brush bending, melt bending, orientation}.  Returns false
-// when i is in no chain of two or more beads.
+// terms that i owns, to e4[4] = {FENE, brush bending, melt bending, orientation}.  With EFLAG the
+// virial goes to bv: half of each of i's bonds (-fac d (x) d, the other half comes from the
+// partner), the whole of the angle centred on i (-f_a (x) r_prev + f_c (x) r_next) and of the
+// orientation term of a head (F_1 (x) (r_1 - r_head)).  Returns false when i is in no chain of two
+// or more beads.
 template <bool MIXED, bool EFLAG>
 __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, int mask, int i, int w,
-                                          real_t<MIXED>* F, real_t<MIXED>* e4) {
+                                          real_t<MIXED>* F, real_t<MIXED>* e4, BondVir<real_t<MIXED>>* bv) {
   using real = real_t<MIXED>;
   const RepDesc& R = s.reps[info_rep(w)];
   int kind = -1, m = 0, n = 0;
@@ -185,6 +203,7 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
         x = x < xm ? x : xm;
         real fac = kc / ((real)1 - x) * ir2;
         F[0] += fac * d[0]; F[1] += fac * d[1]; F[2] += fac * d[2];
+        if (EFLAG) sym_add(bv->fene, (real)-0.5 * fac, d[0], d[1], d[2]);
       }
       if (m < n - 1) {  // bond (m, m+1): first partner; energy counted here
         real d[3];
@@ -193,7 +212,10 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
         x = x < xm ? x : xm;
         real fac = kc / ((real)1 - x) * ir2;
         F[0] -= fac * d[0]; F[1] -= fac * d[1]; F[2] -= fac * d[2];
-        if (EFLAG) e4[0] += kc * ((real)-0.5 * log((real)1 - x));
+        if (EFLAG) {
+          e4[0] += kc * ((real)-0.5 * log((real)1 - x));
+          sym_add(bv->fene, (real)-0.5 * fac, d[0], d[1], d[2]);
+        }
       }
     }
     if (do_bend) {
@@ -209,7 +231,13 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
         if (u == 3) { F[0] += fa[0]; F[1] += fa[1]; F[2] += fa[2]; }
         else if (u == 2) {
           F[0] -= fa[0] + fc[0]; F[1] -= fa[1] + fc[1]; F[2] -= fa[2] + fc[2];
-          if (EFLAG) { if (kind == 0) e4[1] += e; else e4[2] += e; }
+          if (EFLAG) {
+            if (kind == 0) e4[1] += e; else e4[2] += e;
+            real* wb = (kind == 0) ? bv->bend : bv->bendm;
+            const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+            for (int c = 0; c < 6; ++c) wb[c] += fc[ia[c]] * rn[ib[c]] - fa[ia[c]] * rp[ib[c]];
+          }
         } else { F[0] += fc[0]; F[1] += fc[1]; F[2] += fc[2]; }
       }
     }
@@ -259,10 +287,39 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
       const real fm = cst<MIXED>(C.k_or, C.k_or_f) * da;
       const real sgn = (m == 0) ? (real)-1 : (real)1;
       F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
-      if (EFLAG && m == 0) e4[3] += (real)0.5 * fm * da;
+      if (EFLAG && m == 0) {
+        e4[3] += (real)0.5 * fm * da;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) bv->orient[3 * a + b] += fm * dn[a] * rn[b];
+      }
     }
   }
   return true;
+}
+
+// Slots and values of a symmetric tensor (6 components) for obs_push.
+template <typename T>
+__device__ __forceinline__ void sym_slots(int* sl, T* v, int base, const T* w6) {
+  const int idx[6] = {0, 4, 8, 1, 2, 5};
+#pragma unroll
+  for (int c = 0; c < 6; ++c) { sl[c] = base + idx[c]; v[c] = w6[c]; }
+}
+
+// Slots and values of the bonded energies and virial tensors for obs_push (31 of them; terms
+// that are off contribute zeros, which add nothing).
+template <typename T>
+__device__ __forceinline__ void bonded_slots(int* sl, T* v, const T* e4, const BondVir<T>& bv) {
+  sl[0] = O_VINTRA; v[0] = e4[0];
+  sym_slots(sl + 1, v + 1, O_VIR + 9 * V_FENE, bv.fene);
+  sl[7] = O_VBEND; v[7] = e4[1];
+  sym_slots(sl + 8, v + 8, O_VIR + 9 * V_BEND, bv.bend);
+  sl[14] = O_VBENDM; v[14] = e4[2];
+  sym_slots(sl + 15, v + 15, O_VIR + 9 * V_BENDM, bv.bendm);
+  sl[21] = O_VOR; v[21] = e4[3];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) { sl[22 + c] = O_VIR + 9 * V_OR + c; v[22 + c] = bv.orient[c]; }
 }
 
 template <bool MIXED, bool EFLAG>
@@ -274,7 +331,9 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
   const int rep = info_rep(w);
   real F[3] = {0, 0, 0};
   real e4[4] = {0, 0, 0, 0};
-  const bool has = inside && info_mobile(w) && bonded_of<MIXED, EFLAG>(s, C, mask, i, w, F, e4);
+  BondVir<real> bv;
+  if (EFLAG) bv.zero();
+  const bool has = inside && info_mobile(w) && bonded_of<MIXED, EFLAG>(s, C, mask, i, w, F, e4, &bv);
   if (has) {
     if (MIXED && to_f4) {  // fused step: FP32 force array
       float4 f = s.f4[i];
@@ -289,32 +348,72 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
     }
   }
   if (EFLAG) {
-    if (mask & 1) add_obs(acc.col(O_VINTRA), rep, (double)e4[0], has, acc.nrep);
-    if (mask & 2) add_obs(acc.col(O_VBEND), rep, (double)e4[1], has, acc.nrep);
-    if (mask & 4) add_obs(acc.col(O_VBENDM), rep, (double)e4[2], has, acc.nrep);
-    if (mask & 8) add_obs(acc.col(O_VOR), rep, (double)e4[3], has, acc.nrep);
+    int sl[31];
+    real v[31];
+    bonded_slots(sl, v, e4, bv);
+    obs_push<real, 31>(acc, sl, v, rep, has);
   }
 }
 
-// BONDED (fused mixed step only): the particle's bonded force (bonded_of) is added before the
-// FP32 force is stored, which saves the bonded kernel's launch and its read-modify-write of f4.
-// UNI (mixed only): one screening cut-off for every type pair (SimConst::scr2_uni_f).
-template <bool MIXED, bool EFLAG, bool BONDED = false, bool UNI = false>
+// The pair kernel.  Template switches:
+//   MIXED   FP32 pair arithmetic on the fixed-point views (else FP64 throughout);
+//   EFLAG   energies and the virial into the accumulators;
+//   FUSED   the fused mixed-precision step (MIXED only): FP32 partial sums over each batch of kept
+//           pairs are added to an FP64 per-particle total, together with the bonded, wall and body
+//           forces of the particle, and the total is stored (rounded to FP32) in the force array
+//           that the integrator reads;
+//   BONDED  (FUSED only) the particle's bonded terms (bonded_of) in the same thread, which saves
+//           the bonded kernel's launch and its read-modify-write of the force;
+//   UNI     (MIXED only) one screening cut-off for every type pair (SimConst::scr2_uni_f).
+// Without FUSED the forces are added to (accumulate) or stored in the FP64 force arrays.
+// Virial (EFLAG): each visit of a pair adds half of F_ij (x) (r_i - r_j) (the other visit adds the
+// other half); a pair with a fixed wall bead, which has no list of its own, counts in full.
+template <bool MIXED, bool EFLAG, bool FUSED = false, bool BONDED = false, bool UNI = false>
 __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc,
                                                              int bmask = 0) {
   using real = real_t<MIXED>;
+  static_assert(!FUSED || MIXED, "the fused form is the mixed-precision one");
+  static_assert(!BONDED || FUSED, "bonded terms are fused only into the fused form");
   __shared__ PairEntry<real> tab[NPAIR];
+  // FUSED: the particle's FP64 total, in shared memory while the pair loop runs (registers are
+  // scarce there; it is touched once per batch)
+  __shared__ double ftot[FUSED ? 3 : 1][FUSED ? 128 : 1];
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
     if constexpr (MIXED) tab[k] = s.tabf[k]; else tab[k] = s.tabd[k];
   }
-  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool inside = i < s.N;
   const int w = inside ? __ldg(&s.info[i]) : 0;
   const bool active = inside && info_mobile(w);
   const int rep = info_rep(w);
-  real fx = 0, fy = 0, fz = 0;
+  float e_w = 0.f, w_wall = 0.f;  // FUSED: wall energy and virial
+  if constexpr (FUSED) {
+    // the particle's external forces first: its FP64 total starts from them
+    double ez = 0., ex = 0., ey = 0.;
+    if (active) {
+      const int ti = info_type(w);
+      if (C.wall == 2) {  // fluid_wall.f90:96-121 from the FP64 position: distances to both walls
+        const double zd = s.rz[i];
+        const float zl = d2f_fast(zd), zh = d2f_fast(s.reps[rep].L[2] - zd);
+        float fwb, fwt;
+        wall93f_split(C, ti, zl, zh, fwb, fwt, e_w);
+        ez = f2d_fast(fwb) + f2d_fast(fwt);
+        if (EFLAG) w_wall = fwb * zl - fwt * zh;  // each wall's force times z - z_wall
+      }
+      if (C.poiseuille && ti != 0) {  // constant_force.f90:17-21: m g on every non-head bead
+        ex = f2d_fast(C.mass_f[ti] * C.cforce_f[0]);
+        ey = f2d_fast(C.mass_f[ti] * C.cforce_f[1]);
+        ez += f2d_fast(C.mass_f[ti] * C.cforce_f[2]);
+      }
+    }
+    ftot[0][threadIdx.x] = ex;
+    ftot[1][threadIdx.x] = ey;
+    ftot[2][threadIdx.x] = ez;
+  }
+  __syncthreads();
+  real fx = 0, fy = 0, fz = 0;        // the current batch (FUSED), else the whole sum
   real e_lj = 0, e_c = 0;
+  real wv[6] = {0, 0, 0, 0, 0, 0};   // EFLAG: pair virial, xx yy zz xy xz yz
   if (active) {
     const RepDesc& R = s.reps[rep];
     const long long step = R.s_time + *s.steps_done;
@@ -424,6 +523,8 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
         real r2 = r2raw;
         const bool in_lj = r2raw < e.range2;
         real fs = 0;  // force factor along d = r_i - r_j
+        // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
+        const real half = info_mobile(wj) ? (real)0.5 : (real)1;
         if (in_lj) {
           r2 = r2raw < r2min ? r2min : r2raw;
           // MIXED: the hardware reciprocal (2 ulp) instead of the IEEE division sequence
@@ -433,8 +534,7 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
           const real s6 = s2 * s2 * s2;
           const real s12 = s6 * s6;
           fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
-          // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
-          if (EFLAG) e_lj += (info_mobile(wj) ? (real)0.5 : (real)1) * e.eps4 * ((s12 - s6) - e.shift);
+          if (EFLAG) e_lj += half * e.eps4 * ((s12 - s6) - e.shift);
         }
         const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
         if (dpd) {
@@ -478,7 +578,7 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
             const real qq = e.qq;
             const real sqa = cst<MIXED>(C.sqrt_alpha, C.sqrt_alpha_f);
             const real ec = erfc(sqa * r);
-            if (EFLAG) e_c += (info_mobile(wj) ? (real)0.5 : (real)1) * qq * ec * ir;
+            if (EFLAG) e_c += half * qq * ec * ir;
             const real isp = cst<MIXED>(C.inv_sqrt_pi, C.inv_sqrt_pi_f), ac = cst<MIXED>(C.alpha_c, C.alpha_c_f);
             fs += (qq * sqa * isp * (real)2 * exp(-ac * rc2) * ir + qq * ec * ir * ir) * ir;
           }
@@ -486,44 +586,69 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
         fx += fs * dx;
         fy += fs * dy;
         fz += fs * dz;
+        if (EFLAG) sym_add(wv, half * fs, dx, dy, dz);
+      }
+      if constexpr (FUSED) {  // the batch's FP32 partial into the FP64 total
+        ftot[0][threadIdx.x] += f2d_fast(fx);
+        ftot[1][threadIdx.x] += f2d_fast(fy);
+        ftot[2][threadIdx.x] += f2d_fast(fz);
+        fx = fy = fz = 0;
       }
     }
   }
   real eb[4] = {0, 0, 0, 0};
+  // the bonded virial partials of the thread (EFLAG): in shared memory, where the bonded terms'
+  // registers are scarce (27 words per thread: a stride prime to the 32 banks)
+  __shared__ BondVir<real> bvs[(EFLAG && BONDED) ? 128 : 1];
+  BondVir<real>& bv = bvs[(EFLAG && BONDED) ? threadIdx.x : 0];
+  if (EFLAG && BONDED) bv.zero();
   bool hb = false;
-  if constexpr (BONDED) {
+  double fxd = 0., fyd = 0., fzd = 0.;
+  if constexpr (FUSED) {
+    fxd = ftot[0][threadIdx.x];
+    fyd = ftot[1][threadIdx.x];
+    fzd = ftot[2][threadIdx.x];
     if (active) {
-      real fb[3] = {0, 0, 0};
-      hb = bonded_of<MIXED, EFLAG>(s, C, bmask, i, w, fb, eb);
-      fx += fb[0];
-      fy += fb[1];
-      fz += fb[2];
+      if constexpr (BONDED) {
+        real fb[3] = {0, 0, 0};
+        hb = bonded_of<MIXED, EFLAG>(s, C, bmask, i, w, fb, eb, &bv);
+        fxd += f2d_fast(fb[0]);
+        fyd += f2d_fast(fb[1]);
+        fzd += f2d_fast(fb[2]);
+      }
     }
   }
   if (inside) {
-    if (accumulate) {
+    if constexpr (FUSED) {
+      s.f4[i] = make_float4(d2f_fast(fxd), d2f_fast(fyd), d2f_fast(fzd), 0.f);
+    } else if (accumulate) {
       if (active) {
         s.fx[i] += (double)fx;
         s.fy[i] += (double)fy;
         s.fz[i] += (double)fz;
       }
-    } else if constexpr (MIXED) {
-      s.f4[i] = make_float4(fx, fy, fz, 0.f);  // fused step: FP32 forces for the integrator
     } else {
       s.fx[i] = fx;
       s.fy[i] = fy;
       s.fz[i] = fz;
     }
   }
-  if (EFLAG) {
-    add_obs(acc.col(O_VFF), rep, (double)e_lj, active, acc.nrep);
-    if (C.charged) add_obs(acc.col(O_VCOUL), rep, (double)e_c, active, acc.nrep);
+  if (EFLAG) {  // one warp reduction for every energy and virial component of the kernel
+    constexpr int NB = BONDED ? 31 : 0, NW = FUSED ? 2 : 0, NV = 8 + NB + NW;
+    int sl[NV];
+    real v[NV];
+    sl[0] = O_VFF; v[0] = e_lj;
+    sl[1] = O_VCOUL; v[1] = e_c;
+    sym_slots(sl + 2, v + 2, O_VIR + 9 * V_PAIR, wv);
     if constexpr (BONDED) {
-      if (bmask & 1) add_obs(acc.col(O_VINTRA), rep, (double)eb[0], hb, acc.nrep);
-      if (bmask & 2) add_obs(acc.col(O_VBEND), rep, (double)eb[1], hb, acc.nrep);
-      if (bmask & 4) add_obs(acc.col(O_VBENDM), rep, (double)eb[2], hb, acc.nrep);
-      if (bmask & 8) add_obs(acc.col(O_VOR), rep, (double)eb[3], hb, acc.nrep);
+      (void)hb;
+      bonded_slots(sl + 8, v + 8, eb, bv);
     }
+    if constexpr (FUSED) {
+      sl[NV - 2] = O_VFW; v[NV - 2] = e_w;
+      sl[NV - 1] = O_VIR + 9 * V_WALL + 8; v[NV - 1] = w_wall;
+    }
+    obs_push<real, NV>(acc, sl, v, rep, active);
   }
 }
 
@@ -534,22 +659,27 @@ void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool acc
   const int B = (block == 32 || block == 64) ? block : 128;
   const int g = (s.N + B - 1) / B;
   const bool uni = C.scr2_uni_f > 0.f;
-  if (s.mixed && !accumulate && bonded_mask) {
-    if (uni) {
-      if (eflag) k_pair<true, true, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
-      else k_pair<true, false, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+  if (s.mixed && !accumulate) {  // the fused step
+    if (bonded_mask) {
+      if (uni) {
+        if (eflag) k_pair<true, true, true, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
+        else k_pair<true, false, true, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
+      } else {
+        if (eflag) k_pair<true, true, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
+        else k_pair<true, false, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
+      }
     } else {
-      if (eflag) k_pair<true, true, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
-      else k_pair<true, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc, bonded_mask);
+      if (uni) {
+        if (eflag) k_pair<true, true, true, false, true><<<g, B, 0, st>>>(s, C, false, acc);
+        else k_pair<true, false, true, false, true><<<g, B, 0, st>>>(s, C, false, acc);
+      } else {
+        if (eflag) k_pair<true, true, true><<<g, B, 0, st>>>(s, C, false, acc);
+        else k_pair<true, false, true><<<g, B, 0, st>>>(s, C, false, acc);
+      }
     }
-  } else if (s.mixed) {
-    if (uni) {
-      if (eflag) k_pair<true, true, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
-      else k_pair<true, false, false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
-    } else {
-      if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
-      else k_pair<true, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
-    }
+  } else if (s.mixed) {  // the drop-in: added to the FP64 force
+    if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, true, acc);
+    else k_pair<true, false><<<g, B, 0, st>>>(s, C, true, acc);
   } else {
     if (eflag) k_pair<false, true><<<g, B, 0, st>>>(s, C, accumulate, acc);
     else k_pair<false, false><<<g, B, 0, st>>>(s, C, accumulate, acc);
@@ -578,12 +708,20 @@ __global__ void k_wall(DevState s, SimConst C, Acc acc) {
   const bool inside = i < s.N;
   const int w = inside ? s.info[i] : 0;
   const bool active = inside && info_mobile(w);
-  double e = 0.;
+  double e = 0., wzz = 0.;
   if (active) {
     const RepDesc& R = s.reps[info_rep(w)];
-    s.fz[i] += wall93(C, info_type(w), s.rz[i], R.L[2], e);
+    const double z = s.rz[i];
+    double fb, ft;
+    wall93_split(C, info_type(w), z, R.L[2], fb, ft, e);
+    s.fz[i] += fb + ft;
+    wzz = fb * z + ft * (z - R.L[2]);  // each wall's force times z - z_wall
   }
-  if (EFLAG) add_obs(acc.col(O_VFW), info_rep(w), e, active, acc.nrep);
+  if (EFLAG) {
+    const int sl[2] = {O_VFW, O_VIR + 9 * V_WALL + 8};
+    const double v[2] = {e, wzz};
+    obs_push<double, 2>(acc, sl, v, info_rep(w), active);
+  }
 }
 
 void launch_wall(const DevState& s, const SimConst& C, cudaStream_t st, bool eflag, Acc acc) {

@@ -10,7 +10,9 @@
 //   MODE 2  MODE 1 of step n followed by MODE 0 of step n+1 in one pass (the fused step): one
 //           read of r, v, F and one write of r, v and the views per particle per step.
 //   add_ext adds the 9-3 wall force (fluid_wall.f90:96-121) and the body force
-//           (constant_force.f90:17-21) inside the kernel instead of separate passes.
+//           (constant_force.f90:17-21) inside the kernel instead of separate passes (FP64 step;
+//           the mixed step adds them in the pair kernel).  With energies: the kinetic energy and
+//           the kinetic tensor sum m v (x) v (viscosity.f90:20-27) of v(n).
 // All integration is FP64 in both precision modes.
 #include "mfa_state.cuh"
 
@@ -38,7 +40,8 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
   const int w = inside ? s.info[i] : 0;
   const bool mob = inside && info_mobile(w);
   const int rep = info_rep(w);
-  double ke = 0., efw = 0.;
+  double ke = 0., efw = 0., wzz = 0.;
+  double kin[6] = {0., 0., 0., 0., 0., 0.};  // m v (x) v: xx yy zz xy xz yz
   double fh[6] = {0., 0., 0., 0., 0., 0.};  // minus the head force, by half of the chains
   if (mob) {
     const RepDesc& R = s.reps[rep];
@@ -50,9 +53,11 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       double Fx = s.fx[i], Fy = s.fy[i], Fz = s.fz[i];
       if (ADDEXT) {
         if (C.wall == 2) {
-          double e;
-          Fz += wall93(C, t, z, R.L[2], e);
+          double e, fb, ft;
+          wall93_split(C, t, z, R.L[2], fb, ft, e);
+          Fz += fb + ft;
           efw = e;
+          wzz = fb * z + ft * (z - R.L[2]);  // each wall's force times z - z_wall
         }
         if (C.poiseuille && t != 0) {
           const double m = C.mass[t];
@@ -75,7 +80,10 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
         ax = ay = az = 0.;
         if (MODE == 1) { s.fx[i] = 0.; s.fy[i] = 0.; s.fz[i] = 0.; }
       }
-      if (EFLAG) ke = 0.5 * C.mass[t] * (vx * vx + vy * vy + vz * vz);
+      if (EFLAG) {
+        ke = 0.5 * C.mass[t] * (vx * vx + vy * vy + vz * vz);
+        sym_add(kin, C.mass[t], vx, vy, vz);
+      }
       if (MODE == 1) {
         s.ax[i] = ax; s.ay[i] = ay; s.az[i] = az;
         s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
@@ -106,23 +114,18 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
   }
   if (MODE >= 1 && i == 0) *s.steps_done += 1;
   if (EFLAG && MODE >= 1) {
-    add_obs(acc.col(O_TFLUID), rep, ke, mob, acc.nrep);
-    if (ADDEXT && C.wall == 2) add_obs(acc.col(O_VFW), rep, efw, mob, acc.nrep);
-    for (int k = 0; k < 6; ++k) add_obs(acc.col(O_FH + k), rep, fh[k], mob, acc.nrep);
+    int sl[15];
+    double v[15];
+    sl[0] = O_TFLUID; v[0] = ke;
+    const int idx[6] = {0, 4, 8, 1, 2, 5};
+    for (int c = 0; c < 6; ++c) {
+      sl[1 + c] = O_KIN + idx[c]; v[1 + c] = kin[c];
+      sl[7 + c] = O_FH + c; v[7 + c] = fh[c];
+    }
+    sl[13] = O_VFW; v[13] = efw;  // zero unless ADDEXT with implicit walls
+    sl[14] = O_VIR + 9 * V_WALL + 8; v[14] = wzz;
+    obs_push<double, 15>(acc, sl, v, rep, mob);
   }
-}
-
-// FP32 9-3 walls from the FP32 distances to the bottom (zl) and top (zh) wall; 9|A| s^9 z^-10 =
-// 9|A| (s/z)^9 / z, 3 A s^3 z^-4 = 3 A (s/z)^3 / z.
-__device__ __forceinline__ float wall93f(const SimConst& C, int t, float zl, float zh, float& e) {
-  const float sw = C.sigma_wall_f[t], awt = C.a_wall_f[t], aw = fabsf(awt), a_w = C.a_w_f;
-  float iz = 1.f / zl, rd = sw * iz, rd3 = rd * rd * rd, rd9 = rd3 * rd3 * rd3;
-  e = aw * rd9 - a_w * rd3;
-  float f = (9.f * aw * rd9 - 3.f * awt * rd3) * iz;
-  iz = 1.f / zh; rd = sw * iz; rd3 = rd * rd * rd; rd9 = rd3 * rd3 * rd3;
-  e += aw * rd9 - a_w * rd3;
-  f -= (9.f * aw * rd9 - 3.f * awt * rd3) * iz;
-  return f;
 }
 
 // x -> wrapped x of verlet_positions.f90:170-186 (`> L` then `< 0`), decided on the bit pattern:
@@ -143,10 +146,10 @@ __device__ __forceinline__ double wrap_bits(double x, double L, long long Lbits)
 //   MODE 2  both at once: v(n-1/2) -> v(n+1/2) with one FP64 add of dt a(n), r += dt v(n+1/2),
 //           equal in exact arithmetic to MODE 1 followed by MODE 0; kinetic energy from
 //           v(n) = v(n+1/2) - dt/2 a.
-// r + dt v + dt^2/2 a is formed as r + dt (v + dt/2 a).  Forces, accelerations, wall and body
-// forces and velocity increments are FP32; r and v stay FP64.  FUSED reads the FP32 force array
-// of the fused step and adds the 9-3 walls and the body force; otherwise the FP64 force array of
-// the per-routine path is used as is.  Conversions use the integer forms of mfa_dev.cuh.
+// r + dt v + dt^2/2 a is formed as r + dt (v + dt/2 a).  Accelerations and velocity increments
+// are FP32; r and v stay FP64.  FUSED reads the force of the fused step (the pair kernel's total,
+// walls and body force included, rounded to FP32); otherwise the FP64 force array of the
+// per-routine path.  Conversions use the integer forms of mfa_dev.cuh.
 template <int MODE, bool EFLAG, bool FUSED>
 __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc acc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -154,7 +157,8 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
   const int w = inside ? s.info[i] : 0;
   const bool mob = inside && info_mobile(w);
   const int rep = info_rep(w);
-  float ke = 0.f, efw = 0.f;
+  float ke = 0.f;
+  float kin[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // m v (x) v: xx yy zz xy xz yz
   float fh[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // minus the head force, by half of the chains
   if (mob) {
     const RepDesc& R = s.reps[rep];
@@ -167,16 +171,6 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
       if (FUSED) {
         const float4 F4 = s.f4[i];
         Fx = F4.x; Fy = F4.y; Fz = F4.z;
-        if (C.wall == 2) {
-          float e;
-          Fz += wall93f(C, t, d2f_fast(z), d2f_fast(R.L[2] - z), e);
-          efw = e;
-        }
-        if (C.poiseuille && t != 0) {
-          Fx += C.mass_f[t] * C.cforce_f[0];
-          Fy += C.mass_f[t] * C.cforce_f[1];
-          Fz += C.mass_f[t] * C.cforce_f[2];
-        }
       } else {
         Fx = d2f_fast(s.fx[i]); Fy = d2f_fast(s.fy[i]); Fz = d2f_fast(s.fz[i]);
       }
@@ -200,6 +194,7 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
       const float c = (MODE == 2) ? 0.5f : 1.0f;  // v(n) = v + dv/2 (MODE 2) or v + dv (MODE 1)
       const float ux = d2f_fast(vx) + c * dvx, uy = d2f_fast(vy) + c * dvy, uz = d2f_fast(vz) + c * dvz;
       ke = 0.5f * C.mass_f[t] * (ux * ux + uy * uy + uz * uz);
+      sym_add(kin, C.mass_f[t], ux, uy, uz);
     }
     vx += f2d_fast(dvx);
     vy += f2d_fast(dvy);
@@ -231,9 +226,15 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
   }
   if (MODE >= 1 && i == 0) *s.steps_done += 1;
   if (EFLAG && MODE >= 1) {
-    add_obs(acc.col(O_TFLUID), rep, (double)ke, mob, acc.nrep);
-    if (FUSED && C.wall == 2) add_obs(acc.col(O_VFW), rep, (double)efw, mob, acc.nrep);
-    for (int k = 0; k < 6; ++k) add_obs(acc.col(O_FH + k), rep, (double)fh[k], mob, acc.nrep);
+    int sl[13];
+    float v[13];
+    sl[0] = O_TFLUID; v[0] = ke;
+    const int idx[6] = {0, 4, 8, 1, 2, 5};
+    for (int c = 0; c < 6; ++c) {
+      sl[1 + c] = O_KIN + idx[c]; v[1 + c] = kin[c];
+      sl[7 + c] = O_FH + c; v[7 + c] = fh[c];
+    }
+    obs_push<float, 13>(acc, sl, v, rep, mob);
   }
 }
 

@@ -261,13 +261,48 @@ __device__ __forceinline__ bool grid_sum_last(double v, double* part, unsigned* 
   return true;
 }
 
+// The same for NV values at once; part holds gridDim.x x NV partials.
+template <int NV>
+__device__ __forceinline__ bool grid_sum_last_n(const double* v, double* part, unsigned* ticket, double* total) {
+  __shared__ double red[32];
+  __shared__ bool last;
+  double b[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) b[c] = block_sum(v[c], red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < NV; ++c) part[(size_t)blockIdx.x * NV + c] = b[c];
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double t[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) t[c] = 0.;
+  for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < NV; ++c) t[c] += ((volatile double*)part)[(size_t)k * NV + c];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) t[c] = block_sum(t[c], red);
+  if (threadIdx.x != 0) return false;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) total[c] = t[c];
+  *ticket = 0u;  // ready for the next launch
+  return true;
+}
+
 // Thread (k, g) of a block of 32 k x 8 groups sums the chunk partials c = g, g + 8, ..; the
-// eight group sums are then added in group order: a fixed order for every k.
+// eight group sums are then added in group order: a fixed order for every k.  With energies, the
+// reciprocal-space virial sum over k of u_k (delta_ab - 2 k_a k_b (1/k^2 + 1/(4 alpha_c))) as well
+// (u_k = G |rho|^2, the k's term of the energy), the derivative of the energy under a deformation
+// of the cell.
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, Acc acc, bool eflag) {
+__global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, double fac_alpha, Acc acc, bool eflag) {
   __shared__ double2 part[8][32];
   const int kl = threadIdx.x & 31, g = threadIdx.x >> 5;
-  double u = 0.;
+  double u[7] = {0., 0., 0., 0., 0., 0., 0.};  // energy, then the virial xx yy zz xy xz yz
   const int nkb = (K.nk + 31) / 32;
   for (int kb = blockIdx.x; kb < nkb; kb += gridDim.x) {
     const int k = kb * 32 + kl;
@@ -291,7 +326,18 @@ __global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, Acc ac
         im += part[h][kl].y;
       }
       const double G = K.kfac[k];
-      u += G * (re * re + im * im);
+      const double uk = G * (re * re + im * im);
+      u[0] += uk;
+      if (eflag) {
+        const double kx = K.kvec[3 * k], ky = K.kvec[3 * k + 1], kz = K.kvec[3 * k + 2];
+        const double c = 2. * (1. / (kx * kx + ky * ky + kz * kz) + fac_alpha) * uk;
+        u[1] += uk - c * kx * kx;
+        u[2] += uk - c * ky * ky;
+        u[3] += uk - c * kz * kz;
+        u[4] -= c * kx * ky;
+        u[5] -= c * kx * kz;
+        u[6] -= c * ky * kz;
+      }
       if constexpr (MIXED) {
         const double kx = K.kvec[3 * k], a = G * re, b = G * im;
         const int xi = K.kn[k].x + K.nxm;
@@ -304,8 +350,13 @@ __global__ void __launch_bounds__(256) k_ks_rho_sum(KSpace K, double pi4, Acc ac
     }
     __syncthreads();
   }
-  double tot;
-  if (grid_sum_last(u, K.red_part, K.ticket, tot) && eflag) acc.col(O_VCOULK)[K.rep] += tot * pi4 * K.inv_V;
+  double tot[7];
+  if (grid_sum_last_n<7>(u, K.red_part, K.ticket, tot) && eflag) {
+    const double sc = pi4 * K.inv_V;
+    acc.col(O_VCOULK)[K.rep] += tot[0] * sc;
+    const int idx[6] = {0, 4, 8, 1, 2, 5};
+    for (int c = 0; c < 6; ++c) acc.col(O_VIR + 9 * V_KSPACE + idx[c])[K.rep] += tot[1 + c] * sc;
+  }
 }
 
 template <bool MIXED>
@@ -576,8 +627,9 @@ void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaSt
   if (s.mixed) k_ks_rho<true><<<g1, KS_RHO_T, shm1, st>>>(K);
   else k_ks_rho<false><<<g1, KS_RHO_T, shm1, st>>>(K);
   const int gs = std::min(KS_RED_MAX, (K.nk + 31) / 32);
-  if (s.mixed) k_ks_rho_sum<true><<<gs, 256, 0, st>>>(K, 4. * pi, acc, eflag);
-  else k_ks_rho_sum<false><<<gs, 256, 0, st>>>(K, 4. * pi, acc, eflag);
+  const double fac_alpha = 1. / (4. * C.alpha_c);
+  if (s.mixed) k_ks_rho_sum<true><<<gs, 256, 0, st>>>(K, 4. * pi, fac_alpha, acc, eflag);
+  else k_ks_rho_sum<false><<<gs, 256, 0, st>>>(K, 4. * pi, fac_alpha, acc, eflag);
   const dim3 g2((K.nq + KS_FB - 1) / KS_FB, K.nkchunks);
   if (use_dense(K, s.mixed)) {
     kDense[K.qx](K, g2, st);
@@ -596,7 +648,7 @@ __global__ void __launch_bounds__(256) k_ks_dipole(DevState s, KSpace K, double 
     m += K.qval[p] * (s.rz[i] - K.lz_half);
   }
   double tot;
-  if (grid_sum_last(m, K.red_part + KS_RED_MAX, K.ticket + 1, tot)) {
+  if (grid_sum_last(m, K.red_part + 7 * KS_RED_MAX, K.ticket + 1, tot)) {
     K.mz[0] = tot;
     if (eflag) acc.col(O_VDIP)[K.rep] += 2. * pi * tot * tot * K.inv_V;
   }

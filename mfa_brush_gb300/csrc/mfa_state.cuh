@@ -49,6 +49,74 @@ struct Acc {
   __host__ __device__ double* col(int slot) const { return a + (size_t)slot * nrep; }
 };
 
+// Adds NV per-thread values v[c] into the accumulator columns slot[c] at the thread's replica.
+// All 32 lanes of the warp must call it (inactive lanes add nothing).  When every active lane of
+// the warp belongs to one replica (the common case: particles are sorted by replica), the warp
+// sums all values at once by a transpose reduction in T (each of 5 exchange rounds halves the
+// values a lane holds: 31 shuffles for 32 values, after which lane c holds the sum of value c) and
+// lane c adds it to its column with one FP64 atomic; otherwise each value takes add_obs.
+// (T = float in the mixed-precision kernels: the warp sums run on the FP32 pipe, not on the
+// FP64 one, which GB300 issues at 1/64 of the FP32 rate.)
+template <typename T, int NV>
+__device__ __forceinline__ void obs_push(const Acc& acc, const int (&slot)[NV], const T (&v)[NV], int rep,
+                                         bool active) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(FULL, active);
+  if (!act) return;
+  const int r0 = __shfl_sync(FULL, rep, __ffs(act) - 1);
+  if (__all_sync(FULL, !active || rep == r0)) {
+#pragma unroll
+    for (int base = 0; base < NV; base += 32) {
+      T u[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) u[c] = (active && base + c < NV) ? v[base + c < NV ? base + c : 0] : T(0);
+#pragma unroll
+      for (int off = 16; off >= 1; off >>= 1) {
+        const bool up = (lane & off) != 0;
+#pragma unroll
+        for (int j = 0; j < off; ++j) {
+          const T send = up ? u[j] : u[j + off];
+          const T keep = up ? u[j + off] : u[j];
+          u[j] = keep + __shfl_xor_sync(FULL, send, off);
+        }
+      }
+      int sl = -1;
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        if (c == lane && base + c < NV) sl = slot[base + c];
+      const double t = (double)u[0];
+      if (sl >= 0 && t != 0.) atomicAdd(acc.col(sl) + r0, t);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < NV; ++c) add_obs(acc.col(slot[c]), rep, (double)v[c], active, acc.nrep);
+  }
+}
+
+// A symmetric tensor into the 9 slots from `base` (a virial group O_VIR + 9 g, or O_KIN): six
+// components xx yy zz xy xz yz, the host mirrors them to yx zx zy.  One add_obs per component, so
+// all 32 lanes of the warp must call it.
+template <typename T>
+__device__ __forceinline__ void add_obs_sym(const Acc& acc, int base, int rep, const T* w6, bool active) {
+  const int idx[6] = {0, 4, 8, 1, 2, 5};
+#pragma unroll
+  for (int c = 0; c < 6; ++c) add_obs(acc.col(base + idx[c]), rep, (double)w6[c], active, acc.nrep);
+}
+// A general tensor (9 components, row-major a b).
+template <typename T>
+__device__ __forceinline__ void add_obs9(const Acc& acc, int base, int rep, const T* w9, bool active) {
+#pragma unroll
+  for (int c = 0; c < 9; ++c) add_obs(acc.col(base + c), rep, (double)w9[c], active, acc.nrep);
+}
+// w6 += c d (x) d (symmetric, xx yy zz xy xz yz)
+template <typename T>
+__device__ __forceinline__ void sym_add(T* w6, T c, T dx, T dy, T dz) {
+  const T cx = c * dx, cy = c * dy;
+  w6[0] += cx * dx; w6[1] += cy * dy; w6[2] += c * dz * dz;
+  w6[3] += cx * dy; w6[4] += cx * dz; w6[5] += cy * dz;
+}
+
 // ---- rebuild (cell sort + neighbour list); `force` runs it even when the flag is clear -------
 void launch_rebuild(const DevState& s, cudaStream_t st, bool force);
 // largest neighbour-list capacity (entries per particle) a context may grow to
@@ -128,7 +196,7 @@ struct KSpace {
   int* chunk_row;       // [nkchunks+1] first row of each chunk
   double* fpart;        // [nkchunks][nq][3] per-chunk force partials, summed in a fixed order
   // deterministic grid reductions: per-block partials, the last block to finish sums them
-  double* red_part;     // [2*KS_RED_MAX]: rho_sum energy, dipole moment
+  double* red_part;     // [8*KS_RED_MAX]: rho_sum energy and virial (7 per block), dipole moment
   unsigned* ticket;     // [2] zero between launches
   int rep;
   int plain;            // 1: FP32 sums without Kahan compensation (mfa_options.kspace_plain_sums)
@@ -149,24 +217,43 @@ void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaSt
 void launch_dipolar(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
                     bool fused = false);
 
-// implicit 9-3 walls (fluid_wall.f90:93-121): returns F_z, e = energy of both walls
-__device__ __forceinline__ double wall93(const SimConst& C, int t, double z, double D, double& e) {
+// implicit 9-3 walls (fluid_wall.f90:93-121): the bottom wall's F_z in fb, the top wall's in ft,
+// e = energy of both walls
+__device__ __forceinline__ void wall93_split(const SimConst& C, int t, double z, double D, double& fb, double& ft,
+                                             double& e) {
   const double sw = C.sigma_wall[t], awt = C.a_wall[t], aw = fabs(awt);
   const double sw3 = sw * sw * sw, sw9 = sw3 * sw3 * sw3;
-  double f = 0.;
   double iz = 1. / z;
   double iz2 = iz * iz, iz4 = iz2 * iz2, iz8 = iz4 * iz4, iz10 = iz8 * iz2;
   double rd = sw * iz, rd3 = rd * rd * rd, rd9 = rd3 * rd3 * rd3;
   e = aw * rd9 - C.a_w * rd3;
-  f += 9. * aw * sw9 * iz10;
-  f -= 3. * awt * sw3 * iz4;
+  fb = 9. * aw * sw9 * iz10;
+  fb -= 3. * awt * sw3 * iz4;
   iz = 1. / (D - z);
   iz2 = iz * iz; iz4 = iz2 * iz2; iz8 = iz4 * iz4; iz10 = iz8 * iz2;
   rd = sw * iz; rd3 = rd * rd * rd; rd9 = rd3 * rd3 * rd3;
   e += aw * rd9 - C.a_w * rd3;
-  f -= 9. * aw * sw9 * iz10;
-  f += 3. * awt * sw3 * iz4;
-  return f;
+  ft = -9. * aw * sw9 * iz10;
+  ft += 3. * awt * sw3 * iz4;
+}
+
+__device__ __forceinline__ double wall93(const SimConst& C, int t, double z, double D, double& e) {
+  double fb, ft;
+  wall93_split(C, t, z, D, fb, ft, e);
+  return fb + ft;
+}
+
+// The same in FP32 from the distances to the bottom (zl) and top (zh) wall; 9|A| s^9 z^-10 =
+// 9|A| (s/z)^9 / z, 3 A s^3 z^-4 = 3 A (s/z)^3 / z.
+__device__ __forceinline__ void wall93f_split(const SimConst& C, int t, float zl, float zh, float& fb, float& ft,
+                                              float& e) {
+  const float sw = C.sigma_wall_f[t], awt = C.a_wall_f[t], aw = fabsf(awt), a_w = C.a_w_f;
+  float iz = 1.f / zl, rd = sw * iz, rd3 = rd * rd * rd, rd9 = rd3 * rd3 * rd3;
+  e = aw * rd9 - a_w * rd3;
+  fb = (9.f * aw * rd9 - 3.f * awt * rd3) * iz;
+  iz = 1.f / zh; rd = sw * iz; rd3 = rd * rd * rd; rd9 = rd3 * rd3 * rd3;
+  e += aw * rd9 - a_w * rd3;
+  ft = -(9.f * aw * rd9 - 3.f * awt * rd3) * iz;
 }
 
 }  // namespace mfa

@@ -252,6 +252,13 @@ class MdSystem:
         self._ck(self.lib.mfa_kspace_info(self.ctx, C.byref(nk), C.byref(nq)))
         return nk.value, nq.value
 
+    def virial(self):
+        """Virial tensors per term group, kinetic and pressure tensors of every replica, from the
+        last energy record (see mfa_get_virial); a list of dicts of 3x3 arrays."""
+        o = (abi.Virial * self.nrep)()
+        self._ck(self.lib.mfa_get_virial(self.ctx, o))
+        return [x.as_dict() for x in o]
+
     def observe(self):
         """observation.f90 quantities of every replica: Rg^2 (brush, melt), momentum, head forces."""
         o = (abi.Observables * self.nrep)()

@@ -310,10 +310,10 @@ typedef struct orc_sys {
      walls and positions deformed together).  For the pair, bond, angle and wall terms that is the
      sum over the terms of F_a r_b (F on a particle, r its position relative to the other
      particles of the term, or to the wall plane); the k-space and slab-dipole energies depend on
-     the volume as well.  Groups: 0 pair (LJ + DPD + real-space Coulomb), 1 FENE, 2 bending (brush
-     and melt), 3 orientation, 4 walls (zz), 5 k-space, 6 slab dipole; each routine sets its own
-     group (bending and melt bending share theirs, cleared with the forces) */
-  double vir[7][9];
+     the volume as well.  Groups: 0 pair (LJ + DPD + real-space Coulomb), 1 FENE, 2 brush bending,
+     3 melt bending, 4 orientation, 5 walls (zz), 6 k-space, 7 slab dipole; each routine sets its
+     own group */
+  double vir[8][9];
   /* per-particle force scale: the sum of the magnitudes of every force term acting on the
      particle (NULL unless enabled by orc_track_force_scale) */
   double* fscale;
@@ -626,7 +626,7 @@ void orc_get_force_scale(const orc_sys* o, double* out) {
   if (o->fscale) memcpy(out, o->fscale, (size_t)o->n * 8);
   else memset(out, 0, (size_t)o->n * 8);
 }
-/* out[9 g + 3 a + b] = W_ab of group g (7 groups, see orc_sys::vir) */
+/* out[9 g + 3 a + b] = W_ab of group g (8 groups, see orc_sys::vir) */
 void orc_get_virial(const orc_sys* o, double* out) { memcpy(out, o->vir, sizeof o->vir); }
 /* Kinetic tensor sum m v_a v_b over the mobile particles (viscosity.f90:20-27). */
 void orc_kinetic_tensor(const orc_sys* o, double* out) {
@@ -641,6 +641,20 @@ void orc_kinetic_tensor(const orc_sys* o, double* out) {
  * fi accumulates the LJ force on i (f_ipart); force_tmp receives the DPD and Coulomb terms on
  * i and j, and the LJ reaction on j.  Returns nothing; energies via pointers.
  * ---------------------------------------------------------------------------------------- */
+/* Force scale of a DPD pair (1-based i, j): the random and dissipative terms at unit weight,
+ * sigma |g| and gamma (|v_i| + |v_j|).  The weight 1 - r/r_c is itself a difference of numbers of
+ * order one, so the error of either term does not shrink with the weight. */
+static inline void dpd_scale(const orc_sys* o, int i, int j, double g) {
+  if (!o->fscale) return;
+  const double* vi = &o->v[3 * (i - 1)];
+  const double* vj = &o->v[3 * (j - 1)];
+  const double m = o->p.sig * fabs(g) +
+                   o->p.friction1 * (sqrt(vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2]) +
+                                     sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]));
+  o->fscale[i - 1] += m;
+  o->fscale[j - 1] += m;
+}
+
 static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* force_tmp,
                            double* v_ff, double* v_coul, double* w) {
   const mfa_params* p = &o->p;
@@ -674,8 +688,10 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
     {
       double f[3] = {-rd * dr[0], -rd * dr[1], -rd * dr[2]};
       vir_add(w, f, dr);
-      fsc(o, i - 1, f);
-      fsc(o, j - 1, f);
+      /* scale: the repulsive and attractive parts before they cancel */
+      const double m = fabs(l_eps) * (12 * r_12 + 6 * r_6) * inv_r_2 * sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+      fsc_mag(o, i - 1, m);
+      fsc_mag(o, j - 1, m);
     }
     int wall_pair = p->flags.wall == 1 && (ti == p->n_type - 1 || tj == p->n_type - 1);
     if (dpd && p->r_cut_dpd_2 == 0. && !wall_pair) { /* DPD inside the LJ range (dpd_forces.f90:45-53) */
@@ -699,10 +715,7 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
         fij[d] = fr + fd;
       }
       vir_add(w, fij, dr);
-      fsc_mag(o, i - 1, p->sig * w_r * g);
-      fsc_mag(o, j - 1, p->sig * w_r * g);
-      fsc_mag(o, i - 1, p->friction1 * w_d * rdot);
-      fsc_mag(o, j - 1, p->friction1 * w_d * rdot);
+      dpd_scale(o, i, j, g);
     }
   }
   /* real-space Ewald (ewald_real.f90:15-33) */
@@ -754,10 +767,7 @@ static inline void pair_ij(const orc_sys* o, int i, int j, double* fi, double* f
         fij[d] = fr + fd;
       }
       vir_add(w, fij, dr);
-      fsc_mag(o, i - 1, p->sig * w_r * g);
-      fsc_mag(o, j - 1, p->sig * w_r * g);
-      fsc_mag(o, i - 1, p->friction1 * w_d * rdot);
-      fsc_mag(o, j - 1, p->friction1 * w_d * rdot);
+      dpd_scale(o, i, j, g);
     }
   }
 }
@@ -908,7 +918,7 @@ void orc_fluid_wall(orc_sys* o) {
   const mfa_params* p = &o->p;
   double vfw = 0.;
   double D = o->s.boundary[2];
-  memset(o->vir[4], 0, 9 * sizeof(double));
+  memset(o->vir[5], 0, 9 * sizeof(double));
   if (p->flags.wall == 2) {
     for (int i = 0; i < o->nm; ++i) {
       int t = o->a_type[i] - 1;
@@ -929,9 +939,11 @@ void orc_fluid_wall(orc_sys* o) {
       o->force[3 * i + 2] += 3 * p->a_wall[t] * ipow(sw, 3) * ipow(inv_z, 4);
       const double ft = o->force[3 * i + 2] - f1;   /* the top wall's */
       /* each wall's force times the distance vector from the wall plane */
-      o->vir[4][8] += fb * z + ft * (z - D);
-      fsc_mag(o, i, fb);
-      fsc_mag(o, i, ft);
+      o->vir[5][8] += fb * z + ft * (z - D);
+      /* scale: both parts of each wall's force, times 10 (the force goes as z^-10, so a relative
+         error of the distance is amplified tenfold) */
+      fsc_mag(o, i, 10. * (9. * aw * ipow(sw, 9) * (ipow(1. / z, 10) + ipow(inv_z, 10)) +
+                           3. * fabs(p->a_wall[t]) * ipow(sw, 3) * (ipow(1. / z, 4) + ipow(inv_z, 4))));
     }
   }
   o->v_fw = vfw;
@@ -965,8 +977,10 @@ static double fene_bond(orc_sys* o, int ip, int jp, int z_pbc) {
   }
   double f[3] = {-rd * dr[0], -rd * dr[1], -rd * dr[2]};  /* on ip; dr = r_ip - r_jp */
   vir_add(o->vir[1], f, dr);
-  fsc(o, ip, f);
-  fsc(o, jp, f);
+  /* scale: the force over 1 - x (the condition of 1/(1 - x) near full stretch) */
+  const double m = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]) / (1. - x);
+  fsc_mag(o, ip, m);
+  fsc_mag(o, jp, m);
   return pot;
 }
 
@@ -1004,7 +1018,7 @@ static double norm2v(const double* x) { return sqrt(x[0] * x[0] + x[1] * x[1] + 
 /* One bending term (bending.f90:30-109) for the triplet (a, b, c), 0-based, with r_prev =
  * r_b - r_a and r_next = r_c - r_b already min-imaged.  Returns the energy. */
 static double bend_term(orc_sys* o, int ia, int ib, int ic, const double* r_prev, const double* r_next,
-                        double k_b, double a_eq, int form) {
+                        double k_b, double a_eq, int form, double* w) {
   double dot = 0, rp2 = 0, rn2 = 0, dp2 = 0, dn2 = 0;
   for (int j = 0; j < 3; ++j) {
     dot += r_next[j] * r_prev[j];
@@ -1056,16 +1070,19 @@ static double bend_term(orc_sys* o, int ia, int ib, int ic, const double* r_prev
     fa[j] = fb0; fc[j] = fb1; fm[j] = -fb0 - fb1; mrp[j] = -r_prev[j];
   }
   /* sum_k F_k (x) (r_k - r_b): r_a - r_b = -r_prev, r_c - r_b = r_next */
-  vir_add(o->vir[2], fa, mrp);
-  vir_add(o->vir[2], fc, r_next);
+  vir_add(w, fa, mrp);
+  vir_add(w, fc, r_next);
   fsc(o, ia, fa);
-  fsc(o, ib, fm);
+  fsc(o, ib, fa);  /* the centre bead's share: both parts */
+  fsc(o, ib, fc);
   fsc(o, ic, fc);
+  (void)fm;
   return e;
 }
 
-static double bend_chains(orc_sys* o, int beg, int n_chains, int n_mon) {
+static double bend_chains(orc_sys* o, int beg, int n_chains, int n_mon, double* w) {
   double v = 0.;
+  memset(w, 0, 9 * sizeof(double));
   for (int l = 0; l < n_chains; ++l) {
     int base = beg + l * n_mon; /* 0-based index of bead 1 */
     double r_next[3], r_prev[3];
@@ -1076,25 +1093,24 @@ static double bend_chains(orc_sys* o, int beg, int n_chains, int n_mon) {
       for (int d = 0; d < 3; ++d) r_next[d] = o->r0[3 * (base + i) + d] - o->r0[3 * (base + i - 1) + d];
       mic2(o, r_next);
       v += bend_term(o, base + i - 2, base + i - 1, base + i, r_prev, r_next, o->p.k_bend, o->p.alpha_eq,
-                     o->p.bend_form);
+                     o->p.bend_form, w);
     }
   }
   return v;
 }
 
 /* bending(1) (bending.f90:19-121) */
-void orc_bending(orc_sys* o) { o->v_bend = bend_chains(o, 0, o->s.n_chain, o->s.n_mon); }
-/* the bending group of the virial holds brush and melt bending; cleared with the forces */
+void orc_bending(orc_sys* o) { o->v_bend = bend_chains(o, 0, o->s.n_chain, o->s.n_mon, o->vir[2]); }
 /* bending_melt(1) (bending_melt.f90:22-108; the second index there lacks the `beg` offset, a
  * reference defect not reproduced: the consecutive melt bond is used). */
 void orc_bending_melt(orc_sys* o) {
-  o->v_bend_melt = bend_chains(o, o->part_init_d, o->s.n_chain_d, o->s.n_mon_d);
+  o->v_bend_melt = bend_chains(o, o->part_init_d, o->s.n_chain_d, o->s.n_mon_d, o->vir[3]);
 }
 
 /* orientation(1) (orientation.f90:24-88) */
 void orc_orientation(orc_sys* o) {
   double v = 0.;
-  memset(o->vir[3], 0, 9 * sizeof(double));
+  memset(o->vir[4], 0, 9 * sizeof(double));
   const double D = o->s.boundary[2];
   for (int l = 0; l < o->s.n_chain; ++l) {
     int h = l * o->s.n_mon; /* head, 0-based */
@@ -1136,7 +1152,7 @@ void orc_orientation(orc_sys* o) {
       f1[j] = fm * dn[j];
     }
     /* forces on the head and bead 1 only: F_1 (x) (r_1 - r_h) */
-    vir_add(o->vir[3], f1, r_next);
+    vir_add(o->vir[4], f1, r_next);
     fsc(o, h, f1);
     fsc(o, h + 1, f1);
   }
@@ -1207,7 +1223,7 @@ double orc_ewald_k(orc_sys* o) {
     }
   }
   double u = 0.;
-  memset(o->vir[5], 0, 9 * sizeof(double));
+  memset(o->vir[6], 0, 9 * sizeof(double));
   for (int k = 0; k < nk; ++k) {
     const double uk = o->ik2[k] * exp(-o->k2[k] * o->fac_alpha) * (re[k] * re[k] + im[k] * im[k]);
     u += uk;
@@ -1215,10 +1231,10 @@ double orc_ewald_k(orc_sys* o) {
     const double c = 2. * (o->ik2[k] + o->fac_alpha);
     for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b)
-        o->vir[5][3 * a + b] += uk * ((a == b ? 1. : 0.) - c * o->kv[3 * k + a] * o->kv[3 * k + b]);
+        o->vir[6][3 * a + b] += uk * ((a == b ? 1. : 0.) - c * o->kv[3 * k + a] * o->kv[3 * k + b]);
   }
   u = u * 4. * pi * o->inv_V_k;
-  for (int k = 0; k < 9; ++k) o->vir[5][k] *= 4. * pi * o->inv_V_k;
+  for (int k = 0; k < 9; ++k) o->vir[6][k] *= 4. * pi * o->inv_V_k;
   for (int i = 0; i < o->nm; ++i) {
     if (o->q[i] == 0.) continue;
     double fk[3] = {0, 0, 0};
@@ -1252,10 +1268,10 @@ double orc_dipolar_correction(orc_sys* o) {
   double u = 2. * pi * mz * mz * o->inv_V_k;
   /* minus the strain derivative of u (M_z scales with z, the volume with each axis):
      diag(u, u, -u) */
-  memset(o->vir[6], 0, 9 * sizeof(double));
-  o->vir[6][0] = u;
-  o->vir[6][4] = u;
-  o->vir[6][8] = -u;
+  memset(o->vir[7], 0, 9 * sizeof(double));
+  o->vir[7][0] = u;
+  o->vir[7][4] = u;
+  o->vir[7][8] = -u;
   o->v_coul += u;
   return u;
 }

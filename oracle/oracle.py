@@ -93,7 +93,7 @@ def _i(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int32))
 
 
-VIRIAL_GROUPS = ("pair", "fene", "bend", "orientation", "wall", "kspace", "dipole")
+VIRIAL_GROUPS = ("pair", "fene", "bend", "bend_melt", "orientation", "wall", "kspace", "dipole")
 
 ENERGY_KEYS = ("v_fluid_fluid", "v_fluid_wall", "v_wall_wall", "v_intra_molec", "v_bend", "v_bend_melt",
                "v_or", "v_coul", "t_fluid")
@@ -159,7 +159,7 @@ class Oracle:
 
     def virial(self):
         """W_ab = sum of F_a r_b per term group of the last force evaluation (3x3 arrays)."""
-        out = np.zeros(7 * 9)
+        out = np.zeros(8 * 9)
         self.L.orc_get_virial(self.h, _d(out))
         return {g: out[9 * k:9 * k + 9].reshape(3, 3) for k, g in enumerate(VIRIAL_GROUPS)}
 

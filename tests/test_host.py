@@ -33,6 +33,23 @@ def test_abi_struct_sizes_match_header(lib):
     assert (o.profile_from_step, o.kspace_plain_sums) == (0, 0)
 
 
+def test_struct_layouts_match_the_c_compiler(tmp_path):
+    """Sizes of the ctypes mirrors against the C compiler's sizeof of the header's structs."""
+    import ctypes as C
+    import subprocess
+    from mfa_brush_gb300 import abi
+    names = {"mfa_inputs": abi.Inputs, "mfa_params": abi.Params, "mfa_system": abi.System,
+             "mfa_options": abi.Options, "mfa_energies": abi.Energies, "mfa_observables": abi.Observables,
+             "mfa_virial": abi.Virial}
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "mfa_gpu.h"\nint main(void) {\n' +
+                   "".join('  printf("%%zu\\n", sizeof(%s));\n' % n for n in names) + "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == [C.sizeof(t) for t in names.values()]
+
+
 def test_header_flags(try_dir):
     from mfa_brush_gb300 import md
     f = md.flags_from_header(os.path.join(try_dir, "control_simulation.h"))
