@@ -293,7 +293,7 @@ def run_single(args):
                        "chunk_steps": CHUNK, "skin": skin,
                        "l2_flush": ("inputs larger than L2" if n * 96 > 129e6
                                     else "none: the working set fits in L2")},
-            "gpu_launches": int(launches + 10 * rebuilds),
+            "gpu_launches": int(launches + 11 * rebuilds),
             "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": roof,
@@ -383,8 +383,8 @@ def main():
         # every replica of this rank: the rebuild rate depends on the size of the batch
         # each candidate warmed up like the timed run (the first steps after the lattice start
         # are hotter and rebuild more often)
-        best, rates = tune.tune_skin(p, reps, n_sample=len(reps), steps=100, warmup=args.warmup,
-                                     precision=args.precision, device=local)
+        best, rates = tune.tune_skin(p, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8), n_sample=len(reps),
+                                     steps=100, warmup=args.warmup, precision=args.precision, device=local)
         blk, brates = tune.tune_block(p, reps, best, n_sample=len(reps), steps=100, warmup=args.warmup,
                                       precision=args.precision, device=local)
         tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
@@ -412,6 +412,7 @@ def main():
     clk = ClockSampler(local)
     clk.start()
     rb0 = g.rebuild_count()
+    rr0 = g.replica_rebuild_counts()
     l0 = g.launch_count()
     g.synchronize()
     g.event_record(0)
@@ -423,6 +424,8 @@ def main():
     clocks = clk.stop()
     launches = g.launch_count() - l0
     rebuilds = g.rebuild_count() - rb0
+    rep_rb = (g.replica_rebuild_counts() - rr0) * (100.0 / args.steps)
+    n_rep_part = np.array([s.n_part for s in systems], np.float64)
     t = ms / 1000.0
     # the slowest rank's time; the atom count and per-replica energies of every rank (the one
     # end-of-run gather: E/N of each replica of the global set, in global order, on rank 0)
@@ -459,8 +462,13 @@ def main():
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
-            "gpu_launches": int(launches + 10 * rebuilds),
+            "gpu_launches": int(launches + 11 * rebuilds),
             "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
+            "replica_rebuilds_per_100_steps": {
+                "mean": float(rep_rb.mean()), "min": float(rep_rb.min()), "max": float(rep_rb.max()),
+                "particle_weighted": float((rep_rb * n_rep_part).sum() / n_rep_part.sum()),
+                "note": "a replica is rebuilt when its own particles moved half the skin; a step with "
+                        "any rebuild counts once in rebuilds_per_100_steps"},
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,

@@ -180,6 +180,11 @@ typedef struct mfa_options {
   int32_t kspace_plain_sums;/* 1: mixed-precision k-space sums in plain FP32, without the Kahan
                                compensation across particle tiles and k rows (a precision study;
                                default 0)                                                       */
+  int32_t observe;          /* 1: mfa_step adds every energy record of the steps after
+                               profile_from_step (n_relax) to the observation averages
+                               (mfa_get_averages); default 0                                    */
+  int32_t series_capacity;  /* energy records kept on the device for mfa_get_energy_series (a
+                               ring; 0 = none, the default)                                     */
 } mfa_options;
 
 typedef struct mfa_energies {
@@ -222,6 +227,22 @@ typedef struct mfa_virial {
   double volume;            /* Lx Ly D                                                          */
   double pressure[9];       /* (kinetic + total) / volume                                       */
 } mfa_virial;
+
+/* Time averages of the observation phase of one replica (observation.f90:17-291, written to
+   fort.40, fort.42 and fort.43 by observation.f90:295-314 and to the pressure block by
+   obser_out.f90:309-318): sums over the observations divided by their number.              */
+typedef struct mfa_averages {
+  int64_t count;            /* observations summed (count_obs)                                  */
+  double v_total, t_total, e_total;        /* means (fort.40; t_total = t_fluid)               */
+  double v_total2, t_total2, e_total2;     /* means of their squares                           */
+  double v_fluid, t_fluid, e_fluid;        /* v_ff + v_intra + v_fw, t_fluid, v_ff + t_fluid
+                                              (observation.f90:150-157)                        */
+  double v_fluid2, t_fluid2, e_fluid2;
+  double momentum[3];       /* tot_P / count_obs (fort.40)                                       */
+  double rg2_brush[3], rg2_melt[3], rg2_mean[3];  /* r_g2_mean(1..3,:) / count_obs (fort.42)    */
+  double r_par_per2[2];     /* brush and melt (Rg_z^2 - (Rg_x^2 + Rg_y^2)/2) / Rg^2 (fort.43)     */
+  double pressure[9];       /* press_tensor_mean / count_obs: the mean of mfa_virial.pressure   */
+} mfa_averages;
 
 typedef struct mfa_ctx mfa_ctx;
 
@@ -330,6 +351,14 @@ int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out);
    and velocities of the record's step (mfa_step every energy_every steps), or the per-routine
    calls since the last mfa_verlet_velocities (each call replaces its own group).               */
 int mfa_get_virial(mfa_ctx* ctx, mfa_virial* out);
+/* Observation averages of every replica (one mfa_averages each); needs options.observe.        */
+int mfa_get_averages(mfa_ctx* ctx, mfa_averages* out);
+int mfa_reset_averages(mfa_ctx* ctx);
+/* The energy records that mfa_step stored since the previous call (the fort.60/61 series every
+   energy_every steps, verlet_velocities.f90:184-207), oldest first: out[k * n_rep + r] is record
+   k of replica r, at most cap records; *n = records returned.  Needs options.series_capacity;
+   records that the ring overwrote before they were read are lost.                             */
+int mfa_get_energy_series(mfa_ctx* ctx, mfa_energies* out, int32_t cap, int32_t* n);
 /* Observation quantities of every replica (one mfa_observables each) on the current state; the
    head forces are those of the last energy record (mfa_step every energy_every steps, or the
    last mfa_verlet_velocities call).                                                           */
@@ -369,10 +398,11 @@ int mfa_pair_list_static(mfa_ctx* ctx, int32_t rep, int32_t* pairs, int64_t cap,
 int mfa_event_record(mfa_ctx* ctx, int32_t slot);
 int mfa_event_elapsed(mfa_ctx* ctx, int32_t slot_a, int32_t slot_b, float* ms);
 /* Runs nsteps un-graphed steps with events around each kernel family and returns the mean
-   device ms per launch and the launch count per family (names from mfa_kernel_name).  Every
-   timed step rebuilds the cell sort and the lists, so the "rebuild" family is the cost of one
-   rebuild; mfa_step rebuilds only when the displacement test fires (mfa_rebuild_count).      */
-#define MFA_NKFAM 8
+   device ms per launch and the launch count per family (names from mfa_kernel_name).  The
+   "rebuild" family is the rebuild as mfa_step runs it, per step: the replicas whose skin test
+   fired, nothing on most steps; "rebuild_all" is a rebuild of every replica (three, after the
+   steps).                                                                                    */
+#define MFA_NKFAM 9
 int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* launches);
 const char* mfa_kernel_name(int32_t fam);
 /* FP32 FMA throughput of `device` in TFLOP/s (2 FLOP per FMA), measured by eight independent
@@ -381,8 +411,13 @@ const char* mfa_kernel_name(int32_t fam);
 int mfa_fp32_fma_peak(int32_t device, double* tflops);
 /* Number of kernel launches issued by the library since the context was created. */
 int mfa_launch_count(mfa_ctx* ctx, int64_t* n);
-/* Number of cell-sort + neighbour-list rebuilds since the context was created (synchronises). */
+/* Number of cell-sort + neighbour-list rebuilds since the context was created (synchronises):
+   steps on which some replica was rebuilt. */
 int mfa_rebuild_count(mfa_ctx* ctx, int64_t* n);
+/* Rebuilds of each replica since the context was created (n_rep counts; synchronises).  The
+   decision is per replica: a replica is rebuilt when one of its own particles moved more than
+   skin/2 since its last rebuild (check_skin.f90:11-24 decides per system). */
+int mfa_replica_rebuild_counts(mfa_ctx* ctx, int64_t* counts);
 
 #ifdef __cplusplus
 }

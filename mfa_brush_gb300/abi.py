@@ -87,7 +87,8 @@ class System(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", i32), ("device", i32), ("skin", f64), ("nbr_capacity", i32),
                 ("energy_every", i32), ("use_graphs", i32), ("block_size", i32),
-                ("profile_from_step", i32), ("kspace_plain_sums", i32)]
+                ("profile_from_step", i32), ("kspace_plain_sums", i32), ("observe", i32),
+                ("series_capacity", i32)]
 
 
 class Energies(C.Structure):
@@ -106,6 +107,23 @@ class Observables(C.Structure):
     def as_dict(self):
         return {"step": self.step, "rg2_brush": list(self.rg2_brush), "rg2_melt": list(self.rg2_melt),
                 "momentum": list(self.momentum), "f_heads": [list(self.f_heads[0]), list(self.f_heads[1])]}
+
+
+class Averages(C.Structure):
+    _fields_ = ([("count", i64)] +
+                [(k, f64) for k in ("v_total", "t_total", "e_total", "v_total2", "t_total2", "e_total2",
+                                    "v_fluid", "t_fluid", "e_fluid", "v_fluid2", "t_fluid2", "e_fluid2")] +
+                [("momentum", f64 * 3), ("rg2_brush", f64 * 3), ("rg2_melt", f64 * 3), ("rg2_mean", f64 * 3),
+                 ("r_par_per2", f64 * 2), ("pressure", f64 * 9)])
+
+    def as_dict(self):
+        import numpy as np
+        d = {}
+        for k, t in self._fields_:
+            x = getattr(self, k)
+            d[k] = np.array(list(x)) if hasattr(x, "__len__") else x
+        d["pressure"] = d["pressure"].reshape(3, 3)
+        return d
 
 
 VIRIAL_GROUPS = ("pair", "fene", "bend", "bend_melt", "orientation", "wall", "kspace", "dipole")
@@ -171,6 +189,9 @@ SIGNATURES = {
     "mfa_get_profiles": (i32, [vp, i32, dp, dp, dp, P(i64)]),
     "mfa_observe": (i32, [vp, P(Observables)]),
     "mfa_get_virial": (i32, [vp, P(Virial)]),
+    "mfa_get_averages": (i32, [vp, P(Averages)]),
+    "mfa_reset_averages": (i32, [vp]),
+    "mfa_get_energy_series": (i32, [vp, P(Energies), i32, ip]),
     "mfa_list_stats": (i32, [vp, ip, ip]),
     "mfa_kspace_info": (i32, [vp, ip, ip]),
     "mfa_reset_profiles": (i32, [vp]),
@@ -185,8 +206,9 @@ SIGNATURES = {
     "mfa_fp32_fma_peak": (i32, [i32, dp]),
     "mfa_launch_count": (i32, [vp, P(i64)]),
     "mfa_rebuild_count": (i32, [vp, P(i64)]),
+    "mfa_replica_rebuild_counts": (i32, [vp, P(i64)]),
 }
-NKFAM = 8
+NKFAM = 9
 
 _lib = None
 

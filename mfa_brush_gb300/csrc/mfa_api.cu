@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/mfa_gpu.h"
+#include "mfa_obs.cuh"
 #include "mfa_state.cuh"
 
 using namespace mfa;
@@ -44,7 +45,6 @@ struct mfa_ctx {
   bool grow_pending = false;     // the list capacity is to be raised before the next step
   bool overflow_reported = false;  // the current list overflow was returned to the caller already
   long long* h_rebuilds = nullptr;
-  long long* d_rebuilds = nullptr;
   long long last_rebuilds = 0;
   long long host_steps = 0;      // steps completed (host view)
   int last_source = 0;           // 0 none, 1 mfa_step record, 2 per-routine accumulators
@@ -53,7 +53,12 @@ struct mfa_ctx {
   long long launches = 0;
   std::vector<void*> allocs;
   double* stage = nullptr;  // 4 x 3N doubles for host <-> device state movement, made on first use
-  double* obs = nullptr;    // [nrep][9] of mfa_observe, made on first use
+  double* obs = nullptr;    // [nrep][9] of mfa_observe and of the averages
+  double* avg = nullptr;    // [nrep][NAVG] observation averages (options.observe)
+  double* series = nullptr; // [series_capacity][O_VIR][nrep] energy records (options.series_capacity)
+  long long* series_step = nullptr;  // [series_capacity] steps done at each record
+  long long* series_head = nullptr;  // [1] records written
+  long long series_read = 0;         // records returned to the caller
   // device addresses of the file-scope scratch of mfa_pair_list_static, looked up at the first
   // call of that entry point on this context (with the context's device current)
   int* static_pairs = nullptr;
@@ -65,7 +70,7 @@ struct mfa_ctx {
 namespace {
 
 const char* kFamNames[MFA_NKFAM] = {"rebuild", "pair", "bonded", "integrate", "kspace", "profiles", "record",
-                                    "positions"};
+                                    "positions", "rebuild_all"};
 
 int fail(mfa_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -152,27 +157,16 @@ __global__ void k_clear_overflow(unsigned* status) {
   status[1] = 0u;
 }
 
-__global__ void k_count_rebuild(int* flag, long long* n) {
-  if (*flag) *n += 1;
-  *flag = 0;
-}
-
-// rebuild (conditional) + clear flag
+// rebuild of the flagged replicas (all of them when forced); counts and clears the flags
 void rebuild(mfa_ctx* ctx, bool force) {
   launch_rebuild(ctx->S, ctx->st, force);
-  k_count_rebuild<<<1, 1, 0, ctx->st>>>(ctx->S.rebuild_flag, ctx->d_rebuilds);
   ctx->launches += 11;
 }
 
-// Graph form of the skin check: the IF body (the ten rebuild kernels) runs only on steps whose
-// position update raised the flag; other steps launch nothing.
-__global__ void k_cond_rebuild(int* flag, long long* n, cudaGraphConditionalHandle h) {
-  const int f = *flag;
-  cudaGraphSetConditional(h, f ? 1u : 0u);
-  if (f) {
-    *n += 1;
-    *flag = 0;
-  }
+// Graph form of the skin check: the IF body (the eleven rebuild kernels) runs only on steps whose
+// position update raised the flag of some replica; other steps launch nothing.
+__global__ void k_cond_rebuild(const int* flag, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, flag[0] ? 1u : 0u);
 }
 
 int capture_conditional_rebuild(mfa_ctx* ctx) {
@@ -184,7 +178,7 @@ int capture_conditional_rebuild(mfa_ctx* ctx) {
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
-  k_cond_rebuild<<<1, 1, 0, st>>>(ctx->S.rebuild_flag, ctx->d_rebuilds, h);
+  k_cond_rebuild<<<1, 1, 0, st>>>(ctx->S.rebuild_flag, h);
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
   cudaGraphNodeParams cp = {};  // aggregate initialisation: all reserved fields zero
   cp.type = cudaGraphNodeTypeConditional;
@@ -195,7 +189,7 @@ int capture_conditional_rebuild(mfa_ctx* ctx) {
   CK(cudaGraphAddNode(&node, graph, deps, nullptr, nd, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(ctx->st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  launch_rebuild(ctx->S, ctx->st2, true);
+  launch_rebuild(ctx->S, ctx->st2, false);  // the flagged replicas (the flags stay set until its last kernel)
   cudaGraph_t captured;
   CK(cudaStreamEndCapture(ctx->st2, &captured));
   CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
@@ -218,59 +212,13 @@ bool any_chains(const mfa_ctx* ctx) {
 }
 
 void fill_energies(const mfa_ctx* ctx, const double* acc, int rep, mfa_energies* e) {
-  const int R = ctx->nrep;
-  auto A = [&](int slot) { return acc[(size_t)slot * R + rep]; };
-  std::memset(e, 0, sizeof *e);
+  record_energies(acc, ctx->nrep, rep, ctx->hreps[rep], ctx->C, e);
   e->step = ctx->sys[rep].s_time + ctx->host_steps;
-  e->v_fluid_fluid = A(O_VFF) + ctx->v_ff_walls[rep];
-  e->v_fluid_wall = A(O_VFW);
-  e->v_wall_wall = ctx->v_ww[rep];
-  e->v_intra_molec = A(O_VINTRA);
-  e->v_bend = A(O_VBEND);
-  e->v_bend_melt = A(O_VBENDM);
-  e->v_or = A(O_VOR);
-  const bool charged = ctx->P.flags.system == 2 || ctx->P.flags.system == 3;
-  e->v_coul = charged ? A(O_VCOUL) + ctx->v_coul_self[rep] + A(O_VCOULK) + A(O_VDIP) : 0.;
-  e->t_fluid = A(O_TFLUID);
-  e->v_total = e->v_wall_wall + e->v_fluid_wall + e->v_fluid_fluid + e->v_intra_molec;
-  if (ctx->P.flags.bending) e->v_total += e->v_bend;
-  if (ctx->P.flags.orientation) e->v_total += e->v_or;
-  if (ctx->P.flags.bending_melt) e->v_total += e->v_bend_melt;
-  if (charged) e->v_total += e->v_coul;
-  e->e_total = e->v_total + e->t_fluid;
-  e->inv_n = ctx->hreps[rep].inv_n;
 }
 
-// Virial tensors of record `acc` for replica `rep`: the symmetric groups hold xx yy zz xy xz yz
-// and are mirrored here; the orientation group is a full tensor; the slab-dipole group follows from
-// its energy u: diag(u, u, -u).
 void fill_virial(const mfa_ctx* ctx, const double* acc, int rep, mfa_virial* o) {
-  const int R = ctx->nrep;
-  auto A = [&](int slot) { return acc[(size_t)slot * R + rep]; };
-  std::memset(o, 0, sizeof *o);
+  record_virial(acc, ctx->nrep, rep, ctx->hreps[rep], ctx->C, o);
   o->step = ctx->sys[rep].s_time + ctx->host_steps;
-  double* grp[NVIR] = {o->pair, o->fene, o->bend, o->bend_melt, o->orientation, o->wall, o->kspace, o->dipole};
-  for (int g = 0; g < NVIR; ++g) {
-    double* w = grp[g];
-    for (int c = 0; c < 9; ++c) w[c] = A(O_VIR + 9 * g + c);
-    if (g != V_OR)
-      for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < a; ++b) w[3 * a + b] = w[3 * b + a];
-  }
-  const bool charged = ctx->P.flags.system == 2 || ctx->P.flags.system == 3;
-  const double ud = charged ? A(O_VDIP) : 0.;
-  std::memset(o->dipole, 0, sizeof o->dipole);
-  o->dipole[0] = o->dipole[4] = ud;
-  o->dipole[8] = -ud;
-  for (int c = 0; c < 9; ++c) o->kinetic[c] = A(O_KIN + c);
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < a; ++b) o->kinetic[3 * a + b] = o->kinetic[3 * b + a];
-  const double* L = ctx->sys[rep].boundary;
-  o->volume = L[0] * L[1] * L[2];
-  for (int c = 0; c < 9; ++c) {
-    for (int g = 0; g < NVIR; ++g) o->total[c] += grp[g][c];
-    o->pressure[c] = (o->kinetic[c] + o->total[c]) / o->volume;
-  }
 }
 
 // ewald_k(0) (ewald_k.f90:37-124): the k-vectors in the reference's enumeration order, G(k),
@@ -673,6 +621,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     if (F.wall == 2)  // wall_wall.f90:45-48
       ctx->v_ww[r] = 2.0 * (std::fabs(p->a_w) * std::pow(p->sigma_w / D, 9) - p->a_w * std::pow(p->sigma_w / D, 3));
     R.v_ww = ctx->v_ww[r];
+    R.v_ffw = 0.;  // set below for explicit walls
+    R.v_cself = 0.;
     R.inv_n = (F.system == 2) ? 1. / (double)s.n_mon_tot : 1. / (double)(s.n_mon_tot - s.n_chain);
     R.hist_inv_dz = 1. / (D / (double)C.hist_dim);
     std::memcpy(&R.Lbits[0], &R.L[0], 8);
@@ -698,11 +648,13 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
           }
         }
       ctx->v_ff_walls[r] = vw;
+      R.v_ffw = vw;
     }
     if (charged) {
       double vs = 0.;
       for (int t = 0; t < s.n_mon_tot; ++t) vs -= p->charge[a_type[R.p0 + t] - 1] * p->charge[a_type[R.p0 + t] - 1];
       ctx->v_coul_self[r] = vs * p->sqrt_alpha / std::sqrt((double)3.1415926536f);
+      R.v_cself = ctx->v_coul_self[r];
     }
   }
   // ---- per-particle info ----------------------------------------------------------------------
@@ -740,10 +692,12 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.cell_count, cell_off + 1);
   DA(S.cell_start, cell_off + 1);
   DA(S.scan_blk, (cell_off + 1023) / 1024 + 1);
-  DA(S.rebuild_flag, 1);
+  DA(S.rebuild_flag, 1 + n_rep);
+  DA(S.cell_rep, cell_off);
+  DA(S.rebuilds, 1);
+  DA(S.rep_rebuilds, n_rep);
   DA(S.status, 2);  // [0] status bits, [1] largest list count of the rebuilds so far
   DA(S.steps_done, 1);
-  DA(ctx->d_rebuilds, 1);
   DA(ctx->dreps, n_rep);
   DA(ctx->dtabf, NPAIR);
   DA(ctx->dtabd, NPAIR);
@@ -751,6 +705,14 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(ctx->acc_call, NOBS * n_rep);
   DA(ctx->rec, NOBS * n_rep);
   DA(ctx->prof, (size_t)n_rep * C.hist_dim * 21);
+  DA(ctx->obs, (size_t)9 * n_rep);
+  if (ctx->opt.observe) DA(ctx->avg, (size_t)NAVG * n_rep);
+  if (ctx->opt.series_capacity < 0) return fail(ctx, MFA_ERR_ARG, "series_capacity < 0");
+  if (ctx->opt.series_capacity > 0) {
+    DA(ctx->series, (size_t)ctx->opt.series_capacity * O_VIR * n_rep);
+    DA(ctx->series_step, ctx->opt.series_capacity);
+  }
+  DA(ctx->series_head, 1);
   CK(cudaMallocHost(&ctx->h_status, 2 * sizeof(unsigned)));
   CK(cudaMallocHost(&ctx->h_rebuilds, sizeof(long long)));
   ctx->h_status[0] = ctx->h_status[1] = 0;
@@ -775,14 +737,23 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaMemcpyAsync(S.info, info.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(S.tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(S.slot_of_tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(S.rebuild_flag, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(S.rebuild_flag, 0, sizeof(int) * (1 + n_rep), st));
+  {
+    std::vector<int> cr(std::max(cell_off, 1));
+    for (int r = 0; r < n_rep; ++r)
+      for (int c = 0; c < ctx->hreps[r].ncell; ++c) cr[ctx->hreps[r].cell_off + c] = r;
+    CK(cudaMemcpy(S.cell_rep, cr.data(), sizeof(int) * cell_off, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemsetAsync(S.rep_rebuilds, 0, sizeof(long long) * n_rep, st));
   CK(cudaMemsetAsync(S.status, 0, 2 * sizeof(unsigned), st));
   CK(cudaMemsetAsync(S.steps_done, 0, sizeof(long long), st));
-  CK(cudaMemsetAsync(ctx->d_rebuilds, 0, sizeof(long long), st));
+  CK(cudaMemsetAsync(S.rebuilds, 0, sizeof(long long), st));
   CK(cudaMemsetAsync(ctx->acc_step, 0, sizeof(double) * NOBS * n_rep, st));
   CK(cudaMemsetAsync(ctx->acc_call, 0, sizeof(double) * NOBS * n_rep, st));
   CK(cudaMemsetAsync(ctx->rec, 0, sizeof(double) * NOBS * n_rep, st));
   CK(cudaMemsetAsync(ctx->prof, 0, sizeof(double) * n_rep * C.hist_dim * 21, st));
+  if (ctx->avg) CK(cudaMemsetAsync(ctx->avg, 0, sizeof(double) * NAVG * n_rep, st));
+  CK(cudaMemsetAsync(ctx->series_head, 0, sizeof(long long), st));
   for (int k = 9; k < 12; ++k) CK(cudaMemsetAsync(*dst[k], 0, sizeof(double) * Nn, st));
   // ---- state upload (canonical AoS -> slots) --------------------------------------------------
   {
@@ -833,7 +804,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     }
   }
   if (rc != MFA_OK) return rc;
-  CK(cudaMemcpy(ctx->h_rebuilds, ctx->d_rebuilds, sizeof(long long), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ctx->h_rebuilds, ctx->S.rebuilds, sizeof(long long), cudaMemcpyDeviceToHost));
   ctx->last_rebuilds = *ctx->h_rebuilds;
   return MFA_OK;
 }
@@ -911,7 +882,7 @@ int mfa_verlet_positions(mfa_ctx* ctx) {
 int mfa_check_skin(mfa_ctx* ctx, int32_t* rebuilt) {
   if (!ctx) return MFA_ERR_ARG;
   rebuild(ctx, false);
-  CK(cudaMemcpyAsync(ctx->h_rebuilds, ctx->d_rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->h_rebuilds, ctx->S.rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   if (rebuilt) *rebuilt = (*ctx->h_rebuilds != ctx->last_rebuilds) ? 1 : 0;
   ctx->last_rebuilds = *ctx->h_rebuilds;
@@ -1102,7 +1073,9 @@ static int prepare_step(mfa_ctx* ctx) {
   return MFA_OK;
 }
 
-static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool capturing, int* err) {
+// obs: the energy records also go into the observation averages (Rg^2 and momentum of the state
+// of the record's step, so those steps run the velocity and position halves as two kernels).
+static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs, bool capturing, int* err) {
   const DevState& S = ctx->S;
   const SimConst& C = ctx->C;
   cudaStream_t st = ctx->st;
@@ -1122,7 +1095,6 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool cap
       L += 1;  // the rebuild body's launches are not counted: they run only when triggered
     } else {
       launch_rebuild(S, st, false);
-      k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
       L += 11;
     }
     // mixed: bonded terms inside the pair kernel; FP64: their own kernel
@@ -1134,16 +1106,32 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool cap
       launch_dipolar(S, C, ctx->K, st, ef, acc, true);
       L += 7;
     }
-    if (k < n && !prof) {
+    const bool split = prof || (obs && ef);
+    if (k < n && !split) {
       launch_integrate(S, C, st, 2, true, ef, acc);
       L += 1;
     } else {
       launch_integrate(S, C, st, 1, true, ef, acc);
       L += 1;
       if (prof) { launch_profiles(S, C, st, ctx->prof, C.hist_dim); L += 1; }
-      if (k < n) { launch_integrate(S, C, st, 0, false, false, acc); L += 1; }
     }
-    if (ef) { launch_record(acc, ctx->rec, st); L += 1; }
+    if (ef) {
+      launch_record(acc, ctx->rec, st);
+      L += 1;
+      if (obs) {
+        launch_observe(S, C, st, ctx->obs);
+        launch_obs_accum(S, C, st, ctx->rec, ctx->obs, ctx->avg);
+        L += 2;
+      }
+      if (ctx->series) {
+        launch_series(S, st, ctx->rec, ctx->series, ctx->series_step, ctx->series_head, ctx->opt.series_capacity);
+        L += 2;
+      }
+    }
+    if (split && k < n) {
+      launch_integrate(S, C, st, 0, false, false, acc);
+      L += 1;
+    }
   }
   return L;
 }
@@ -1169,24 +1157,27 @@ int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
   if (nsteps <= 0) return MFA_OK;
   RET(prepare_step(ctx));
   const long long s0 = ctx->sys[0].s_time + ctx->host_steps;
-  bool prof = ctx->P.flags.profiles && (ctx->host_steps >= ctx->opt.profile_from_step);
-  if (ctx->P.flags.profiles && !prof && ctx->host_steps + nsteps > ctx->opt.profile_from_step) {
+  const bool phased = ctx->P.flags.profiles || ctx->opt.observe;
+  const bool observing = phased && ctx->host_steps >= ctx->opt.profile_from_step;
+  if (phased && !observing && ctx->host_steps + nsteps > ctx->opt.profile_from_step) {
     // split at the start of the observation phase (md_main.f90:202)
     int first = (int)(ctx->opt.profile_from_step - ctx->host_steps);
     int r = mfa_step(ctx, first);
     if (r) return r;
     return mfa_step(ctx, nsteps - first);
   }
+  const bool prof = ctx->P.flags.profiles && observing;
+  const bool obs = ctx->opt.observe && observing;
   const int phase = (int)(s0 % ctx->opt.energy_every);
   long long L = 0;
   if (ctx->opt.use_graphs) {
-    auto key = std::make_tuple(nsteps, phase, (int)prof, 0);
+    auto key = std::make_tuple(nsteps, phase, (int)prof, (int)obs);
     auto it = ctx->graphs.find(key);
     if (it == ctx->graphs.end()) {
       cudaGraph_t g;
       int err = MFA_OK;
       CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-      L = issue_steps(ctx, nsteps, phase, prof, true, &err);
+      L = issue_steps(ctx, nsteps, phase, prof, obs, true, &err);
       cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
       if (err != MFA_OK) return err;
       CK(ec);
@@ -1199,7 +1190,7 @@ int mfa_step(mfa_ctx* ctx, int32_t nsteps) {
     L = it->second.second;
   } else {
     int err = MFA_OK;
-    L = issue_steps(ctx, nsteps, phase, prof, false, &err);
+    L = issue_steps(ctx, nsteps, phase, prof, obs, false, &err);
     CK(cudaGetLastError());
   }
   ctx->launches += L;
@@ -1290,6 +1281,76 @@ int mfa_get_energies(mfa_ctx* ctx, mfa_energies* out) {
   return MFA_OK;
 }
 
+int mfa_get_averages(mfa_ctx* ctx, mfa_averages* out) {
+  if (!ctx || !out) return MFA_ERR_ARG;
+  if (!ctx->avg) return fail(ctx, MFA_ERR_STATE, "observation averages need options.observe = 1");
+  const int R = ctx->nrep;
+  std::vector<double> h((size_t)NAVG * R);
+  CK(cudaMemcpyAsync(h.data(), ctx->avg, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (r) return r;
+  for (int k = 0; k < R; ++k) {
+    const double* a = &h[(size_t)NAVG * k];
+    mfa_averages& o = out[k];
+    std::memset(&o, 0, sizeof o);
+    o.count = (int64_t)a[A_COUNT];
+    if (o.count == 0) continue;
+    const double ic = 1. / a[A_COUNT];
+    o.v_total = a[A_VT] * ic; o.t_total = a[A_TT] * ic; o.e_total = a[A_ET] * ic;
+    o.v_total2 = a[A_VT2] * ic; o.t_total2 = a[A_TT2] * ic; o.e_total2 = a[A_ET2] * ic;
+    o.v_fluid = a[A_VF] * ic; o.t_fluid = a[A_TF] * ic; o.e_fluid = a[A_EF] * ic;
+    o.v_fluid2 = a[A_VF2] * ic; o.t_fluid2 = a[A_TF2] * ic; o.e_fluid2 = a[A_EF2] * ic;
+    for (int d = 0; d < 3; ++d) {
+      o.momentum[d] = a[A_MOM + d] * ic;
+      o.rg2_brush[d] = a[A_RGB + d] * ic;
+      o.rg2_melt[d] = a[A_RGM + d] * ic;
+      o.rg2_mean[d] = a[A_RGA + d] * ic;
+    }
+    o.r_par_per2[0] = a[A_RPP] * ic;
+    o.r_par_per2[1] = a[A_RPP + 1] * ic;
+    for (int c = 0; c < 9; ++c) o.pressure[c] = a[A_P + c] * ic;
+  }
+  return MFA_OK;
+}
+
+int mfa_reset_averages(mfa_ctx* ctx) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (ctx->avg) CK(cudaMemsetAsync(ctx->avg, 0, sizeof(double) * NAVG * ctx->nrep, ctx->st));
+  return MFA_OK;
+}
+
+int mfa_get_energy_series(mfa_ctx* ctx, mfa_energies* out, int32_t cap, int32_t* n) {
+  if (!ctx || !n || cap < 0 || (cap > 0 && !out)) return MFA_ERR_ARG;
+  *n = 0;
+  if (!ctx->series) return fail(ctx, MFA_ERR_STATE, "the energy series needs options.series_capacity > 0");
+  long long head = 0;
+  CK(cudaMemcpyAsync(&head, ctx->series_head, sizeof head, cudaMemcpyDeviceToHost, ctx->st));
+  RET(post_status(ctx));
+  int r = check_status(ctx);
+  if (r) return r;
+  const int R = ctx->nrep, scap = ctx->opt.series_capacity;
+  long long first = std::max(ctx->series_read, head - scap);  // the oldest record still in the ring
+  const long long cnt = std::min<long long>(head - first, cap);
+  std::vector<double> rec((size_t)O_VIR * R, 0.), acc((size_t)NOBS * R, 0.);
+  for (long long k = 0; k < cnt; ++k) {
+    const int slot = (int)((first + k) % scap);
+    long long sd = 0;
+    CK(cudaMemcpy(rec.data(), ctx->series + (size_t)slot * O_VIR * R, sizeof(double) * rec.size(),
+                  cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&sd, ctx->series_step + slot, sizeof sd, cudaMemcpyDeviceToHost));
+    std::copy(rec.begin(), rec.end(), acc.begin());
+    for (int q = 0; q < R; ++q) {
+      mfa_energies& e = out[k * R + q];
+      record_energies(acc.data(), R, q, ctx->hreps[q], ctx->C, &e);
+      e.step = ctx->sys[q].s_time + sd;
+    }
+  }
+  ctx->series_read = first + cnt;
+  *n = (int32_t)cnt;
+  return MFA_OK;
+}
+
 int mfa_get_virial(mfa_ctx* ctx, mfa_virial* out) {
   if (!ctx || !out) return MFA_ERR_ARG;
   std::vector<double> h(NOBS * ctx->nrep);
@@ -1305,7 +1366,6 @@ int mfa_get_virial(mfa_ctx* ctx, mfa_virial* out) {
 int mfa_observe(mfa_ctx* ctx, mfa_observables* out) {
   if (!ctx || !out) return MFA_ERR_ARG;
   const int R = ctx->nrep;
-  if (!ctx->obs) RET(dalloc(ctx, &ctx->obs, (size_t)9 * R));
   launch_observe(ctx->S, ctx->C, ctx->st, ctx->obs);
   ctx->launches += 1;
   std::vector<double> h((size_t)9 * R), a((size_t)NOBS * R);
@@ -1529,10 +1589,8 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
   mark(7);
   for (int k = 1; k <= nsteps; ++k) {
     const bool ef = (k == nsteps);
-    // a rebuild on every step: the "rebuild" family is then the cost of one rebuild (the
-    // fused step runs it only on steps whose displacement test fires)
-    launch_rebuild(S, st, true);
-    k_count_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, ctx->d_rebuilds);
+    // the rebuild as the fused step runs it: the replicas whose skin test fired, if any
+    launch_rebuild(S, st, false);
     mark(0);
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
     mark(1);
@@ -1545,6 +1603,11 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
     launch_integrate(S, C, st, k < nsteps ? 2 : 1, true, ef, acc);
     mark(3);
     if (ef) { launch_record(acc, ctx->rec, st); mark(6); }
+  }
+  // then a rebuild of every replica, three times
+  for (int k = 0; k < 3; ++k) {
+    launch_rebuild(S, st, true);
+    mark(8);
   }
   CK(cudaStreamSynchronize(st));
   std::vector<double> tot(MFA_NKFAM, 0.);
@@ -1571,9 +1634,16 @@ int mfa_launch_count(mfa_ctx* ctx, int64_t* n) {
   return MFA_OK;
 }
 
+int mfa_replica_rebuild_counts(mfa_ctx* ctx, int64_t* counts) {
+  if (!ctx || !counts) return MFA_ERR_ARG;
+  CK(cudaMemcpyAsync(counts, ctx->S.rep_rebuilds, sizeof(long long) * ctx->nrep, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return MFA_OK;
+}
+
 int mfa_rebuild_count(mfa_ctx* ctx, int64_t* n) {
   if (!ctx || !n) return MFA_ERR_ARG;
-  CK(cudaMemcpyAsync(ctx->h_rebuilds, ctx->d_rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->h_rebuilds, ctx->S.rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   *n = *ctx->h_rebuilds;
   return MFA_OK;

@@ -118,6 +118,8 @@ struct RepDesc {
   unsigned long long seed;
   long long s_time;
   double lz_half, v_ww, inv_n;
+  double v_ffw;         // LJ energy of the fixed wall beads among themselves (WALL 1; a constant)
+  double v_cself;       // Ewald self energy (a constant)
   double hist_inv_dz;
   long long Lbits[2];   // bit patterns of Lx, Ly: for positive doubles, integer order = numeric order
 };

@@ -14,6 +14,7 @@
 //           the mixed step adds them in the pair kernel).  With energies: the kinetic energy and
 //           the kinetic tensor sum m v (x) v (viscosity.f90:20-27) of v(n).
 // All integration is FP64 in both precision modes.
+#include "mfa_obs.cuh"
 #include "mfa_state.cuh"
 
 namespace mfa {
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
       const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
       const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
-      if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) *s.rebuild_flag = 1;
+      if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) flag_rebuild(s, rep);
       if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(s.status, ST_NAN);
     }
   }
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
       const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
       const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
       const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
-      if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) *s.rebuild_flag = 1;
+      if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) flag_rebuild(s, rep);
       const long long bx = __double_as_longlong(x), bz = __double_as_longlong(z);
       if (((bx >> 52) & 0x7FF) == 0x7FF || ((bz >> 52) & 0x7FF) == 0x7FF) atomicOr(s.status, ST_NAN);
     }
@@ -412,6 +413,63 @@ __global__ void __launch_bounds__(OBS_THREADS) k_observe(DevState s, SimConst C,
   }
 }
 
+__global__ void k_obs_accum(const double* __restrict__ rec, int nrep, const RepDesc* __restrict__ reps, SimConst C,
+                            const double* __restrict__ obs, double* __restrict__ avg) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrep) return;
+  mfa_energies e;
+  record_energies(rec, nrep, r, reps[r], C, &e);
+  mfa_virial w;
+  record_virial(rec, nrep, r, reps[r], C, &w);
+  double* a = avg + (size_t)r * NAVG;
+  // observation.f90:140-170 (t_total = t_fluid: the wall beads do not move)
+  const double vt = e.v_total, tt = e.t_fluid, et = e.e_total;
+  const double vf = e.v_fluid_fluid + e.v_intra_molec + e.v_fluid_wall, tf = e.t_fluid, ef = e.v_fluid_fluid + e.t_fluid;
+  a[A_COUNT] += 1.;
+  a[A_VT] += vt; a[A_TT] += tt; a[A_ET] += et;
+  a[A_VT2] += vt * vt; a[A_TT2] += tt * tt; a[A_ET2] += et * et;
+  a[A_VF] += vf; a[A_TF] += tf; a[A_EF] += ef;
+  a[A_VF2] += vf * vf; a[A_TF2] += tf * tf; a[A_EF2] += ef * ef;
+  // observation.f90:247-291: Rg^2 means (brush, melt, their average), r_par_per2, momentum
+  const double* o = obs + 9 * (size_t)r;
+  for (int d = 0; d < 3; ++d) {
+    a[A_MOM + d] += o[6 + d];
+    a[A_RGB + d] += o[d];
+    a[A_RGM + d] += o[3 + d];
+    a[A_RGA + d] += 0.5 * (o[d] + o[3 + d]);
+  }
+  const double sb = o[0] + o[1] + o[2], sm = o[3] + o[4] + o[5];
+  if (sb > 0.) a[A_RPP] += (o[2] - 0.5 * (o[0] + o[1])) / sb;  // (the reference divides by zero
+  if (sm > 0.) a[A_RPP + 1] += (o[5] - 0.5 * (o[3] + o[4])) / sm;  //  when there are no chains)
+  // obser_out.f90:309: press_tensor_mean
+  for (int c = 0; c < 9; ++c) a[A_P + c] += w.pressure[c];
+}
+
+void launch_obs_accum(const DevState& s, const SimConst& C, cudaStream_t st, const double* rec, const double* obs,
+                      double* avg) {
+  k_obs_accum<<<(s.nrep + 127) / 128, 128, 0, st>>>(rec, s.nrep, s.reps, C, obs, avg);
+}
+
+// The energy slots of the record (every slot before the virial) into the series ring at the
+// current head; the head moves on in a separate one-thread kernel, after every thread has read it.
+__global__ void k_series_store(const double* __restrict__ rec, int nrep, double* __restrict__ series,
+                               long long* __restrict__ series_step, const long long* head, int cap,
+                               const long long* steps_done) {
+  const int slot = (int)(*head % cap);
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < O_VIR * nrep) series[(size_t)slot * O_VIR * nrep + k] = rec[k];
+  if (k == 0) series_step[slot] = *steps_done;
+}
+
+__global__ void k_series_advance(long long* head) { *head += 1; }
+
+void launch_series(const DevState& s, cudaStream_t st, const double* rec, double* series, long long* series_step,
+                   long long* head, int cap) {
+  const int n = O_VIR * s.nrep;
+  k_series_store<<<(n + 255) / 256, 256, 0, st>>>(rec, s.nrep, series, series_step, head, cap, s.steps_done);
+  k_series_advance<<<1, 1, 0, st>>>(head);
+}
+
 void launch_observe(const DevState& s, const SimConst& C, cudaStream_t st, double* out) {
   k_observe<<<s.nrep, OBS_THREADS, 0, st>>>(s, C, out);
 }
@@ -483,7 +541,7 @@ __global__ void k_refresh_views(DevState s, float skin_half2) {
   const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
   const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
   const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
-  if (info_mobile(w) && dx * dx + dy * dy + dz * dz > skin_half2) *s.rebuild_flag = 1;
+  if (info_mobile(w) && dx * dx + dy * dy + dz * dz > skin_half2) flag_rebuild(s, info_rep(w));
 }
 
 void launch_refresh_views(const DevState& s, const SimConst& C, cudaStream_t st) {

@@ -12,13 +12,20 @@
 //                final order (replica, cell, tag) and every later FP sum order are deterministic;
 //   5. permute:  FP64 state gathered into the new order, views and rebuild references rewritten;
 //   6. list:     full neighbour list over the 27 surrounding cells (x,y periodic, z bounded).
-// Every kernel reads the flag first and exits when it is clear, so the sequence can sit inside a
-// captured CUDA graph and cost a few microseconds on steps that need no rebuild.
+// The decision is per replica, as the reference decides per system: the position kernel raises the
+// flag of the replica whose particle moved, and every kernel below skips the particles and cells of
+// the replicas that are not flagged (their slots, cells and lists stay as they are: a replica's
+// slots are one fixed range, its cells one fixed range, and its lists name only its own slots).
+// Every kernel reads the global flag first and exits when it is clear, so the sequence can sit
+// inside a captured CUDA graph and cost a few microseconds on steps that need no rebuild.
 #include "mfa_state.cuh"
 
 namespace mfa {
 
-__device__ __forceinline__ bool skip(const int* flag, bool force) { return !force && *flag == 0; }
+// nothing to rebuild at all
+__device__ __forceinline__ bool skip(const int* flag, bool force) { return !force && flag[0] == 0; }
+// nothing to rebuild for replica `rep`
+__device__ __forceinline__ bool rep_idle(const int* flag, int rep, bool force) { return !force && flag[1 + rep] == 0; }
 
 __device__ __forceinline__ void cell_coords(const RepDesc& R, double x, double y, double z, int& ix, int& iy,
                                             int& iz) {
@@ -30,9 +37,13 @@ __device__ __forceinline__ void cell_coords(const RepDesc& R, double x, double y
   iz = min(max(iz, 0), R.nc[2] - 1);
 }
 
-__global__ void k_zero_counts(int n, int* __restrict__ count, const int* flag, bool force) {
+// counts of the flagged replicas' cells (and the entry past the last cell) to zero; the other
+// replicas keep the counts of their last rebuild, which still describe their slots
+__global__ void k_zero_counts(int n, int* __restrict__ count, const int* __restrict__ cell_rep, const int* flag,
+                              bool force) {
   if (skip(flag, force)) return;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) count[c] = 0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+    if (c == n - 1 || !rep_idle(flag, cell_rep[c], force)) count[c] = 0;
 }
 
 __global__ void k_bin(DevState s, bool force) {
@@ -40,6 +51,7 @@ __global__ void k_bin(DevState s, bool force) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.N) return;
   int w = s.info[i];
+  if (rep_idle(s.rebuild_flag, info_rep(w), force)) return;
   const RepDesc& R = s.reps[info_rep(w)];
   int ix, iy, iz;
   if (s.mixed) {  // the list builder's integer formula on the fixed-point view
@@ -70,7 +82,7 @@ __global__ void k_bin(DevState s, bool force) {
   // Particles are still nearly sorted by cell, so neighbouring lanes share cells: the lanes of one
   // cell take consecutive ranks from a single atomicAdd (k_sort_cells orders each cell by tag
   // afterwards, so the order of the ranks does not matter).
-  const unsigned grp = __match_any_sync(__activemask(), c);
+  const unsigned grp = __match_any_sync(__activemask(), c);  // the lanes still here
   const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
   int base = 0;
   if (lane == leader) base = atomicAdd(&s.cell_count[c], __popc(grp));
@@ -156,6 +168,7 @@ __global__ void k_place(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.N) return;
+  if (rep_idle(s.rebuild_flag, info_rep(s.info[i]), force)) return;
   s.perm[s.cell_start[s.cell_of[i]] + s.rank[i]] = i;
 }
 
@@ -163,6 +176,7 @@ __global__ void k_sort_cells(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= s.ncell_tot) return;
+  if (rep_idle(s.rebuild_flag, s.cell_rep[c], force)) return;
   int b = s.cell_start[c], n = s.cell_count[c];
   for (int k = 1; k < n; ++k) {  // insertion sort by tag
     int p = s.perm[b + k];
@@ -180,6 +194,7 @@ __global__ void k_permute(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.N) return;
+  if (rep_idle(s.rebuild_flag, info_rep(s.info[i]), force)) return;  // slot i's replica
   int o = s.perm[i];
   s.tmp[0][i] = s.rx[o];
   s.tmp[1][i] = s.ry[o];
@@ -216,6 +231,7 @@ __global__ void k_copyback(DevState s, bool force) {
   if (skip(s.rebuild_flag, force)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.N) return;
+  if (rep_idle(s.rebuild_flag, info_rep(s.info[i]), force)) return;
   double x = s.tmp[0][i], y = s.tmp[1][i], z = s.tmp[2][i];
   double vx = s.tmp[3][i], vy = s.tmp[4][i], vz = s.tmp[5][i];
   s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
@@ -258,6 +274,11 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
   __shared__ int blk_max;
   const int cap = s.nbr_cap;
   int* mine = nl_sh + threadIdx.x * (NL_STAGE | 1);
+  const int i = blockIdx.x * NL_BLOCK + threadIdx.x;
+  const int w = (i < s.N) ? s.info[i] : 0;
+  const bool doit = i < s.N && !rep_idle(s.rebuild_flag, info_rep(w), force);  // the replica is rebuilt
+  // a block of replicas that are not rebuilt leaves at once (no table set-up, no status atomic)
+  if (!__syncthreads_or(doit)) return;
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
     rl2d[k] = s.tabd[k].rlist2;
     rl2f[k] = s.tabf ? s.tabf[k].rlist2 : 0.f;
@@ -269,10 +290,8 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
   }
   if (threadIdx.x == 0) blk_max = 0;
   __syncthreads();
-  const int i = blockIdx.x * NL_BLOCK + threadIdx.x;
-  const int w = (i < s.N) ? s.info[i] : 0;
   int cnt = 0, found = 0;  // entries stored, neighbours found (more when the list overflows)
-  if (i < s.N && info_mobile(w)) {
+  if (doit && info_mobile(w)) {
     const RepDesc& R = s.reps[info_rep(w)];
     const int ti = info_type(w);
     int ix, iy, iz;
@@ -380,7 +399,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
   __syncthreads();
   if (threadIdx.x == 0) atomicMax(s.status + 1, (unsigned)blk_max);  // largest count, for the host
   const int mx = min(blk_max, NL_STAGE);
-  if (i < s.N) {
+  if (doit) {
     for (int k = 0; k < mx; ++k)
       if (k < cnt) s.nbr[(size_t)k * s.Np + i] = mine[k];
     s.nn[i] = cnt;
@@ -388,7 +407,22 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
 }
 
 
-__global__ void k_clear_flag(int* flag) { *flag = 0; }
+// End of a rebuild: counts it (when some replica was flagged) and the flagged replicas' rebuilds,
+// then clears the flags.
+__global__ void k_clear_flags(int* flag, int nrep, long long* rebuilds, long long* rep_rebuilds) {
+  const bool any = flag[0] != 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
+    if (flag[1 + r]) {
+      rep_rebuilds[r] += 1;
+      flag[1 + r] = 0;
+    }
+  }
+  if (threadIdx.x == 0 && any) {
+    *rebuilds += 1;
+    flag[0] = 0;
+  }
+}
 
 void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   const int B = 256;
@@ -397,7 +431,7 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   // counts and scan run one entry past the last cell, so that cell_start[c + 1] ends every cell c
   const int nc1 = s.ncell_tot + 1;
   int nb = (nc1 + 1023) / 1024;
-  k_zero_counts<<<min((nc1 + B - 1) / B, 4096), B, 0, st>>>(nc1, s.cell_count, s.rebuild_flag, force);
+  k_zero_counts<<<min((nc1 + B - 1) / B, 4096), B, 0, st>>>(nc1, s.cell_count, s.cell_rep, s.rebuild_flag, force);
   k_bin<<<gN, B, 0, st>>>(s, force);
   k_scan_local<<<nb, 1024, 0, st>>>(nc1, s.cell_count, s.cell_start, s.scan_blk, s.rebuild_flag, force);
   k_scan_blocks<<<1, 1024, 0, st>>>(nb, s.scan_blk, s.rebuild_flag, force);
@@ -410,6 +444,7 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   auto kern = var == 2 ? k_nlist<true, true> : var == 1 ? k_nlist<true, false> : k_nlist<false, false>;
   const int gl = (s.N + NL_BLOCK - 1) / NL_BLOCK;
   kern<<<gl, NL_BLOCK, 0, st>>>(s, force);
+  k_clear_flags<<<1, 256, 0, st>>>(s.rebuild_flag, s.nrep, s.rebuilds, s.rep_rebuilds);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -33,7 +33,10 @@ struct DevState {
   int ncell_tot;
   // control words
   float rl2_uni;  // SimConst::rl2_uni_f (0: per-pair list cut-offs)
-  int* rebuild_flag;
+  int* rebuild_flag;          // [1 + nrep]: [0] some replica needs a rebuild, [1 + r] replica r does
+  int* cell_rep;              // [ncell_tot] replica of each list cell
+  long long* rebuilds;        // [1] rebuild events (any replica)
+  long long* rep_rebuilds;    // [nrep] rebuilds of each replica
   unsigned* status;
   long long* steps_done;
   // tables
@@ -117,8 +120,15 @@ __device__ __forceinline__ void sym_add(T* w6, T c, T dx, T dy, T dz) {
   w6[3] += cx * dy; w6[4] += cx * dz; w6[5] += cy * dz;
 }
 
-// ---- rebuild (cell sort + neighbour list); `force` runs it even when the flag is clear -------
+// ---- rebuild (cell sort + neighbour list) --------------------------------------------------------
+// Rebuilds the replicas whose flag is set (every replica when `force`), then counts the rebuild
+// and clears the flags.
 void launch_rebuild(const DevState& s, cudaStream_t st, bool force);
+// The skin test's outcome for replica `rep` (check_skin.f90:11-24 decides per system).
+__device__ __forceinline__ void flag_rebuild(const DevState& s, int rep) {
+  s.rebuild_flag[1 + rep] = 1;
+  s.rebuild_flag[0] = 1;
+}
 // largest neighbour-list capacity (entries per particle) a context may grow to
 constexpr int NL_CAP_MAX = 420;
 // ---- forces ------------------------------------------------------------------------------------
@@ -142,6 +152,12 @@ void launch_profiles(const DevState& s, const SimConst& C, cudaStream_t st, doub
 void launch_record(Acc acc, double* out, cudaStream_t st);
 // observation quantities per replica: out[9 r + 0..2] brush Rg^2, 3..5 melt Rg^2, 6..8 momentum
 void launch_observe(const DevState& s, const SimConst& C, cudaStream_t st, double* out);
+// one observation into the averages avg[nrep][NAVG] (mfa_obs.cuh) from the record and out above
+void launch_obs_accum(const DevState& s, const SimConst& C, cudaStream_t st, const double* rec, const double* obs,
+                      double* avg);
+// the record's energy slots into the series ring [cap][O_VIR][nrep] at *head, then ++*head
+void launch_series(const DevState& s, cudaStream_t st, const double* rec, double* series, long long* series_step,
+                   long long* head, int cap);
 // ---- host <-> device layout ----------------------------------------------------------------------
 // canonical AoS (3*tag+d) <-> slot order
 void launch_scatter_state(const DevState& s, cudaStream_t st, const double* r, const double* v,

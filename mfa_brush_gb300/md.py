@@ -68,7 +68,7 @@ def read_deck(deck_dir, conf="conf_old"):
 
 
 def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, device=0, nbr_capacity=0,
-            profile_from_step=0, block_size=0, kspace_plain_sums=False):
+            profile_from_step=0, block_size=0, kspace_plain_sums=False, observe=False, series_capacity=0):
     o = abi.Options()
     _lib().mfa_default_options(C.byref(o))
     o.precision = abi.PREC_MIXED if precision in ("mixed", abi.PREC_MIXED) else abi.PREC_FP64
@@ -80,6 +80,8 @@ def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, devic
     o.profile_from_step = profile_from_step
     o.block_size = block_size
     o.kspace_plain_sums = 1 if kspace_plain_sums else 0
+    o.observe = 1 if observe else 0
+    o.series_capacity = series_capacity
     return o
 
 
@@ -252,6 +254,23 @@ class MdSystem:
         self._ck(self.lib.mfa_kspace_info(self.ctx, C.byref(nk), C.byref(nq)))
         return nk.value, nq.value
 
+    def averages(self):
+        """Observation averages of every replica (options observe=True), a list of dicts."""
+        o = (abi.Averages * self.nrep)()
+        self._ck(self.lib.mfa_get_averages(self.ctx, o))
+        return [x.as_dict() for x in o]
+
+    def reset_averages(self):
+        self._ck(self.lib.mfa_reset_averages(self.ctx))
+
+    def energy_series(self, cap=100000):
+        """Energy records stored since the last call (options series_capacity > 0): a list over
+        records of lists over replicas of energy dicts."""
+        out = (abi.Energies * (cap * self.nrep))()
+        n = abi.i32(0)
+        self._ck(self.lib.mfa_get_energy_series(self.ctx, out, cap, C.byref(n)))
+        return [[out[k * self.nrep + r].as_dict() for r in range(self.nrep)] for k in range(n.value)]
+
     def virial(self):
         """Virial tensors per term group, kinetic and pressure tensors of every replica, from the
         last energy record (see mfa_get_virial); a list of dicts of 3x3 arrays."""
@@ -328,6 +347,12 @@ class MdSystem:
         cnt = (abi.i32 * abi.NKFAM)()
         self._ck(self.lib.mfa_kernel_times(self.ctx, nsteps, ms, cnt))
         return {self.lib.mfa_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(abi.NKFAM)}
+
+    def replica_rebuild_counts(self):
+        """Rebuilds of each replica since the context was made."""
+        out = np.zeros(self.nrep, np.int64)
+        self._ck(self.lib.mfa_replica_rebuild_counts(self.ctx, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
 
     def rebuild_count(self):
         n = abi.i64(0)

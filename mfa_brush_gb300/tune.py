@@ -3,9 +3,10 @@
 The skin trades the list rebuild (sort + list build, whose frequency falls as the skin grows) for
 the pair kernel (whose lists lengthen with it).  The best value depends on the density, the
 temperature, the time step and the replica mix, so it is measured: the fused step is timed at
-each candidate skin, over enough steps to include several rebuilds.  The rebuild fires when any
-particle of the batch has moved half the skin, so its rate grows with the number of particles:
-time the whole batch (n_sample >= the replica count) when the tuned skin is for that batch.
+each candidate skin, over enough steps to include several rebuilds.  A replica is rebuilt when one
+of its own particles has moved half the skin, and a step with any rebuild pays the fixed cost of
+the sort's passes over the whole batch, so the rate and cost depend on the batch: time the whole
+batch (n_sample >= the replica count) when the tuned skin is for that batch.
 """
 import numpy as np
 
@@ -20,7 +21,7 @@ def sample_replicas(reps, n_sample):
     return [reps[k] for k in sorted(set(idx.tolist()))]
 
 
-def tune_skin(params, reps, candidates=(0.5, 0.6, 0.7, 0.8, 0.9), n_sample=32, steps=80, warmup=20,
+def tune_skin(params, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9), n_sample=32, steps=80, warmup=20,
               precision="mixed", device=0, chunk=10):
     """Times mfa_step on a sample of `reps` (list of (System, a_type, r0, v)) at each candidate
     skin; returns (best skin, {skin: atom-steps/s})."""

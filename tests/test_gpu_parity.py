@@ -197,20 +197,29 @@ def test_wca_channel_fused_mixed_vs_oracle(gpu, oracle_mod):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_batched_replicas_equal_single(gpu, precision):
-    """A replica inside a batch gets bit-identical forces to the same replica run alone."""
+    """A replica inside a batch gets a bit-identical trajectory to the same replica run alone,
+    rebuilds included: each replica is rebuilt when its own particles have moved half the skin
+    (check_skin.f90 decides per system), so its sort order and lists do not depend on the others.
+    The cold replica (velocities scaled by 0.1) is rebuilt less often than the others."""
     p = configs.wca_params(gamma=5.0)
     reps = [configs.brush_channel(15.0, 12.0, 0.2, 20, seed=11),
             configs.brush_channel(18.0, 15.0, 0.1, 35, seed=12),
             configs.brush_channel(16.0, 10.0, 0.05, 50, seed=13)]
+    s2, a2, r2, v2 = reps[2]
+    reps[2] = (s2, a2, r2, v2 * 0.1)
     systems, a_type, r0, v = configs.concat(reps)
-    gb = md.MdSystem(p, systems, a_type, r0, v, precision=precision)
-    gb.step(3)
+    # an ample list capacity: a capacity growth rebuilds every replica at once
+    gb = md.MdSystem(p, systems, a_type, r0, v, precision=precision, nbr_capacity=160)
+    gb.step(60)
     rb, vb, ab, fb = gb.state()
+    counts = gb.replica_rebuild_counts()
+    assert counts.min() >= 0 and counts.max() >= 2 and counts[2] < counts.max()
     off = 0
-    for (s, at, r, vv) in reps:
-        g1 = md.MdSystem(p, s, at, r, vv, precision=precision)
-        g1.step(3)
+    for k, (s, at, r, vv) in enumerate(reps):
+        g1 = md.MdSystem(p, s, at, r, vv, precision=precision, nbr_capacity=160)
+        g1.step(60)
         r1, v1, a1, f1 = g1.state()
+        assert g1.replica_rebuild_counts()[0] == counts[k]
         n = s.n_part
         assert np.array_equal(r1, rb[off:off + n])
         assert np.array_equal(v1, vb[off:off + n])

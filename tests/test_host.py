@@ -40,7 +40,7 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
     from mfa_brush_gb300 import abi
     names = {"mfa_inputs": abi.Inputs, "mfa_params": abi.Params, "mfa_system": abi.System,
              "mfa_options": abi.Options, "mfa_energies": abi.Energies, "mfa_observables": abi.Observables,
-             "mfa_virial": abi.Virial}
+             "mfa_virial": abi.Virial, "mfa_averages": abi.Averages}
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include "mfa_gpu.h"\nint main(void) {\n' +
                    "".join('  printf("%%zu\\n", sizeof(%s));\n' % n for n in names) + "  return 0;\n}\n")
