@@ -158,12 +158,13 @@ __global__ void k_clear_overflow(unsigned* status) {
 }
 
 // rebuild of the flagged replicas (all of them when forced); counts and clears the flags
+constexpr int kRebuildLaunches = 12;
 void rebuild(mfa_ctx* ctx, bool force) {
   launch_rebuild(ctx->S, ctx->st, force);
-  ctx->launches += 11;
+  ctx->launches += kRebuildLaunches;
 }
 
-// Graph form of the skin check: the IF body (the eleven rebuild kernels) runs only on steps whose
+// Graph form of the skin check: the IF body (the twelve rebuild kernels) runs only on steps whose
 // position update raised the flag of some replica; other steps launch nothing.
 __global__ void k_cond_rebuild(const int* flag, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, flag[0] ? 1u : 0u);
@@ -693,6 +694,12 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.cell_start, cell_off + 1);
   DA(S.scan_blk, (cell_off + 1023) / 1024 + 1);
   DA(S.rebuild_flag, 1 + n_rep);
+  DA(S.wl_rep, n_rep + 1);
+  DA(S.wl_p, n_rep + 1);
+  DA(S.wl_c, n_rep + 1);
+  DA(S.wl_k, n_rep + 1);
+  DA(S.wl_n, 2);
+  CK(cudaDeviceGetAttribute(&S.nsm, cudaDevAttrMultiProcessorCount, ctx->device));
   DA(S.cell_rep, cell_off);
   DA(S.rebuilds, 1);
   DA(S.rep_rebuilds, n_rep);
@@ -1095,7 +1102,7 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs
       L += 1;  // the rebuild body's launches are not counted: they run only when triggered
     } else {
       launch_rebuild(S, st, false);
-      L += 11;
+      L += kRebuildLaunches;
     }
     // mixed: bonded terms inside the pair kernel; FP64: their own kernel
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);

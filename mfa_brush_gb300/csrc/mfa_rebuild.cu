@@ -13,19 +13,20 @@
 //   5. permute:  FP64 state gathered into the new order, views and rebuild references rewritten;
 //   6. list:     full neighbour list over the 27 surrounding cells (x,y periodic, z bounded).
 // The decision is per replica, as the reference decides per system: the position kernel raises the
-// flag of the replica whose particle moved, and every kernel below skips the particles and cells of
-// the replicas that are not flagged (their slots, cells and lists stay as they are: a replica's
+// flag of the replica whose particle moved.  k_worklist lists the flagged replicas with prefix sums
+// of their particles, cells and list chunks, and every kernel after it strides over that work on a
+// grid of fixed size; the other replicas' slots, cells and lists stay as they are (a replica's
 // slots are one fixed range, its cells one fixed range, and its lists name only its own slots).
-// Every kernel reads the global flag first and exits when it is clear, so the sequence can sit
-// inside a captured CUDA graph and cost a few microseconds on steps that need no rebuild.
+// In a captured CUDA graph the sequence sits in the body of a conditional node that runs only on
+// steps where some replica is flagged.
+#include <algorithm>
+
 #include "mfa_state.cuh"
 
 namespace mfa {
 
 // nothing to rebuild at all
 __device__ __forceinline__ bool skip(const int* flag, bool force) { return !force && flag[0] == 0; }
-// nothing to rebuild for replica `rep`
-__device__ __forceinline__ bool rep_idle(const int* flag, int rep, bool force) { return !force && flag[1 + rep] == 0; }
 
 __device__ __forceinline__ void cell_coords(const RepDesc& R, double x, double y, double z, int& ix, int& iy,
                                             int& iz) {
@@ -37,21 +38,133 @@ __device__ __forceinline__ void cell_coords(const RepDesc& R, double x, double y
   iz = min(max(iz, 0), R.nc[2] - 1);
 }
 
-// counts of the flagged replicas' cells (and the entry past the last cell) to zero; the other
-// replicas keep the counts of their last rebuild, which still describe their slots
-__global__ void k_zero_counts(int n, int* __restrict__ count, const int* __restrict__ cell_rep, const int* flag,
-                              bool force) {
-  if (skip(flag, force)) return;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-    if (c == n - 1 || !rep_idle(flag, cell_rep[c], force)) count[c] = 0;
+// ---- work list ------------------------------------------------------------------------------
+// The kernels of a rebuild stride over the work of the listed replicas only (their particles,
+// cells or list-builder chunks) on grids of a fixed size, so a rebuild of a few replicas costs
+// little more than their own work.
+constexpr int WL_THREADS = 1024;
+// particles per block of the list builder (one chunk of a replica's slots)
+constexpr int NL_BLOCK = 128;
+
+// The replicas to rebuild (flagged, or all when forced) and the prefix sums of their particles,
+// cells and list chunks: one block, a scan over the replicas in chunks of its threads.
+__global__ void __launch_bounds__(WL_THREADS) k_worklist(DevState s, bool force) {
+  __shared__ int sc[4][WL_THREADS / 32];
+  __shared__ int carry[4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const bool any = force || s.rebuild_flag[0] != 0;
+  if (threadIdx.x < 4) carry[threadIdx.x] = 0;
+  __syncthreads();
+  for (int base = 0; base < s.nrep && any; base += WL_THREADS) {
+    const int r = base + threadIdx.x;
+    const bool sel = r < s.nrep && (force || s.rebuild_flag[1 + r] != 0);
+    int v[4] = {0, 0, 0, 0};
+    if (sel) {
+      const RepDesc& R = s.reps[r];
+      v[0] = 1; v[1] = R.n_part; v[2] = R.ncell; v[3] = (R.n_part + NL_BLOCK - 1) / NL_BLOCK;
+    }
+    int x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {  // inclusive warp scans
+      x[q] = v[q];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x[q], o);
+        if (lane >= o) x[q] += y;
+      }
+      if (lane == 31) sc[q][wid] = x[q];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int t = sc[q][lane];
+        int u = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, u, o);
+          if (lane >= o) u += y;
+        }
+        sc[q][lane] = u - t;  // exclusive warp offsets
+      }
+    }
+    __syncthreads();
+    int ex[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ex[q] = carry[q] + sc[q][wid] + x[q] - v[q];
+    if (sel) {
+      s.wl_rep[ex[0]] = r;
+      s.wl_p[ex[0]] = ex[1];
+      s.wl_c[ex[0]] = ex[2];
+      s.wl_k[ex[0]] = ex[3];
+    }
+    __syncthreads();
+    if (threadIdx.x == WL_THREADS - 1 || r == s.nrep - 1)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) carry[q] = ex[q] + v[q];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int n = any ? carry[0] : 0;
+    s.wl_n[0] = n;
+    s.wl_n[1] = 0;  // the list builder's chunk queue
+    s.wl_p[n] = any ? carry[1] : 0;
+    s.wl_c[n] = any ? carry[2] : 0;
+    s.wl_k[n] = any ? carry[3] : 0;
+  }
 }
 
-__global__ void k_bin(DevState s, bool force) {
-  if (skip(s.rebuild_flag, force)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.N) return;
+// Work item g of a prefix array pre (n listed replicas) -> its replica r and index loc inside it:
+// the last k with pre[k] <= g, found by a binary search.
+__device__ __forceinline__ int wl_find(const int* __restrict__ pre, int n, int g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&pre[mid]) <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ void wl_map(const int* __restrict__ pre, const int* __restrict__ list, int n, int g,
+                                       int& r, int& loc) {
+  const int k = wl_find(pre, n, g);
+  r = __ldg(&list[k]);
+  loc = g - __ldg(&pre[k]);
+}
+// The same for the lanes of a warp that hold consecutive items (a grid-stride loop): the first
+// active lane searches, the others step forward from its replica.
+__device__ __forceinline__ void wl_map_warp(const int* __restrict__ pre, const int* __restrict__ list, int n, int g,
+                                            int& r, int& loc) {
+  const unsigned m = __activemask();
+  const int leader = __ffs(m) - 1;
+  int k = 0;
+  if ((int)(threadIdx.x & 31) == leader) k = wl_find(pre, n, g);
+  k = __shfl_sync(m, k, leader);
+  while (k + 1 < n && __ldg(&pre[k + 1]) <= g) ++k;
+  r = __ldg(&list[k]);
+  loc = g - __ldg(&pre[k]);
+}
+
+#define WL_FOR(pre, g)                                                                             \
+  const int wl_cnt_ = *s.wl_n;                                                                     \
+  const int wl_tot_ = s.pre[wl_cnt_];                                                              \
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < wl_tot_; g += gridDim.x * blockDim.x)
+
+// counts of the listed replicas' cells to zero; the other replicas keep the counts of their last
+// rebuild, which still describe their slots (the entry past the last cell stays zero)
+__global__ void k_zero_counts(DevState s) {
+  WL_FOR(wl_c, g) {
+    int r, c;
+    wl_map_warp(s.wl_c, s.wl_rep, wl_cnt_, g, r, c);
+    s.cell_count[s.reps[r].cell_off + c] = 0;
+  }
+}
+
+__global__ void k_bin(DevState s) {
+  WL_FOR(wl_p, g) {
+  int rr, loc;
+  wl_map_warp(s.wl_p, s.wl_rep, wl_cnt_, g, rr, loc);
+  const int i = s.reps[rr].p0 + loc;
   int w = s.info[i];
-  if (rep_idle(s.rebuild_flag, info_rep(w), force)) return;
   const RepDesc& R = s.reps[info_rep(w)];
   int ix, iy, iz;
   if (s.mixed) {  // the list builder's integer formula on the fixed-point view
@@ -88,6 +201,7 @@ __global__ void k_bin(DevState s, bool force) {
   if (lane == leader) base = atomicAdd(&s.cell_count[c], __popc(grp));
   base = __shfl_sync(grp, base, leader);
   s.rank[i] = base + __popc(grp & ((1u << lane) - 1u));
+  }
 }
 
 // exclusive scan, 1024 elements per block
@@ -164,19 +278,20 @@ __global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__
   if (i < n) out[i] += blk[blockIdx.x];
 }
 
-__global__ void k_place(DevState s, bool force) {
-  if (skip(s.rebuild_flag, force)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.N) return;
-  if (rep_idle(s.rebuild_flag, info_rep(s.info[i]), force)) return;
-  s.perm[s.cell_start[s.cell_of[i]] + s.rank[i]] = i;
+__global__ void k_place(DevState s) {
+  WL_FOR(wl_p, g) {
+    int r, loc;
+    wl_map_warp(s.wl_p, s.wl_rep, wl_cnt_, g, r, loc);
+    const int i = s.reps[r].p0 + loc;
+    s.perm[s.cell_start[s.cell_of[i]] + s.rank[i]] = i;
+  }
 }
 
-__global__ void k_sort_cells(DevState s, bool force) {
-  if (skip(s.rebuild_flag, force)) return;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= s.ncell_tot) return;
-  if (rep_idle(s.rebuild_flag, s.cell_rep[c], force)) return;
+__global__ void k_sort_cells(DevState s) {
+  WL_FOR(wl_c, g) {
+  int r, lc;
+  wl_map_warp(s.wl_c, s.wl_rep, wl_cnt_, g, r, lc);
+  const int c = s.reps[r].cell_off + lc;
   int b = s.cell_start[c], n = s.cell_count[c];
   for (int k = 1; k < n; ++k) {  // insertion sort by tag
     int p = s.perm[b + k];
@@ -188,13 +303,14 @@ __global__ void k_sort_cells(DevState s, bool force) {
     }
     s.perm[b + m + 1] = p;
   }
+  }
 }
 
-__global__ void k_permute(DevState s, bool force) {
-  if (skip(s.rebuild_flag, force)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.N) return;
-  if (rep_idle(s.rebuild_flag, info_rep(s.info[i]), force)) return;  // slot i's replica
+__global__ void k_permute(DevState s) {
+  WL_FOR(wl_p, g) {
+  int r, loc;
+  wl_map_warp(s.wl_p, s.wl_rep, wl_cnt_, g, r, loc);
+  const int i = s.reps[r].p0 + loc;
   int o = s.perm[i];
   s.tmp[0][i] = s.rx[o];
   s.tmp[1][i] = s.ry[o];
@@ -207,6 +323,7 @@ __global__ void k_permute(DevState s, bool force) {
   s.tmp[8][i] = s.az[o];
   s.tmp_tag[i] = s.tag[o];
   s.tmp_info[i] = s.info[o];
+  }
 }
 
 // Writes the pair-kernel views of slot i and returns the fixed-point position (w in q.w).
@@ -227,11 +344,11 @@ __device__ __forceinline__ int4 write_views(const DevState& s, int i, const RepD
   return q;
 }
 
-__global__ void k_copyback(DevState s, bool force) {
-  if (skip(s.rebuild_flag, force)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.N) return;
-  if (rep_idle(s.rebuild_flag, info_rep(s.info[i]), force)) return;
+__global__ void k_copyback(DevState s) {
+  WL_FOR(wl_p, g) {
+  int rr, loc;
+  wl_map_warp(s.wl_p, s.wl_rep, wl_cnt_, g, rr, loc);
+  const int i = s.reps[rr].p0 + loc;
   double x = s.tmp[0][i], y = s.tmp[1][i], z = s.tmp[2][i];
   double vx = s.tmp[3][i], vy = s.tmp[4][i], vz = s.tmp[5][i];
   s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
@@ -245,6 +362,7 @@ __global__ void k_copyback(DevState s, bool force) {
   int4 q = write_views(s, i, R, x, y, z, vx, vy, vz, w, t);
   q.w = 0;
   s.ref[i] = q;
+  }
 }
 
 // Full Verlet list: every mobile particle lists all j (mobile or wall) with r^2 < (rc_ij+skin)^2.
@@ -258,27 +376,25 @@ __global__ void k_copyback(DevState s, bool force) {
 // k-th neighbours of 128 consecutive particles are 128 consecutive ints of nbr, so every store is
 // coalesced (scattered 4-byte stores into the column-major list cost read-modify-writes in HBM).
 // The fixed staging size keeps the shared memory (17 KB per block) independent of the list
-// capacity, so eight blocks fit on an SM.
-constexpr int NL_BLOCK = 128;
+// capacity, so eight blocks fit on an SM.  The blocks take chunks of the replicas being rebuilt
+// from a queue.
 // entries per particle staged in shared memory (the first NL_STAGE rows of the list are written
 // coalesced; a particle with more neighbours writes the rest straight to the list)
 constexpr int NL_STAGE = 32;
 
 template <bool MIXED, bool UNI>
-__global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
-  if (skip(s.rebuild_flag, force)) return;
+__global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s) {
+  const int nwl = *s.wl_n;
+  const int nchunks = s.wl_k[nwl];
+  if ((int)blockIdx.x >= nchunks) return;
   __shared__ int nl_sh[NL_BLOCK * (NL_STAGE | 1)];
   __shared__ float rl2f[NPAIR];
   __shared__ double rl2d[NPAIR];
   __shared__ float rlmax[MAXT];
   __shared__ int blk_max;
+  __shared__ int chunk;
   const int cap = s.nbr_cap;
   int* mine = nl_sh + threadIdx.x * (NL_STAGE | 1);
-  const int i = blockIdx.x * NL_BLOCK + threadIdx.x;
-  const int w = (i < s.N) ? s.info[i] : 0;
-  const bool doit = i < s.N && !rep_idle(s.rebuild_flag, info_rep(w), force);  // the replica is rebuilt
-  // a block of replicas that are not rebuilt leaves at once (no table set-up, no status atomic)
-  if (!__syncthreads_or(doit)) return;
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
     rl2d[k] = s.tabd[k].rlist2;
     rl2f[k] = s.tabf ? s.tabf[k].rlist2 : 0.f;
@@ -288,6 +404,19 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
     for (int t = 0; t < MAXT; ++t) m = fmax(m, s.tabd[threadIdx.x * MAXT + t].rlist2);
     rlmax[threadIdx.x] = (float)m * 1.0004f;
   }
+  for (;;) {
+  // the next chunk from the queue (chunks differ in cost: a queue keeps the blocks busy)
+  __syncthreads();
+  if (threadIdx.x == 0) chunk = atomicAdd(s.wl_n + 1, 1);
+  __syncthreads();
+  const int ch = chunk;
+  if (ch >= nchunks) break;
+  int rc, kc;  // the chunk's replica and its index there (the same for the whole block)
+  wl_map(s.wl_k, s.wl_rep, nwl, ch, rc, kc);
+  const int i0 = s.reps[rc].p0 + kc * NL_BLOCK, i1 = min(s.reps[rc].p0 + s.reps[rc].n_part, i0 + NL_BLOCK);
+  const int i = i0 + threadIdx.x;
+  const bool doit = i < i1;
+  const int w = doit ? s.info[i] : 0;
   if (threadIdx.x == 0) blk_max = 0;
   __syncthreads();
   int cnt = 0, found = 0;  // entries stored, neighbours found (more when the list overflows)
@@ -404,6 +533,8 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s, bool force) {
       if (k < cnt) s.nbr[(size_t)k * s.Np + i] = mine[k];
     s.nn[i] = cnt;
   }
+  __syncthreads();  // the staging area and blk_max are reused by the next chunk
+  }
 }
 
 
@@ -426,24 +557,28 @@ __global__ void k_clear_flags(int* flag, int nrep, long long* rebuilds, long lon
 
 void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   const int B = 256;
-  int gN = (s.N + B - 1) / B;
-  int gC = (s.ncell_tot + B - 1) / B;
-  // counts and scan run one entry past the last cell, so that cell_start[c + 1] ends every cell c
+  // fixed grids that stride over the work list: a few waves of the GPU, at most what the largest
+  // work (every particle or cell) fills
+  const int gN = std::min((s.N + B - 1) / B, s.nsm * 8);
+  const int gC = std::min((s.ncell_tot + B - 1) / B, s.nsm * 8);
+  // the scan runs over every cell and one entry past the last, so that cell_start[c + 1] ends
+  // every cell c; the cells of the replicas not rebuilt keep their counts and so their starts
   const int nc1 = s.ncell_tot + 1;
   int nb = (nc1 + 1023) / 1024;
-  k_zero_counts<<<min((nc1 + B - 1) / B, 4096), B, 0, st>>>(nc1, s.cell_count, s.cell_rep, s.rebuild_flag, force);
-  k_bin<<<gN, B, 0, st>>>(s, force);
+  k_worklist<<<1, WL_THREADS, 0, st>>>(s, force);
+  k_zero_counts<<<gC, B, 0, st>>>(s);
+  k_bin<<<gN, B, 0, st>>>(s);
   k_scan_local<<<nb, 1024, 0, st>>>(nc1, s.cell_count, s.cell_start, s.scan_blk, s.rebuild_flag, force);
   k_scan_blocks<<<1, 1024, 0, st>>>(nb, s.scan_blk, s.rebuild_flag, force);
   k_scan_add<<<nb, 1024, 0, st>>>(nc1, s.cell_start, s.scan_blk, s.rebuild_flag, force);
-  k_place<<<gN, B, 0, st>>>(s, force);
-  k_sort_cells<<<gC, B, 0, st>>>(s, force);
-  k_permute<<<gN, B, 0, st>>>(s, force);
-  k_copyback<<<gN, B, 0, st>>>(s, force);
+  k_place<<<gN, B, 0, st>>>(s);
+  k_sort_cells<<<gC, B, 0, st>>>(s);
+  k_permute<<<gN, B, 0, st>>>(s);
+  k_copyback<<<gN, B, 0, st>>>(s);
   const int var = s.mixed ? (s.rl2_uni > 0.f ? 2 : 1) : 0;
   auto kern = var == 2 ? k_nlist<true, true> : var == 1 ? k_nlist<true, false> : k_nlist<false, false>;
-  const int gl = (s.N + NL_BLOCK - 1) / NL_BLOCK;
-  kern<<<gl, NL_BLOCK, 0, st>>>(s, force);
+  const int gl = std::min((s.N + NL_BLOCK - 1) / NL_BLOCK, s.nsm * 8);
+  kern<<<gl, NL_BLOCK, 0, st>>>(s);
   k_clear_flags<<<1, 256, 0, st>>>(s.rebuild_flag, s.nrep, s.rebuilds, s.rep_rebuilds);
 }
 

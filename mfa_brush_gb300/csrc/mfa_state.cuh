@@ -35,6 +35,11 @@ struct DevState {
   float rl2_uni;  // SimConst::rl2_uni_f (0: per-pair list cut-offs)
   int* rebuild_flag;          // [1 + nrep]: [0] some replica needs a rebuild, [1 + r] replica r does
   int* cell_rep;              // [ncell_tot] replica of each list cell
+  // work list of a rebuild (k_worklist): the replicas to rebuild in ascending order (wl_rep), the
+  // prefix sums over them of their particles (wl_p), cells (wl_c) and list-builder chunks (wl_k),
+  // each [nrep + 1], their number (wl_n[0]) and the list builder's chunk queue (wl_n[1])
+  int *wl_rep, *wl_p, *wl_c, *wl_k, *wl_n;
+  int nsm;                    // streaming multiprocessors of the device (grids of the rebuild)
   long long* rebuilds;        // [1] rebuild events (any replica)
   long long* rep_rebuilds;    // [nrep] rebuilds of each replica
   unsigned* status;
