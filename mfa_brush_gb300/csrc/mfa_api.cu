@@ -692,7 +692,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   S.ncell_tot = cell_off;
   DA(S.cell_count, cell_off + 1);
   DA(S.cell_start, cell_off + 1);
-  DA(S.scan_blk, (cell_off + 1023) / 1024 + 1);
+  DA(S.scan_blk, 2 * 256);  // the cell-start scan's block sums and offsets
   DA(S.rebuild_flag, 1 + n_rep);
   DA(S.wl_rep, n_rep + 1);
   DA(S.wl_p, n_rep + 1);

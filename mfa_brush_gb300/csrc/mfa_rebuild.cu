@@ -6,7 +6,7 @@
 // list is rebuilt when the position kernel has raised `rebuild_flag` (displacement > skin/2):
 //   1. bin:      cell of every particle on the replica's list grid (cell edge >= r_cut_max+skin),
 //                per-cell counts with one atomic per particle;
-//   2. scan:     exclusive prefix sum of the counts (three kernels);
+//   2. scan:     cell starts from the counts of the rebuilt replicas' cells (three kernels);
 //   3. place:    particle -> (cell start + atomic rank);
 //   4. order:    each cell's segment sorted by tag (cells hold a handful of particles), so the
 //                final order (replica, cell, tag) and every later FP sum order are deterministic;
@@ -25,8 +25,6 @@
 
 namespace mfa {
 
-// nothing to rebuild at all
-__device__ __forceinline__ bool skip(const int* flag, bool force) { return !force && flag[0] == 0; }
 
 __device__ __forceinline__ void cell_coords(const RepDesc& R, double x, double y, double z, int& ix, int& iy,
                                             int& iz) {
@@ -108,6 +106,7 @@ __global__ void __launch_bounds__(WL_THREADS) k_worklist(DevState s, bool force)
     const int n = any ? carry[0] : 0;
     s.wl_n[0] = n;
     s.wl_n[1] = 0;  // the list builder's chunk queue
+    s.cell_start[s.ncell_tot] = s.N;  // the end of the last cell
     s.wl_p[n] = any ? carry[1] : 0;
     s.wl_c[n] = any ? carry[2] : 0;
     s.wl_k[n] = any ? carry[3] : 0;
@@ -132,8 +131,8 @@ __device__ __forceinline__ void wl_map(const int* __restrict__ pre, const int* _
 }
 // The same for the lanes of a warp that hold consecutive items (a grid-stride loop): the first
 // active lane searches, the others step forward from its replica.
-__device__ __forceinline__ void wl_map_warp(const int* __restrict__ pre, const int* __restrict__ list, int n, int g,
-                                            int& r, int& loc) {
+__device__ __forceinline__ int wl_map_warp(const int* __restrict__ pre, const int* __restrict__ list, int n, int g,
+                                           int& r, int& loc) {
   const unsigned m = __activemask();
   const int leader = __ffs(m) - 1;
   int k = 0;
@@ -142,6 +141,7 @@ __device__ __forceinline__ void wl_map_warp(const int* __restrict__ pre, const i
   while (k + 1 < n && __ldg(&pre[k + 1]) <= g) ++k;
   r = __ldg(&list[k]);
   loc = g - __ldg(&pre[k]);
+  return k;  // the position in the list
 }
 
 #define WL_FOR(pre, g)                                                                             \
@@ -204,78 +204,120 @@ __global__ void k_bin(DevState s) {
   }
 }
 
-// exclusive scan, 1024 elements per block
-__global__ void __launch_bounds__(1024) k_scan_local(int n, const int* __restrict__ in, int* __restrict__ out,
-                                                     int* __restrict__ blk, const int* flag, bool force) {
-  if (skip(flag, force)) return;
+// ---- cell starts of the listed replicas ---------------------------------------------------------
+// The cells of the listed replicas, one after another in list order, form one sequence g; E[g] is
+// the exclusive prefix sum of their counts.  A replica's counts sum to its particle count, so E at
+// the first cell of the k-th listed replica is wl_p[k], and the start of cell g is
+// p0 + E[g] - wl_p[k].  The starts of the other replicas' cells stay as they were, and the first
+// cell of every replica starts at its p0, so cell_start[c + 1] ends every cell c.  Three kernels on
+// a fixed grid of SCAN_BLOCKS blocks: each block's share of the sequence is summed, the block sums
+// are scanned, and each block scans its share again from its offset and writes the starts.
+constexpr int SCAN_BLOCKS = 256;
+constexpr int SCAN_T = 1024;
+
+__device__ __forceinline__ void scan_share(const DevState& s, int& lo, int& hi) {
+  const int tot = s.wl_c[*s.wl_n];
+  const int seg = ((tot + SCAN_BLOCKS - 1) / SCAN_BLOCKS + SCAN_T - 1) / SCAN_T * SCAN_T;
+  lo = min(tot, (int)blockIdx.x * seg);
+  hi = min(tot, lo + seg);
+}
+
+// block sum of v (all threads); the total in every thread
+__device__ __forceinline__ int block_sum_int(int v, int* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  int t = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_wscan_sum(DevState s) {
+  __shared__ int red[SCAN_T / 32];
+  int lo, hi;
+  scan_share(s, lo, hi);
+  const int n = *s.wl_n;
+  int v = 0;
+  for (int g = lo + threadIdx.x; g < hi; g += SCAN_T) {
+    int r, c;
+    wl_map_warp(s.wl_c, s.wl_rep, n, g, r, c);
+    v += s.cell_count[s.reps[r].cell_off + c];
+  }
+  v = block_sum_int(v, red);
+  if (threadIdx.x == 0) s.scan_blk[blockIdx.x] = v;
+}
+
+// exclusive scan of the SCAN_BLOCKS block sums (one block)
+__global__ void __launch_bounds__(SCAN_T) k_wscan_blocks(DevState s) {
   __shared__ int warp_tot[32];
-  int i = blockIdx.x * 1024 + threadIdx.x;
-  int v = (i < n) ? in[i] : 0;
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int v = threadIdx.x < SCAN_BLOCKS ? s.scan_blk[threadIdx.x] : 0;
   int x = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, x, o);
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
   if (lane == 31) warp_tot[wid] = x;
   __syncthreads();
   if (wid == 0) {
-    int t = warp_tot[lane];
+    const int t = warp_tot[lane];
     int u = t;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, u, o);
+      const int y = __shfl_up_sync(0xffffffffu, u, o);
       if (lane >= o) u += y;
     }
-    warp_tot[lane] = u - t;  // exclusive warp offsets
-    if (lane == 31) blk[blockIdx.x] = u;
+    warp_tot[lane] = u - t;
   }
   __syncthreads();
-  if (i < n) out[i] = x - v + warp_tot[wid];
+  if (threadIdx.x < SCAN_BLOCKS) s.scan_blk[SCAN_BLOCKS + threadIdx.x] = x - v + warp_tot[wid];
 }
 
-__global__ void __launch_bounds__(1024) k_scan_blocks(int nb, int* __restrict__ blk, const int* flag, bool force) {
-  if (skip(flag, force)) return;
+__global__ void __launch_bounds__(SCAN_T) k_wscan_write(DevState s) {
   __shared__ int warp_tot[32];
   __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
+  int lo, hi;
+  scan_share(s, lo, hi);
+  const int n = *s.wl_n;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = s.scan_blk[SCAN_BLOCKS + blockIdx.x];
   __syncthreads();
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int base = 0; base < nb; base += 1024) {
-    int i = base + threadIdx.x;
-    int v = (i < nb) ? blk[i] : 0;
+  for (int base = lo; base < hi; base += SCAN_T) {
+    const int g = base + threadIdx.x;
+    int r = 0, c = 0, k = 0, v = 0;
+    if (g < hi) {
+      k = wl_map_warp(s.wl_c, s.wl_rep, n, g, r, c);
+      v = s.cell_count[s.reps[r].cell_off + c];
+    }
     int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
     if (lane == 31) warp_tot[wid] = x;
     __syncthreads();
     if (wid == 0) {
-      int t = warp_tot[lane];
+      const int t = warp_tot[lane];
       int u = t;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, u, o);
+        const int y = __shfl_up_sync(0xffffffffu, u, o);
         if (lane >= o) u += y;
       }
       warp_tot[lane] = u - t;
     }
     __syncthreads();
-    int excl = x - v + warp_tot[wid] + carry;
+    const int e = carry + warp_tot[wid] + x - v;  // E[g]
+    if (g < hi) s.cell_start[s.reps[r].cell_off + c] = s.reps[r].p0 + e - s.wl_p[k];
     __syncthreads();
-    if (i < nb) blk[i] = excl;
-    if (threadIdx.x == 1023) carry = excl + v;
+    if (threadIdx.x == SCAN_T - 1) carry = e + v;
     __syncthreads();
   }
-}
-
-__global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__ blk, const int* flag, bool force) {
-  if (skip(flag, force)) return;
-  int i = blockIdx.x * 1024 + threadIdx.x;
-  if (i < n) out[i] += blk[blockIdx.x];
 }
 
 __global__ void k_place(DevState s) {
@@ -561,16 +603,12 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   // work (every particle or cell) fills
   const int gN = std::min((s.N + B - 1) / B, s.nsm * 8);
   const int gC = std::min((s.ncell_tot + B - 1) / B, s.nsm * 8);
-  // the scan runs over every cell and one entry past the last, so that cell_start[c + 1] ends
-  // every cell c; the cells of the replicas not rebuilt keep their counts and so their starts
-  const int nc1 = s.ncell_tot + 1;
-  int nb = (nc1 + 1023) / 1024;
   k_worklist<<<1, WL_THREADS, 0, st>>>(s, force);
   k_zero_counts<<<gC, B, 0, st>>>(s);
   k_bin<<<gN, B, 0, st>>>(s);
-  k_scan_local<<<nb, 1024, 0, st>>>(nc1, s.cell_count, s.cell_start, s.scan_blk, s.rebuild_flag, force);
-  k_scan_blocks<<<1, 1024, 0, st>>>(nb, s.scan_blk, s.rebuild_flag, force);
-  k_scan_add<<<nb, 1024, 0, st>>>(nc1, s.cell_start, s.scan_blk, s.rebuild_flag, force);
+  k_wscan_sum<<<SCAN_BLOCKS, SCAN_T, 0, st>>>(s);
+  k_wscan_blocks<<<1, SCAN_T, 0, st>>>(s);
+  k_wscan_write<<<SCAN_BLOCKS, SCAN_T, 0, st>>>(s);
   k_place<<<gN, B, 0, st>>>(s);
   k_sort_cells<<<gC, B, 0, st>>>(s);
   k_permute<<<gN, B, 0, st>>>(s);

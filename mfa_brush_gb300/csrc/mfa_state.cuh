@@ -29,7 +29,8 @@ struct DevState {
   int *nn, *nbr;
   int nbr_cap;
   // cells
-  int *cell_of, *rank, *perm, *cell_count, *cell_start, *scan_blk;
+  int *cell_of, *rank, *perm, *cell_count, *cell_start;
+  int* scan_blk;              // [2 * 256] block sums and offsets of the cell-start scan
   int ncell_tot;
   // control words
   float rl2_uni;  // SimConst::rl2_uni_f (0: per-pair list cut-offs)
