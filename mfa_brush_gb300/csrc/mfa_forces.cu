@@ -72,6 +72,12 @@ __device__ __forceinline__ void bead_delta(const BeadPos<MIXED>& a, const BeadPo
   }
 }
 
+// a * b rounded on its own, never merged into a multiply-add: a force term that the virial of an
+// energy kernel also reads is rounded alike in the kernels with and without energies (whether the
+// compiler merges a product into an add depends on the product's other uses)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 // One angle term of bending.f90:47-109 with r_prev = r_c - r_{c-1}, r_next = r_{c+1} - r_c.
 // fa acts on c-1, fc on c+1 (c gets -fa-fc).  MIXED computes the angle as atan2(|p x n|, p.n),
 // which keeps FP32 accurate for the nearly straight chains that stiff brushes produce.
@@ -141,8 +147,8 @@ __device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, cons
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    fa[j] = fm * dp[j];
-    fc[j] = fm * dn[j];
+    fa[j] = mul_rn(fm, dp[j]);
+    fc[j] = mul_rn(fm, dn[j]);
   }
 }
 
@@ -286,7 +292,8 @@ __device__ __forceinline__ bool bonded_of(const DevState& s, const SimConst& C, 
       const real da = alpha - cst<MIXED>(C.alpha_or, C.alpha_or_f);
       const real fm = cst<MIXED>(C.k_or, C.k_or_f) * da;
       const real sgn = (m == 0) ? (real)-1 : (real)1;
-      F[0] += sgn * fm * dn[0]; F[1] += sgn * fm * dn[1]; F[2] += sgn * fm * dn[2];
+      const real sf = sgn * fm;
+      F[0] += mul_rn(sf, dn[0]); F[1] += mul_rn(sf, dn[1]); F[2] += mul_rn(sf, dn[2]);
       if (EFLAG && m == 0) {
         e4[3] += (real)0.5 * fm * da;
 #pragma unroll
@@ -355,6 +362,91 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
   }
 }
 
+// kept pairs per batch (a thread screens its list until it has this many, then they are evaluated),
+// and list entries screened per group (their loads are all in flight at once)
+constexpr int PAIR_BATCH = 16;
+constexpr int PAIR_G = 4;
+
+// Force factor fs of the pair (i, j) along d = r_i - r_j (LJ with the switch-on clamp, DPD with the
+// pair's Philox noise, real-space Coulomb), fluid_fluid.f90:97-261, dpd_forces.f90:45-115,
+// ewald_real.f90:15-33; with EFLAG the pair's share `half` of its energies.
+template <bool MIXED, bool EFLAG>
+__device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimConst& C,
+                                                 const PairEntry<real_t<MIXED>>& e, real_t<MIXED> dx,
+                                                 real_t<MIXED> dy, real_t<MIXED> dz, int wj, int j,
+                                                 real_t<MIXED> vix, real_t<MIXED> viy, real_t<MIXED> viz, int tag_i,
+                                                 int p0, unsigned long long seed, long long step, real_t<MIXED> r2min,
+                                                 real_t<MIXED> half, real_t<MIXED>& e_lj, real_t<MIXED>& e_c) {
+  using real = real_t<MIXED>;
+  (void)wj;
+  const real sig = cst<MIXED>(C.sig, C.sig_f), gam = cst<MIXED>(C.gamma, C.gamma_f);
+  const real coul_rc2 = cst<MIXED>(C.coul_rc2, C.coul_rc2_f);
+  const real r2raw = dx * dx + dy * dy + dz * dz;
+  const int fl = e.flags;
+  real r2 = r2raw;
+  const bool in_lj = r2raw < e.range2;
+  real fs = 0;  // force factor along d = r_i - r_j
+  if (in_lj) {
+    r2 = r2raw < r2min ? r2min : r2raw;
+    // MIXED: the hardware reciprocal (2 ulp) instead of the IEEE division sequence
+    real inv_r2;
+    if constexpr (MIXED) inv_r2 = __fdividef(1.f, r2); else inv_r2 = (real)1 / r2;
+    const real s2 = e.sig2 * inv_r2;
+    const real s6 = s2 * s2 * s2;
+    const real s12 = s6 * s6;
+    fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
+    if (EFLAG) e_lj += half * e.eps4 * ((s12 - s6) - e.shift);
+  }
+  const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
+  if (dpd) {
+    real vjx, vjy, vjz;
+    int tag_j;
+    if constexpr (MIXED) {
+      float4 v4 = __ldg(&s.vf[j]);
+      vjx = v4.x; vjy = v4.y; vjz = v4.z;
+      tag_j = __float_as_int(v4.w) - p0;
+    } else {
+      dbl4 v4 = s.vd[j];
+      vjx = v4.x; vjy = v4.y; vjz = v4.z;
+      tag_j = (int)__double_as_longlong(v4.w) - p0;
+    }
+    real r, ir;
+    if constexpr (MIXED) {  // one hardware reciprocal square root (2 ulp)
+      ir = rsqrtf(r2);
+      r = r2 * ir;
+    } else {
+      r = sqrt(r2);
+      ir = (real)1 / r;
+    }
+    real wr, wd;
+    if (C.dpd_weight1) {
+      wr = wd = 1;
+    } else {
+      wr = (real)1 - r * ((fl & PF_DPD_OWN) ? e.inv_dpd_rc : e.inv_rc);
+      wd = wr * wr;
+    }
+    real g;
+    if constexpr (MIXED) g = pair_gauss_f(seed, step, tag_i, tag_j);
+    else g = pair_gauss_d(seed, step, tag_i, tag_j);
+    const real rdot = ((vix - vjx) * dx + (viy - vjy) * dy + (viz - vjz) * dz) * ir;
+    fs += (sig * wr * g - gam * wd * rdot) * ir;
+  }
+  if (fl & PF_COUL) {
+    const bool in_c = (coul_rc2 > 0) ? (r2raw < coul_rc2) : in_lj;
+    if (in_c) {
+      const real rc2 = in_lj ? r2 : r2raw;
+      const real r = sqrt(rc2), ir = (real)1 / r;
+      const real qq = e.qq;
+      const real sqa = cst<MIXED>(C.sqrt_alpha, C.sqrt_alpha_f);
+      const real ec = erfc(sqa * r);
+      if (EFLAG) e_c += half * qq * ec * ir;
+      const real isp = cst<MIXED>(C.inv_sqrt_pi, C.inv_sqrt_pi_f), ac = cst<MIXED>(C.alpha_c, C.alpha_c_f);
+      fs += (qq * sqa * isp * (real)2 * exp(-ac * rc2) * ir + qq * ec * ir * ir) * ir;
+    }
+  }
+  return fs;
+}
+
 // The pair kernel.  Template switches:
 //   MIXED   FP32 pair arithmetic on the fixed-point views (else FP64 throughout);
 //   EFLAG   energies and the virial into the accumulators;
@@ -420,7 +512,6 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
     const real r2min = C.force_switch_on ? (real)r2min_of(C, step) : (real)0;
     const int ti = info_type(w);
     const int n = __ldg(&s.nn[i]);
-    const real sig = cst<MIXED>(C.sig, C.sig_f), gam = cst<MIXED>(C.gamma, C.gamma_f);
     const int p0 = R.p0;
     // own position / velocity
     int4 qi;
@@ -443,7 +534,6 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
     const double L0 = R.L[0], L1 = R.L[1], iL0 = R.invL[0], iL1 = R.invL[1];
     const unsigned long long seed = R.seed;
     const int* __restrict__ nb = s.nbr + i;
-    const real coul_rc2 = cst<MIXED>(C.coul_rc2, C.coul_rc2_f);
     auto delta = [&](int j, real& dx, real& dy, real& dz) -> int {
       if constexpr (MIXED) {
         const int4 qj = __ldg(&s.pfx[j]);
@@ -463,8 +553,8 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
     // ones inside any interaction range, (2) evaluate LJ + DPD + Coulomb on the kept pairs only.
     // Without the split a warp runs the Philox/DPD body whenever any lane has an interacting
     // pair, i.e. on almost every list entry.
-    constexpr int BATCH = 16;
-    constexpr int G = 4;  // list entries screened per group: their loads are all in flight at once
+    constexpr int BATCH = PAIR_BATCH;
+    constexpr int G = PAIR_G;  // list entries screened per group: their loads are all in flight at once
     int jl[BATCH];
     int k = 0;
     // screening against the largest cut-off of the type pair; MIXED uses the coarse conversion
@@ -517,75 +607,20 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
         const int j = jl[t];
         real dx, dy, dz;
         const int wj = delta(j, dx, dy, dz);
-        const real r2raw = dx * dx + dy * dy + dz * dz;
         const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
-        const int fl = e.flags;
-        real r2 = r2raw;
-        const bool in_lj = r2raw < e.range2;
-        real fs = 0;  // force factor along d = r_i - r_j
         // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
         const real half = info_mobile(wj) ? (real)0.5 : (real)1;
-        if (in_lj) {
-          r2 = r2raw < r2min ? r2min : r2raw;
-          // MIXED: the hardware reciprocal (2 ulp) instead of the IEEE division sequence
-          real inv_r2;
-          if constexpr (MIXED) inv_r2 = __fdividef(1.f, r2); else inv_r2 = (real)1 / r2;
-          const real s2 = e.sig2 * inv_r2;
-          const real s6 = s2 * s2 * s2;
-          const real s12 = s6 * s6;
-          fs = e.eps4 * ((real)12 * s12 - (real)6 * s6) * inv_r2;
-          if (EFLAG) e_lj += half * e.eps4 * ((s12 - s6) - e.shift);
+        const real fs = pair_fs<MIXED, EFLAG>(s, C, e, dx, dy, dz, wj, j, vix, viy, viz, tag_i, p0, seed, step,
+                                              r2min, half, e_lj, e_c);
+        if constexpr (MIXED) {  // unmerged products and sums: alike with and without energies
+          fx = __fadd_rn(fx, __fmul_rn(fs, dx));
+          fy = __fadd_rn(fy, __fmul_rn(fs, dy));
+          fz = __fadd_rn(fz, __fmul_rn(fs, dz));
+        } else {
+          fx += fs * dx;
+          fy += fs * dy;
+          fz += fs * dz;
         }
-        const bool dpd = (in_lj && (fl & PF_DPD_LJ)) || ((fl & PF_DPD_OWN) && r2 < e.dpd_rc2);
-        if (dpd) {
-          real vjx, vjy, vjz;
-          int tag_j;
-          if constexpr (MIXED) {
-            float4 v4 = __ldg(&s.vf[j]);
-            vjx = v4.x; vjy = v4.y; vjz = v4.z;
-            tag_j = __float_as_int(v4.w) - p0;
-          } else {
-            dbl4 v4 = s.vd[j];
-            vjx = v4.x; vjy = v4.y; vjz = v4.z;
-            tag_j = (int)__double_as_longlong(v4.w) - p0;
-          }
-          real r, ir;
-          if constexpr (MIXED) {  // one hardware reciprocal square root (2 ulp)
-            ir = rsqrtf(r2);
-            r = r2 * ir;
-          } else {
-            r = sqrt(r2);
-            ir = (real)1 / r;
-          }
-          real wr, wd;
-          if (C.dpd_weight1) {
-            wr = wd = 1;
-          } else {
-            wr = (real)1 - r * ((fl & PF_DPD_OWN) ? e.inv_dpd_rc : e.inv_rc);
-            wd = wr * wr;
-          }
-          real g;
-          if constexpr (MIXED) g = pair_gauss_f(seed, step, tag_i, tag_j);
-          else g = pair_gauss_d(seed, step, tag_i, tag_j);
-          const real rdot = ((vix - vjx) * dx + (viy - vjy) * dy + (viz - vjz) * dz) * ir;
-          fs += (sig * wr * g - gam * wd * rdot) * ir;
-        }
-        if (fl & PF_COUL) {
-          const bool in_c = (coul_rc2 > 0) ? (r2raw < coul_rc2) : in_lj;
-          if (in_c) {
-            const real rc2 = in_lj ? r2 : r2raw;
-            const real r = sqrt(rc2), ir = (real)1 / r;
-            const real qq = e.qq;
-            const real sqa = cst<MIXED>(C.sqrt_alpha, C.sqrt_alpha_f);
-            const real ec = erfc(sqa * r);
-            if (EFLAG) e_c += half * qq * ec * ir;
-            const real isp = cst<MIXED>(C.inv_sqrt_pi, C.inv_sqrt_pi_f), ac = cst<MIXED>(C.alpha_c, C.alpha_c_f);
-            fs += (qq * sqa * isp * (real)2 * exp(-ac * rc2) * ir + qq * ec * ir * ir) * ir;
-          }
-        }
-        fx += fs * dx;
-        fy += fs * dy;
-        fz += fs * dz;
         if (EFLAG) sym_add(wv, half * fs, dx, dy, dz);
       }
       if constexpr (FUSED) {  // the batch's FP32 partial into the FP64 total

@@ -183,57 +183,83 @@ def test_charged_nve_energy_excursion_within_3x_fp64_oracle(gpu, oracle_mod):
 
 
 def test_dpd_statistics_match_oracle(gpu, oracle_mod):
-    """With the DPD noise on, the fused mixed step and the FP64 oracle sample the same process
-    (same Philox stream, same start; the trajectories part after a few hundred steps).  Over 4000
-    steps after 1500 of equilibration (WCA channel, DPD with its own 1.5 sigma cut-off, kT = 1),
-    sampled every 100 steps: kinetic temperature, velocity kurtosis (3 for a Maxwell
-    distribution), brush height (mean distance of the brush beads from their own wall) and the
-    solvent z-profile agree within their statistical errors."""
+    """With the DPD noise on, the fused mixed step samples the same process as FP64.  WCA channel
+    10 x 10 x 10 sigma with 12-bead chains, DPD with its own 1.5 sigma cut-off, kT = 1: 1500 steps
+    of equilibration, then 60 samples 100 steps apart of the kinetic temperature, the velocity
+    kurtosis (3 for a Maxwell distribution), the brush height (mean distance of the brush beads
+    from their own wall) and the solvent z-profile.
+    (1) Eight independent replicas (own starts, own Philox keys) run batched on the mixed path and
+    on the FP64 path; their per-replica means agree within 5 standard errors over the replicas
+    (the brush height relaxes over thousands of steps, so the samples of one trajectory are far
+    from independent; the replicas are).
+    (2) The oracle runs the first replica (the same start and Philox stream; the trajectories part
+    after a few hundred steps): its temperature and kurtosis are the Maxwell values, and its brush
+    height and profile lie within the spread of the GPU replicas."""
     inp = configs.wca_inputs(gamma=5.0, kT=1.0, dt=0.005)
     inp.flags.dpd_cut_off = 1.5  # DPD_CUT_OFF
     p, _ = md.derive(inp)
-    s, a_type, r0, v = configs.brush_channel(10.0, 10.0, 0.15, 12, rho=0.7, seed=13)
-    g = md.MdSystem(p, s, a_type, r0, v, precision="mixed")
-    o = oracle_mod.Oracle(p, s, a_type, r0, v)
-    threads = max(1, os.cpu_count() or 1)
-    nb, D = s.n_mon * s.n_chain, s.boundary[2]
-    mob = a_type != 1
-    bottom = np.zeros(s.n_part, bool)
-    bottom[: (s.n_chain // 2) * s.n_mon] = True  # the first half of the chains hang from z = 0
-    brush = a_type == 2
+    reps = [configs.brush_channel(10.0, 10.0, 0.15, 12, rho=0.7, seed=13 + k) for k in range(8)]
+    systems, a_type, r0, v = configs.concat(reps)
 
-    def sample(r, vv):
-        vm = vv[mob]
+    def sample(s, at, r, vv):
+        nb, D = s.n_mon * s.n_chain, s.boundary[2]
+        vm = vv[at != 1]
         t = np.mean(vm ** 2)
         k4 = np.mean(vm ** 4) / t ** 2
+        bottom = np.zeros(s.n_part, bool)
+        bottom[: (s.n_chain // 2) * s.n_mon] = True  # the first half of the chains hang from z = 0
+        brush = at == 2
         h = np.mean(np.where(bottom[brush], r[brush, 2], D - r[brush, 2]))
         prof = np.histogram(r[nb:, 2], bins=10, range=(0.0, D))[0].astype(float)
-        return t, k4, h, prof
+        return np.concatenate([[t, k4, h], prof / prof.sum()])
 
-    g.step(1500)
+    def replica_means(precision):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision=precision)
+        g.step(1500)
+        acc = []
+        for _ in range(60):
+            g.step(100)
+            r, vv = g.state()[:2]
+            row, off = [], 0
+            for s, at, _, _ in reps:
+                sl = slice(off, off + s.n_part)
+                row.append(sample(s, at, r[sl], vv[sl]))
+                off += s.n_part
+            acc.append(row)
+        g.close()
+        return np.mean(np.array(acc), axis=0)  # (replica, observable)
+
+    mix, f64 = replica_means("mixed"), replica_means("fp64")
+    se = np.hypot(mix.std(axis=0, ddof=1), f64.std(axis=0, ddof=1)) / np.sqrt(len(reps))
+    dm = np.abs(mix.mean(axis=0) - f64.mean(axis=0))
+    prof_l1 = np.abs(mix[:, 3:].mean(axis=0) - f64[:, 3:].mean(axis=0)).sum()
+    print("DPD statistics over %d replicas, mixed / FP64: <v^2> %.4f / %.4f  kurtosis %.3f / %.3f  "
+          "brush height %.3f / %.3f (standard error %.3f)  profile L1 %.4f"
+          % (len(reps), mix[:, 0].mean(), f64[:, 0].mean(), mix[:, 1].mean(), f64[:, 1].mean(),
+             mix[:, 2].mean(), f64[:, 2].mean(), se[2], prof_l1))
+    assert np.all(np.abs(mix[:, 0] - 1.0) < 0.05) and np.all(np.abs(f64[:, 0] - 1.0) < 0.05)
+    for c in range(len(dm)):  # temperature, kurtosis, brush height, the ten profile bins
+        assert dm[c] < 5 * se[c] + 1e-3, (c, dm[c], se[c])
+    assert prof_l1 < 0.04
+
+    s, at, r, vv = reps[0]
+    o = oracle_mod.Oracle(p, s, at, r, vv)
+    threads = max(1, os.cpu_count() or 1)
     o.step(1500, threads, 0)
-    sg, so = [], []
+    so = []
     for _ in range(60):
-        g.step(100)
         o.step(100, threads, 0)
-        sg.append(sample(*g.state()[:2]))
-        so.append(sample(*o.state()[:2]))
-
-    def stat(samples, k):
-        x = np.array([q[k] for q in samples])
-        return x.mean(axis=0), x.std(axis=0) / np.sqrt(len(x) / 4.0)  # blocks of 4 samples as independent
-
-    (tg, etg), (to, eto) = stat(sg, 0), stat(so, 0)
-    (kg, _), (ko, _) = stat(sg, 1), stat(so, 1)
-    (hg, ehg), (ho, eho) = stat(sg, 2), stat(so, 2)
-    (pg, _), (po, _) = stat(sg, 3), stat(so, 3)
-    print("DPD statistics, mixed vs FP64 oracle: <v^2> %.4f / %.4f  kurtosis %.3f / %.3f  brush height "
-          "%.3f / %.3f  profile L1 %.3f" % (tg, to, kg, ko, hg, ho, np.abs(pg - po).sum() / po.sum()))
-    assert abs(tg - 1.0) < 0.05 and abs(to - 1.0) < 0.05
-    assert abs(tg - to) < 4 * np.hypot(etg, eto) + 0.01
-    assert abs(kg - 3.0) < 0.1 and abs(ko - 3.0) < 0.1
-    assert abs(hg - ho) < max(4 * np.hypot(ehg, eho), 0.03 * ho)
-    assert np.abs(pg - po).sum() / po.sum() < 0.06
+        so.append(sample(s, at, *o.state()[:2]))
+    o.close()
+    so = np.mean(np.array(so), axis=0)
+    pool = np.concatenate([mix, f64])
+    spread = pool.std(axis=0, ddof=1)
+    print("oracle, replica 0: <v^2> %.4f  kurtosis %.3f  brush height %.3f (GPU replicas %.3f +- %.3f)  "
+          "profile L1 to the GPU mean %.4f" % (so[0], so[1], so[2], pool[:, 2].mean(), spread[2],
+                                               np.abs(so[3:] - pool[:, 3:].mean(axis=0)).sum()))
+    assert abs(so[0] - 1.0) < 0.05 and abs(so[1] - 3.0) < 0.1
+    assert abs(so[2] - pool[:, 2].mean()) < 4 * spread[2] + 1e-3
+    assert np.abs(so[3:] - pool[:, 3:].mean(axis=0)).sum() < 0.08
 
 
 def test_charged_brush_full_size_stays_in_channel(gpu):

@@ -379,6 +379,32 @@ def test_pair_block_size_does_not_change_the_trajectory(gpu, block):
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("setup", ["brush", "melt", "two_liquid"])
+def test_energy_cadence_does_not_change_the_trajectory(gpu, setup):
+    """Steps that record energies run the pair kernel's energy variant, which also forms energies
+    and virial tensors from the force terms; the force terms it shares with them are rounded
+    unmerged (no multiply-add whose use depends on the variant), so 30 fused steps with energies
+    every step, every 10th step and every 7th step give the same state bit for bit (brush
+    replicas; melt in brush with cosine bending; two liquids with the body force)."""
+    if setup == "brush":
+        p = configs.wca_params(gamma=5.0)
+        systems, a_type, r0, v = configs.concat(configs.replicas(4, seed=9))
+    elif setup == "melt":
+        p, (systems, a_type, r0, v) = configs.melt_brush(L=14.0, D=24.0)
+    else:
+        p, _ = md.derive(configs.two_liquid_inputs(f_x=0.01))
+        systems, a_type, r0, v = configs.two_liquid_channel(L=14.0, D=12.0, seed=5)
+    out = []
+    for every in (1, 10, 7):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", energy_every=every)
+        g.step(30)
+        out.append(g.state())
+        g.close()
+    for o in out[1:]:
+        for x, y in zip(out[0], o):
+            assert np.array_equal(x, y)
+
+
 def test_measurement_aids(gpu):
     """mfa_fp32_fma_peak measures a plausible FP32 FMA throughput (a GB300 has 152 SMs x 128 lanes
     x 2 FLOP x ~2 GHz = ~80 TFLOP/s nominal); mfa_kspace_info gives the k-set and charge counts of
