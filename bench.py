@@ -340,6 +340,8 @@ def main():
     ap.add_argument("--kernel-steps", type=int, default=20)
     ap.add_argument("--block", type=int, default=128,
                     help="threads per block of the pair kernel (32, 64, 128); tuned with --skin auto")
+    ap.add_argument("--list-cells", type=int, default=0,
+                    help="list-build cells per list cut-off (1, 2, 3; 0 = the library's choice)")
     ap.add_argument("--skin", default="auto",
                     help="list skin in sigma, or 'auto': the whole set timed at 0.5-0.9")
     args = ap.parse_args()
@@ -384,9 +386,10 @@ def main():
         # each candidate warmed up like the timed run (the first steps after the lattice start
         # are hotter and rebuild more often)
         best, rates = tune.tune_skin(p, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8), n_sample=len(reps),
-                                     steps=100, warmup=args.warmup, precision=args.precision, device=local)
+                                     steps=100, warmup=args.warmup, precision=args.precision, device=local,
+                                     list_cells=args.list_cells)
         blk, brates = tune.tune_block(p, reps, best, n_sample=len(reps), steps=100, warmup=args.warmup,
-                                      precision=args.precision, device=local)
+                                      precision=args.precision, device=local, list_cells=args.list_cells)
         tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
                  "block_candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in brates.items()},
                  "block_size": blk,
@@ -396,7 +399,7 @@ def main():
         args.block = blk
     args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin,
-                    block_size=args.block)
+                    block_size=args.block, list_cells=args.list_cells)
 
     def barrier():
         if dist is not None:
@@ -458,7 +461,7 @@ def main():
                        "replicas": args.replicas * world, "particles_per_gpu": n_atoms,
                        "particles_total": n_all, "seed": args.seed,
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
-                       "pair_block": args.block,
+                       "pair_block": args.block, "list_cells": g.list_cells(),
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
@@ -489,7 +492,8 @@ def main():
             "sample": "every 16th replica of the set, each alone in its own FP64 context, 10-step graphs",
             "speedup_of_value": value / world / fv}
         # the same batch in the plain FP64 mode (precision alone, batching held fixed)
-        gd = md.MdSystem(p, systems, a_type, r0, v, precision="fp64", device=local, skin=args.skin)
+        gd = md.MdSystem(p, systems, a_type, r0, v, precision="fp64", device=local, skin=args.skin,
+                         list_cells=args.list_cells)
         for _ in range(2):
             gd.step(CHUNK)
         gd.synchronize()

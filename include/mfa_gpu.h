@@ -185,6 +185,12 @@ typedef struct mfa_options {
                                (mfa_get_averages); default 0                                    */
   int32_t series_capacity;  /* energy records kept on the device for mfa_get_energy_series (a
                                ring; 0 = none, the default)                                     */
+  int32_t list_cells;       /* list-build cells per list cut-off (r_cut_max + skin) along each
+                               axis: 1, 2 or 3; 0 (the default) = the smallest value for which
+                               every box holds 2*list_cells+1 cells in x and y.  The list search
+                               walks the (2*list_cells+1)^3 cells around a particle as x-rows and
+                               skips the rows and row ends beyond the cut-off.  The lists hold the
+                               same pairs whatever the value; their order differs.               */
 } mfa_options;
 
 typedef struct mfa_energies {
@@ -335,6 +341,9 @@ int mfa_step(mfa_ctx* ctx, int32_t nsteps);
    mfa_verlet_positions raises the capacity by half (up to its maximum) and rebuilds the lists;
    the overflow status of the old capacity is cleared by that rebuild.                         */
 int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count);
+/* The options the context runs with: those given to mfa_init / mfa_batch_init, with list_cells
+   resolved to the value in use.                                                               */
+int mfa_get_options(mfa_ctx* ctx, mfa_options* out);
 /* Size of the reciprocal-space sum: k-vectors of the reference's k-set (ewald_k.f90:47-124) and
    charged particles; both 0 for an uncharged context.                                         */
 int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged);

@@ -88,7 +88,7 @@ class Options(C.Structure):
     _fields_ = [("precision", i32), ("device", i32), ("skin", f64), ("nbr_capacity", i32),
                 ("energy_every", i32), ("use_graphs", i32), ("block_size", i32),
                 ("profile_from_step", i32), ("kspace_plain_sums", i32), ("observe", i32),
-                ("series_capacity", i32)]
+                ("series_capacity", i32), ("list_cells", i32)]
 
 
 class Energies(C.Structure):
@@ -193,6 +193,7 @@ SIGNATURES = {
     "mfa_reset_averages": (i32, [vp]),
     "mfa_get_energy_series": (i32, [vp, P(Energies), i32, ip]),
     "mfa_list_stats": (i32, [vp, ip, ip]),
+    "mfa_get_options": (i32, [vp, P(Options)]),
     "mfa_kspace_info": (i32, [vp, ip, ip]),
     "mfa_reset_profiles": (i32, [vp]),
     "mfa_cell_list": (i32, [vp, i32, i32, ip, ip, i32, ip]),

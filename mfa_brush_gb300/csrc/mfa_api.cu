@@ -578,6 +578,16 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   ctx->v_ff_walls.assign(n_rep, 0.);
   int cell_off = 0, p0 = 0;
   double dens_max = 0.;
+  // list-build cells per list cut-off: as asked, else the fewest (the largest cells: fewest rows
+  // to walk) that every replica's box holds 2h+1 of in x and y
+  int nl_h = ctx->opt.list_cells;
+  if (nl_h < 0 || nl_h > 3) return fail(ctx, MFA_ERR_ARG, "list_cells must be 0, 1, 2 or 3");
+  if (nl_h == 0) {
+    nl_h = 1;
+    for (int r = 0; r < n_rep; ++r)
+      for (int d = 0; d < 2; ++d)
+        while (nl_h < 3 && std::floor(ctx->sys[r].boundary[d] / (rl_max / nl_h)) < 2 * nl_h + 1) ++nl_h;
+  }
   for (int r = 0; r < n_rep; ++r) {
     const mfa_system& s = ctx->sys[r];
     RepDesc& R = ctx->hreps[r];
@@ -589,11 +599,13 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       R.sfx[d] = (d < 2) ? 4294967296.0 / s.boundary[d] : 1073741824.0 / s.boundary[d];
       R.ufx[d] = 1. / R.sfx[d];
       R.ufx_f[d] = (float)R.ufx[d];
-      // list cells of at least half the list cut-off: the 5x5x5 stencil covers every neighbour
-      int nc = (int)std::floor(s.boundary[d] / (0.5 * rl_max));
+      // list cells of at least 1/h of the list cut-off: the (2h+1)^3 stencil covers every
+      // neighbour, and 2h+1 cells in x and y keep each cell of a stencil row distinct
+      int nc = (int)std::floor(s.boundary[d] / (rl_max / nl_h));
       if (nc < 1) nc = 1;
-      if (d < 2 && nc < 5)
-        return fail(ctx, MFA_ERR_UNSUPPORTED, "box shorter than 2.5*(r_cut_max+skin) in x or y");
+      if (d < 2 && nc < 2 * nl_h + 1)
+        return fail(ctx, MFA_ERR_UNSUPPORTED,
+                    "box shorter than (2 + 1/list_cells)*(r_cut_max+skin) in x or y");
       R.nc[d] = nc;
       R.inv_lc[d] = (double)nc / s.boundary[d];
       R.lc_f[d] = (float)(s.boundary[d] / nc);
@@ -727,6 +739,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   S.tabf = ctx->dtabf;
   S.tabd = ctx->dtabd;
   S.rl2_uni = S.mixed ? C.rl2_uni_f : 0.f;
+  S.nl_h = nl_h;
   // neighbour capacity: 2x the mean count of the densest replica + 32, at least 48
   int cap = ctx->opt.nbr_capacity;
   if (cap <= 0) {
@@ -1150,6 +1163,13 @@ int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count) {
   if (capacity) *capacity = ctx->S.nbr_cap;
   if (max_count) *max_count = (int32_t)ctx->h_status[1];
   return r;
+}
+
+int mfa_get_options(mfa_ctx* ctx, mfa_options* out) {
+  if (!ctx || !out) return MFA_ERR_ARG;
+  *out = ctx->opt;
+  out->list_cells = ctx->S.nl_h;
+  return MFA_OK;
 }
 
 int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged) {

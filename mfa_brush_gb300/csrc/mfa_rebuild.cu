@@ -408,9 +408,10 @@ __global__ void k_copyback(DevState s) {
 }
 
 // Full Verlet list: every mobile particle lists all j (mobile or wall) with r^2 < (rc_ij+skin)^2.
-// One thread per particle.  Cells are at least half the list cut-off wide, and the 5x5x5 cells
-// around a particle are walked as 25 x-rows: the cells of a row are consecutive in the sorted
-// order unless the row wraps in x, so a row is one contiguous slot range (two when it wraps).
+// One thread per particle.  Cells are at least 1/H of the list cut-off wide (H = 2 by default),
+// and the (2H+1)^3 cells around a particle are walked as (2H+1)^2 x-rows: the cells of a row are
+// consecutive in the sorted order unless the row wraps in x, so a row is one contiguous slot range
+// (two when it wraps).
 // Rows whose y/z distance from the particle exceeds the largest list cut-off of its type are
 // skipped, and each kept row is trimmed in x to the cells within that cut-off, which removes
 // about half of the candidates.  Each thread stages its first NL_STAGE entries in shared memory
@@ -424,7 +425,7 @@ __global__ void k_copyback(DevState s) {
 // coalesced; a particle with more neighbours writes the rest straight to the list)
 constexpr int NL_STAGE = 32;
 
-template <bool MIXED, bool UNI>
+template <bool MIXED, bool UNI, int H>
 __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s) {
   const int nwl = *s.wl_n;
   const int nchunks = s.wl_k[nwl];
@@ -503,17 +504,26 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s) {
       d = fmaxf(d, 0.f) * l;
       return d * d;
     };
-    const float gxp1 = gap2(fl(ix + 1) - px, lx), gxp2 = gap2(fl(ix + 2) - px, lx);
-    const float gxm1 = gap2(px - fl(ix), lx), gxm2 = gap2(px - fl(ix - 1), lx);
-    for (int dz = -2; dz <= 2; ++dz) {
+    float gxp[H], gxm[H];  // squared gaps to the cells ix + k and ix - k, k = 1..H
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+      gxp[k - 1] = gap2(fl(ix + k) - px, lx);
+      gxm[k - 1] = gap2(px - fl(ix - k + 1), lx);
+    }
+    for (int dz = -H; dz <= H; ++dz) {
       const int cz = iz + dz;
       if (cz < 0 || cz >= R.nc[2]) continue;
       const float rz2 = rl2max - ((dz > 0) ? gap2(fl(cz) - pz, lz) : (dz < 0 ? gap2(pz - fl(cz + 1), lz) : 0.f));
-      for (int dy = -2; dy <= 2; ++dy) {
+      for (int dy = -H; dy <= H; ++dy) {
         int cy = iy + dy;
         const float rem2 = rz2 - ((dy > 0) ? gap2(fl(cy) - py, ly) : (dy < 0 ? gap2(py - fl(cy + 1), ly) : 0.f));
         if (rem2 <= 0.f) continue;  // the whole row is beyond the list cut-off
-        const int xa = ix - (gxm1 < rem2) - (gxm2 < rem2), xb = ix + (gxp1 < rem2) + (gxp2 < rem2);
+        int xa = ix, xb = ix;
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+          xa -= gxm[k] < rem2;
+          xb += gxp[k] < rem2;
+        }
         cy += (cy < 0) ? R.nc[1] : 0;
         cy -= (cy >= R.nc[1]) ? R.nc[1] : 0;
         const int row = R.cell_off + (cz * R.nc[1] + cy) * nx;
@@ -614,7 +624,11 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   k_permute<<<gN, B, 0, st>>>(s);
   k_copyback<<<gN, B, 0, st>>>(s);
   const int var = s.mixed ? (s.rl2_uni > 0.f ? 2 : 1) : 0;
-  auto kern = var == 2 ? k_nlist<true, true> : var == 1 ? k_nlist<true, false> : k_nlist<false, false>;
+  using KernT = void (*)(DevState);
+  const KernT kerns[3][3] = {{k_nlist<false, false, 1>, k_nlist<true, false, 1>, k_nlist<true, true, 1>},
+                             {k_nlist<false, false, 2>, k_nlist<true, false, 2>, k_nlist<true, true, 2>},
+                             {k_nlist<false, false, 3>, k_nlist<true, false, 3>, k_nlist<true, true, 3>}};
+  const KernT kern = kerns[s.nl_h - 1][var];
   const int gl = std::min((s.N + NL_BLOCK - 1) / NL_BLOCK, s.nsm * 8);
   kern<<<gl, NL_BLOCK, 0, st>>>(s);
   k_clear_flags<<<1, 256, 0, st>>>(s.rebuild_flag, s.nrep, s.rebuilds, s.rep_rebuilds);

@@ -68,7 +68,8 @@ def read_deck(deck_dir, conf="conf_old"):
 
 
 def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, device=0, nbr_capacity=0,
-            profile_from_step=0, block_size=0, kspace_plain_sums=False, observe=False, series_capacity=0):
+            profile_from_step=0, block_size=0, kspace_plain_sums=False, observe=False, series_capacity=0,
+            list_cells=0):
     o = abi.Options()
     _lib().mfa_default_options(C.byref(o))
     o.precision = abi.PREC_MIXED if precision in ("mixed", abi.PREC_MIXED) else abi.PREC_FP64
@@ -82,6 +83,7 @@ def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, devic
     o.kspace_plain_sums = 1 if kspace_plain_sums else 0
     o.observe = 1 if observe else 0
     o.series_capacity = series_capacity
+    o.list_cells = list_cells
     return o
 
 
@@ -241,6 +243,16 @@ class MdSystem:
         e = (abi.Energies * self.nrep)()
         self._ck(self.lib.mfa_get_energies(self.ctx, e))
         return [x.as_dict() for x in e]
+
+    def options_in_use(self):
+        """The context's options (abi.Options), list_cells resolved to the value in use."""
+        o = abi.Options()
+        self._ck(self.lib.mfa_get_options(self.ctx, C.byref(o)))
+        return o
+
+    def list_cells(self):
+        """List-build cells per list cut-off in use (1, 2 or 3)."""
+        return self.options_in_use().list_cells
 
     def list_stats(self):
         """(neighbour-list capacity, largest list count seen at the rebuilds so far)."""

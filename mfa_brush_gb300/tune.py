@@ -22,15 +22,16 @@ def sample_replicas(reps, n_sample):
 
 
 def tune_skin(params, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9), n_sample=32, steps=80, warmup=20,
-              precision="mixed", device=0, chunk=10):
+              precision="mixed", device=0, chunk=10, **opt):
     """Times mfa_step on a sample of `reps` (list of (System, a_type, r0, v)) at each candidate
-    skin; returns (best skin, {skin: atom-steps/s})."""
+    skin (further keyword arguments are options of every context); returns (best skin,
+    {skin: atom-steps/s})."""
     sample = sample_replicas(reps, n_sample)
     systems, a_type, r0, v = configs.concat(sample)
     n_atoms = int(sum(s.n_part for s in systems))
     rates = {}
     for skin in candidates:
-        g = md.MdSystem(params, systems, a_type, r0, v, precision=precision, device=device, skin=skin)
+        g = md.MdSystem(params, systems, a_type, r0, v, precision=precision, device=device, skin=skin, **opt)
         for _ in range(max(1, warmup // chunk)):
             g.step(chunk)
         g.synchronize()
@@ -46,7 +47,7 @@ def tune_skin(params, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9), n_sa
 
 
 def tune_block(params, reps, skin, candidates=(64, 128), n_sample=32, steps=80, warmup=20,
-               precision="mixed", device=0, chunk=10):
+               precision="mixed", device=0, chunk=10, **opt):
     """Times mfa_step at the given skin with each candidate pair-kernel block size (threads per
     block); returns (best block size, {block: atom-steps/s})."""
     sample = sample_replicas(reps, n_sample)
@@ -55,7 +56,7 @@ def tune_block(params, reps, skin, candidates=(64, 128), n_sample=32, steps=80, 
     rates = {}
     for b in candidates:
         g = md.MdSystem(params, systems, a_type, r0, v, precision=precision, device=device, skin=skin,
-                        block_size=b)
+                        block_size=b, **opt)
         for _ in range(max(1, warmup // chunk)):
             g.step(chunk)
         g.synchronize()

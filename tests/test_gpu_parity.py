@@ -462,3 +462,46 @@ def test_state_round_trip_pinned_and_pageable(gpu):
     assert g.rebuild_count() == rb + 1
     r_back = g.state()[0]
     assert np.abs(r_back - moved).max() < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("setup", ["brush", "melt"])
+def test_list_cells_give_the_same_lists(gpu, precision, setup):
+    """List-build cells of the whole, a half and a third of the list cut-off (list_cells 1, 2, 3)
+    walk 3^3, 5^3 and 7^3 cells; the lists hold the same pairs in another order.  Per replica the
+    same interacting pairs and the same largest list count; pair forces equal up to the order of
+    the sums (FP64 1e-12, mixed 1e-5 of F_rms); 20 steps of the fused step stay within 1e-6 sigma
+    (brush replicas with one cut-off; melt in brush with per-type cut-offs)."""
+    if setup == "brush":
+        p = configs.wca_params(gamma=5.0)
+        systems, a_type, r0, v = configs.concat(configs.replicas(4, seed=9))
+        systems = list(systems)
+    else:
+        p, (s, a_type, r0, v) = configs.melt_brush(L=14.0, D=24.0)
+        systems = [s]
+    out = {}
+    for h in (1, 2, 3):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision=precision, list_cells=h)
+        assert g.list_cells() == h
+        pairs = [set(map(tuple, np.sort(g.pair_list(k), axis=1).tolist())) for k in range(len(systems))]
+        g.zero_force()
+        g.fluid_fluid()
+        f = g.state()[3]
+        mx = g.list_stats()[1]
+        g.step(20)
+        out[h] = (pairs, f, mx, g.state()[0])
+        g.close()
+    g = md.MdSystem(p, systems, a_type, r0, v, precision=precision)
+    assert g.list_cells() == 1  # these boxes hold three cells of the list cut-off in x and y
+    g.close()
+    pairs2, f2, mx2, r2 = out[2]
+    frms = np.sqrt(np.mean(np.sum(f2 ** 2, axis=1)))
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for h in (1, 3):
+        pairs, f, mx, r = out[h]
+        assert pairs == pairs2 and mx == mx2
+        assert np.abs(f - f2).max() <= tol * frms, (h, np.abs(f - f2).max() / frms)
+        d = r - r2
+        L = np.concatenate([np.tile(np.array(list(s.boundary))[:2], (s.n_part, 1)) for s in systems])
+        d[:, :2] -= L * np.round(d[:, :2] / L)
+        assert np.abs(d).max() < 1e-6, (h, np.abs(d).max())
