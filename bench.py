@@ -342,8 +342,10 @@ def main():
                     help="threads per block of the pair kernel (32, 64, 128); tuned with --skin auto")
     ap.add_argument("--list-cells", type=int, default=0,
                     help="list-build cells per list cut-off (1, 2, 3; 0 = the library's choice)")
+    ap.add_argument("--pair-schedule", type=int, default=0,
+                    help="pair kernel schedule: 0 one block per tile, 1 persistent blocks over a tile queue")
     ap.add_argument("--skin", default="auto",
-                    help="list skin in sigma, or 'auto': the whole set timed at 0.5-0.9")
+                    help="list skin in sigma, or 'auto': the whole set timed at 0.3-0.8, then the list cell size, the pair block size and schedule at the chosen skin")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
@@ -388,18 +390,24 @@ def main():
         best, rates = tune.tune_skin(p, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8), n_sample=len(reps),
                                      steps=100, warmup=args.warmup, precision=args.precision, device=local,
                                      list_cells=args.list_cells)
-        blk, brates = tune.tune_block(p, reps, best, n_sample=len(reps), steps=100, warmup=args.warmup,
-                                      precision=args.precision, device=local, list_cells=args.list_cells)
+        kw = dict(n_sample=len(reps), steps=100, warmup=args.warmup, precision=args.precision, device=local)
+        lc, lrates = tune.tune_option(p, reps, best, "list_cells", (1, 2, 3), **kw)
+        blk, brates = tune.tune_block(p, reps, best, list_cells=lc, **kw)
+        sch, srates = tune.tune_option(p, reps, best, "pair_schedule", (0, 1), list_cells=lc, block_size=blk, **kw)
         tuned = {"candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in rates.items()},
+                 "list_cells_candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in lrates.items()},
                  "block_candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in brates.items()},
-                 "block_size": blk,
+                 "pair_schedule_candidates": {str(k): round(v_ / 1e9, 4) for k, v_ in srates.items()},
+                 "block_size": blk, "list_cells": lc, "pair_schedule": sch,
                  "unit": "G atom-steps/s on the %d replicas of this GPU, 100 steps each after %d "
                          "warm-up steps" % (len(reps), args.warmup)}
         args.skin = best
         args.block = blk
+        args.list_cells = lc
+        args.pair_schedule = sch
     args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin,
-                    block_size=args.block, list_cells=args.list_cells)
+                    block_size=args.block, list_cells=args.list_cells, pair_schedule=args.pair_schedule)
 
     def barrier():
         if dist is not None:
@@ -461,7 +469,7 @@ def main():
                        "replicas": args.replicas * world, "particles_per_gpu": n_atoms,
                        "particles_total": n_all, "seed": args.seed,
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
-                       "pair_block": args.block, "list_cells": g.list_cells(),
+                       "pair_block": args.block, "list_cells": g.list_cells(), "pair_schedule": args.pair_schedule,
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},

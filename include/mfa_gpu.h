@@ -191,6 +191,10 @@ typedef struct mfa_options {
                                walks the (2*list_cells+1)^3 cells around a particle as x-rows and
                                skips the rows and row ends beyond the cut-off.  The lists hold the
                                same pairs whatever the value; their order differs.               */
+  int32_t pair_schedule;    /* 0 (default): the pair kernel runs one block per 128 particles;
+                               1: as many blocks as fit on the GPU at once, each taking blocks of
+                               particles from a queue (an atomic ticket, no waiting) until none
+                               is left.  The forces are the same bit for bit.                    */
 } mfa_options;
 
 typedef struct mfa_energies {

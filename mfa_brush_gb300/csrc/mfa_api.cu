@@ -706,6 +706,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.cell_start, cell_off + 1);
   DA(S.scan_blk, 2 * 256);  // the cell-start scan's block sums and offsets
   DA(S.rebuild_flag, 1 + n_rep);
+  DA(S.pair_q, 2);
   DA(S.wl_rep, n_rep + 1);
   DA(S.wl_p, n_rep + 1);
   DA(S.wl_c, n_rep + 1);
@@ -740,6 +741,9 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   S.tabd = ctx->dtabd;
   S.rl2_uni = S.mixed ? C.rl2_uni_f : 0.f;
   S.nl_h = nl_h;
+  if (ctx->opt.pair_schedule < 0 || ctx->opt.pair_schedule > 1)
+    return fail(ctx, MFA_ERR_ARG, "pair_schedule must be 0 or 1");
+  S.pair_persist = ctx->opt.pair_schedule;
   // neighbour capacity: 2x the mean count of the densest replica + 32, at least 48
   int cap = ctx->opt.nbr_capacity;
   if (cap <= 0) {
@@ -758,6 +762,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaMemcpyAsync(S.tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(S.slot_of_tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(S.rebuild_flag, 0, sizeof(int) * (1 + n_rep), st));
+  CK(cudaMemsetAsync(S.pair_q, 0, sizeof(int) * 2, st));
   {
     std::vector<int> cr(std::max(cell_off, 1));
     for (int r = 0; r < n_rep; ++r)

@@ -460,9 +460,13 @@ __device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimCon
 // Without FUSED the forces are added to (accumulate) or stored in the FP64 force arrays.
 // Virial (EFLAG): each visit of a pair adds half of F_ij (x) (r_i - r_j) (the other visit adds the
 // other half); a pair with a fixed wall bead, which has no list of its own, counts in full.
-template <bool MIXED, bool EFLAG, bool FUSED = false, bool BONDED = false, bool UNI = false>
-__global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimConst C, bool accumulate, Acc acc,
-                                                             int bmask = 0) {
+//   PERSIST (FUSED only) a grid of the blocks that fit on the GPU at once; each block takes tiles
+//           of blockDim.x particles from a queue (s.pair_q[0], one atomic ticket per tile, no
+//           waiting) and the last block to finish resets the queue for the next launch.  Compiled
+//           for 8 resident blocks per SM (64 registers): at 9 the tile loop spills.
+template <bool MIXED, bool EFLAG, bool FUSED = false, bool BONDED = false, bool UNI = false, bool PERSIST = false>
+__global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(DevState s, SimConst C, bool accumulate,
+                                                                             Acc acc, int bmask = 0) {
   using real = real_t<MIXED>;
   static_assert(!FUSED || MIXED, "the fused form is the mixed-precision one");
   static_assert(!BONDED || FUSED, "bonded terms are fused only into the fused form");
@@ -473,7 +477,21 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
   for (int k = threadIdx.x; k < NPAIR; k += blockDim.x) {
     if constexpr (MIXED) tab[k] = s.tabf[k]; else tab[k] = s.tabd[k];
   }
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int tile_sh;
+  const int ntile = (s.N + blockDim.x - 1) / blockDim.x;
+  for (int pass = 0;; ++pass) {
+  int tile;
+  if constexpr (PERSIST) {
+    __syncthreads();  // every thread is done with the previous tile's ticket
+    if (threadIdx.x == 0) tile_sh = atomicAdd(s.pair_q, 1);
+    __syncthreads();
+    tile = tile_sh;
+    if (tile >= ntile) break;
+  } else {
+    if (pass) break;
+    tile = blockIdx.x;
+  }
+  const int i = tile * blockDim.x + threadIdx.x;
   const bool inside = i < s.N;
   const int w = inside ? __ldg(&s.info[i]) : 0;
   const bool active = inside && info_mobile(w);
@@ -685,6 +703,13 @@ __global__ void __launch_bounds__(128, MIXED ? 9 : 4) k_pair(DevState s, SimCons
     }
     obs_push<real, NV>(acc, sl, v, rep, active);
   }
+  }
+  if constexpr (PERSIST) {  // the last block out resets the queue (every block has drawn its last ticket)
+    if (threadIdx.x == 0 && atomicAdd(s.pair_q + 1, 1) == (int)gridDim.x - 1) {
+      s.pair_q[0] = 0;
+      s.pair_q[1] = 0;
+    }
+  }
 }
 
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag, Acc acc,
@@ -695,22 +720,24 @@ void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool acc
   const int g = (s.N + B - 1) / B;
   const bool uni = C.scr2_uni_f > 0.f;
   if (s.mixed && !accumulate) {  // the fused step
-    if (bonded_mask) {
-      if (uni) {
-        if (eflag) k_pair<true, true, true, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
-        else k_pair<true, false, true, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
-      } else {
-        if (eflag) k_pair<true, true, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
-        else k_pair<true, false, true, true><<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
-      }
+    using KernT = void (*)(DevState, SimConst, bool, Acc, int);
+    // [bonded][uni][eflag]
+    const KernT ks[2][2][2] = {{{k_pair<true, false, true>, k_pair<true, true, true>},
+                                {k_pair<true, false, true, false, true>, k_pair<true, true, true, false, true>}},
+                               {{k_pair<true, false, true, true>, k_pair<true, true, true, true>},
+                                {k_pair<true, false, true, true, true>, k_pair<true, true, true, true, true>}}};
+    // the persistent schedule for the steps without energies: [bonded][uni]
+    const KernT kp[2][2] = {{k_pair<true, false, true, false, false, true>, k_pair<true, false, true, false, true, true>},
+                            {k_pair<true, false, true, true, false, true>, k_pair<true, false, true, true, true, true>}};
+    const int bi = bonded_mask ? 1 : 0, ui = uni ? 1 : 0;
+    if (s.pair_persist && !eflag) {
+      const KernT k = kp[bi][ui];
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, B, 0);
+      const int grid = std::min(g, std::max(per_sm, 1) * s.nsm);
+      k<<<grid, B, 0, st>>>(s, C, false, acc, bonded_mask);
     } else {
-      if (uni) {
-        if (eflag) k_pair<true, true, true, false, true><<<g, B, 0, st>>>(s, C, false, acc);
-        else k_pair<true, false, true, false, true><<<g, B, 0, st>>>(s, C, false, acc);
-      } else {
-        if (eflag) k_pair<true, true, true><<<g, B, 0, st>>>(s, C, false, acc);
-        else k_pair<true, false, true><<<g, B, 0, st>>>(s, C, false, acc);
-      }
+      ks[bi][ui][eflag ? 1 : 0]<<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
     }
   } else if (s.mixed) {  // the drop-in: added to the FP64 force
     if (eflag) k_pair<true, true><<<g, B, 0, st>>>(s, C, true, acc);

@@ -1,4 +1,5 @@
-"""Autotuning of the neighbour-list skin and of the pair kernel's block size.
+"""Autotuning of the neighbour-list skin, the list-build cell size, the pair kernel's block size
+and its schedule (one block per tile, or persistent blocks over a tile queue).
 
 The skin trades the list rebuild (sort + list build, whose frequency falls as the skin grows) for
 the pair kernel (whose lists lengthen with it).  The best value depends on the density, the
@@ -10,7 +11,7 @@ batch (n_sample >= the replica count) when the tuned skin is for that batch.
 """
 import numpy as np
 
-from . import configs, md
+from . import abi, configs, md
 
 
 def sample_replicas(reps, n_sample):
@@ -67,5 +68,34 @@ def tune_block(params, reps, skin, candidates=(64, 128), n_sample=32, steps=80, 
         ms = g.event_elapsed(0, 1)
         g.close()
         rates[int(b)] = n_atoms * max(1, steps // chunk) * chunk / (ms / 1000.0)
+    best = max(rates, key=rates.get)
+    return best, rates
+
+
+def tune_option(params, reps, skin, name, candidates, n_sample=32, steps=80, warmup=20, precision="mixed",
+                device=0, chunk=10, **opt):
+    """Times mfa_step at the given skin with each candidate value of the context option `name`
+    (an mfa_options field: list_cells, pair_schedule, block_size); a candidate that the library
+    refuses for these boxes is skipped.  Returns (best value, {value: atom-steps/s})."""
+    sample = sample_replicas(reps, n_sample)
+    systems, a_type, r0, v = configs.concat(sample)
+    n_atoms = int(sum(s.n_part for s in systems))
+    rates = {}
+    for c in candidates:
+        try:
+            g = md.MdSystem(params, systems, a_type, r0, v, precision=precision, device=device, skin=skin,
+                            **dict(opt, **{name: c}))
+        except abi.MfaError:
+            continue
+        for _ in range(max(1, warmup // chunk)):
+            g.step(chunk)
+        g.synchronize()
+        g.event_record(0)
+        for _ in range(max(1, steps // chunk)):
+            g.step(chunk)
+        g.event_record(1)
+        ms = g.event_elapsed(0, 1)
+        g.close()
+        rates[c] = n_atoms * max(1, steps // chunk) * chunk / (ms / 1000.0)
     best = max(rates, key=rates.get)
     return best, rates

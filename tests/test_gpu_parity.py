@@ -405,6 +405,24 @@ def test_energy_cadence_does_not_change_the_trajectory(gpu, setup):
             assert np.array_equal(x, y)
 
 
+def test_persistent_pair_schedule_does_not_change_the_trajectory(gpu):
+    """mfa_options.pair_schedule 1 (persistent blocks taking 128-particle tiles from a queue)
+    changes only which block evaluates a particle: 30 fused steps (rebuilds included, energies
+    every 10th step) give the same state bit for bit, and the queue is reset between launches
+    (a second context and a second run agree too)."""
+    p = configs.wca_params(gamma=5.0)
+    systems, a_type, r0, v = configs.concat(configs.replicas(6, seed=4))
+    out = []
+    for sch in (0, 1, 1):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", pair_schedule=sch)
+        g.step(30)
+        out.append(g.state())
+        g.close()
+    for o in out[1:]:
+        for x, y in zip(out[0], o):
+            assert np.array_equal(x, y)
+
+
 def test_measurement_aids(gpu):
     """mfa_fp32_fma_peak measures a plausible FP32 FMA throughput (a GB300 has 152 SMs x 128 lanes
     x 2 FLOP x ~2 GHz = ~80 TFLOP/s nominal); mfa_kspace_info gives the k-set and charge counts of
