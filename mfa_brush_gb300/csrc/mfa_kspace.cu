@@ -9,18 +9,19 @@
 //                 from an FP64 phase reduced to [-1/2, 1/2) turns (sincospi); stored column-major
 //                 ([column][particle]) so that a warp reads 32 particles of one column at once;
 //   k_ks_rho:     rho(row, nx) = sum_p (q Y Z)(p, row) X(p, nx) as a complex matrix product per
-//                 block of 64 rows x 32 nx slots x a particle chunk: lane = slot, warp = 8 rows,
-//                 tiles of 32 particles in shared memory; plain sums over a tile and Kahan-
-//                 compensated sums across tiles in FP32 (MIXED), or FP64 sums; one partial per
-//                 particle chunk;
+//                 block of 64 rows x 16 |nx| slots x a particle chunk, +nx and -nx from the same
+//                 four real sums (X(-n) = conj X(n)): lane = slot, half-warp = 4 rows, tiles of
+//                 32 particles in shared memory; plain sums over a tile and Kahan-compensated
+//                 sums across tiles in FP32 (MIXED), or FP64 sums; one partial per particle
+//                 chunk;
 //   k_ks_rho_sum: the partials of each k summed in a fixed order; G rho per k and the dense
 //                 (row, slot) table of (G rho, kx G rho) for the force; U reduced
 //                 deterministically (per-block partials, the last block adds them);
-//   k_ks_force_dense (mixed, nxm <= 15): thread per particle with X(-nxm..nxm) in registers, a
-//                 chunk of 32 rows per block streamed from the dense table: per row
-//                 S = sum conj(X) G rho and S_x = sum conj(X) kx G rho, then Im(conj(Y Z) S_x)
-//                 to F_x and ky, kz times Im(conj(Y Z) S) to F_y, F_z; rows added with Kahan
-//                 compensation;
+//   k_ks_force_dense (mixed, nxm <= 15): thread per particle with X(0..nxm) in registers, a
+//                 chunk of 32 rows per block streamed from the dense table with its +nx and -nx
+//                 slots folded together: per row S = sum conj(X) G rho and
+//                 S_x = sum conj(X) kx G rho, then Im(conj(Y Z) S_x) to F_x and ky, kz times
+//                 Im(conj(Y Z) S) to F_y, F_z; rows added with Kahan compensation;
 //   k_ks_force:   the same per row, one k at a time from shared memory (FP64, or nxm > 15);
 //   k_ks_force_sum: the chunk partials in a fixed order, times -8 pi q / V, into the force array.
 // dipolar_correction.f90:20-33 (Yeh-Berkowitz slab term) is k_ks_dipole + k_ks_dipole_force, FP64.
@@ -90,17 +91,23 @@ __global__ void k_ks_tables(DevState s, KSpace K) {
 
 constexpr int KS_TILE = 32;  // particles per shared-memory tile of k_ks_rho (one per lane)
 
-// rho(row, nx) = sum_p A(p, row) X(p, nx), A = q Y(ny) Z(nz): a complex matrix product per
-// block of KS_RB rows, 32 nx slots (blockIdx.z) and a chunk of particles.  Lane l owns slot
-// nx = 32 z + l - nxm, warp w owns rows 8 w .. 8 w + 7; slots outside a row's k-range are
-// computed and not stored.  Per particle a lane reads its X (the warp reads one contiguous
-// 256-byte row) and the eight A of its warp (broadcasts, four 16-byte loads) for 32 FMAs.
-// The staging stores, one particle per lane, use odd (X) or 4 mod 32 word (A) row strides.
+// rho(row, nx) = sum_p A(p, row) X(p, nx), A = q Y(ny) Z(nz), with X(p, -n) = conj X(p, n): the
+// four real sums P1 = sum a c, P2 = sum b d, P3 = sum a d, P4 = sum b c over A = a + ib,
+// X(p, n) = c + id give both rho(row, n) = (P1 - P2, P3 + P4) and rho(row, -n) = (P1 + P2,
+// P4 - P3).  A block takes KS_RB rows, 16 slots n = 16 z .. 16 z + 15 (blockIdx.z) and a chunk of
+// particles.  Lane l owns slot n = 16 z + (l & 15); warp w owns rows 8 w .. 8 w + 7, four of them
+// per half-warp (l >> 4).  Per particle a lane reads its X (the half-warps share the 16 slots)
+// and its four A (two 16-byte loads, one address per half-warp) for 16 FMAs, which cover up to
+// eight k: half the products of a slot per signed nx.  Slots outside a row's k-range are
+// computed and not stored.  The staging stores, one particle per lane, use odd (X) or 4 mod 32
+// word (A) row strides.
 constexpr int KS_RHO_T = 256;  // threads of a k_ks_rho block (8 warps)
-constexpr int KS_RW = 8;       // rows per warp
+constexpr int KS_RW = 8;       // rows per warp (four per half-warp)
 constexpr int KS_RB = 64;      // rows per block
-constexpr int KS_XS = 33;      // X row stride (8-byte slots)
+constexpr int KS_SL = 16;      // |nx| slots per block
+constexpr int KS_XS = KS_SL + 1;  // X row stride (8-byte slots)
 constexpr int KS_AS = KS_RB + 2;  // A row stride (8-byte slots; 16-byte aligned rows)
+static_assert(KS_TILE * KS_XS * sizeof(float2) % 16 == 0, "the A rows follow the X rows 16-byte aligned");
 
 template <bool MIXED>
 __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
@@ -108,23 +115,27 @@ __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
   using Cx = kcplx<MIXED>;
   extern __shared__ __align__(16) unsigned char shraw[];
   Cx* Xs = reinterpret_cast<Cx*>(shraw);              // [KS_TILE][KS_XS]
-  Cx* As = Xs + KS_TILE * KS_XS;                      // [KS_TILE][KS_AS] (16-byte aligned)
+  Cx* As = Xs + KS_TILE * KS_XS;                      // [KS_TILE][KS_AS] (16-byte aligned: 32 x 17 x 8 B)
   int2* rc = reinterpret_cast<int2*>(As + KS_TILE * KS_AS);  // [KS_RB] signed Y column, Z column
   const Cx* tab = ktab<MIXED>(K);
   const int rbeg = blockIdx.x * KS_RB, nr = min(KS_RB, K.nrows - rbeg);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, half = lane >> 4;
   constexpr int NW = KS_RHO_T / 32;
-  const int sbase = blockIdx.z * 32;
-  const bool act = warp * KS_RW < nr;
+  constexpr int RL = KS_RW / 2;  // rows per lane
+  const int slot = blockIdx.z * KS_SL + (lane & (KS_SL - 1));  // |nx| of the lane
+  const int r0 = warp * KS_RW + half * RL;                      // the lane's first row
+  const bool act = r0 < nr;
   for (int r = threadIdx.x; r < nr; r += KS_RHO_T) {
     const int4 R = K.rows[rbeg + r];
     const int yc = K.nxm + 1 + abs(R.z);
     rc[r] = make_int2(R.z < 0 ? -yc : yc, K.nxm + K.nym + 2 + R.w);
   }
   const int p_beg = blockIdx.y * K.pchunk, p_end = min(K.nq, p_beg + K.pchunk);
-  real sr[KS_RW], si[KS_RW], cr[KS_RW], ci[KS_RW];
+  real s[4][RL], c[4][RL];  // sums P1..P4 across tiles and their compensations
 #pragma unroll
-  for (int i = 0; i < KS_RW; ++i) sr[i] = si[i] = cr[i] = ci[i] = 0;
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int i = 0; i < RL; ++i) s[a][i] = c[a][i] = 0;
   for (int t0 = p_beg; t0 < p_end; t0 += KS_TILE) {
     const int nt = min(KS_TILE, p_end - t0);
     __syncthreads();
@@ -132,19 +143,15 @@ __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
       const int pq = t0 + lane;
       real q;
       if constexpr (MIXED) q = K.qvalf[pq]; else q = K.qval[pq];
-      Cx xv[32 / NW];
 #pragma unroll
-      for (int i = 0; i < 32 / NW; ++i) {  // slot columns warp + NW i
-        const int nx = sbase + warp + NW * i - K.nxm;
-        xv[i].x = 0;
-        xv[i].y = 0;
-        if (nx <= K.nxm) {
-          xv[i] = tab[(size_t)abs(nx) * K.nq + pq];
-          if (nx < 0) xv[i].y = -xv[i].y;
-        }
+      for (int i = 0; i < KS_SL / NW; ++i) {  // slot columns warp + NW i
+        const int n = blockIdx.z * KS_SL + warp + NW * i;
+        Cx xv;
+        xv.x = 0;
+        xv.y = 0;
+        if (n <= K.nxm) xv = tab[(size_t)n * K.nq + pq];
+        Xs[lane * KS_XS + warp + NW * i] = xv;
       }
-#pragma unroll
-      for (int i = 0; i < 32 / NW; ++i) Xs[lane * KS_XS + warp + NW * i] = xv[i];
 #pragma unroll
       for (int h = 0; h < KS_RB / NW; h += 4) {  // rows warp + NW (h .. h+3)
         Cx yv[4], zv[4];
@@ -174,52 +181,60 @@ __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
     __syncthreads();
     if (act) {
       // plain sums over the tile's particles, compensated sums across tiles
-      real tr[KS_RW], ti[KS_RW];
+      real t[4][RL];
 #pragma unroll
-      for (int i = 0; i < KS_RW; ++i) tr[i] = ti[i] = 0;
-#pragma unroll 1
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int i = 0; i < RL; ++i) t[a][i] = 0;
+#pragma unroll 2
       for (int p = 0; p < nt; ++p) {
-        const Cx x = Xs[p * KS_XS + lane];
-        Cx A[KS_RW];
+        const Cx x = Xs[p * KS_XS + (lane & (KS_SL - 1))];
+        Cx A[RL];
         if constexpr (MIXED) {
-          const float4* A4 = reinterpret_cast<const float4*>(As + p * KS_AS + warp * KS_RW);
+          const float4* A4 = reinterpret_cast<const float4*>(As + p * KS_AS + r0);
 #pragma unroll
-          for (int i = 0; i < KS_RW / 2; ++i) {
+          for (int i = 0; i < RL / 2; ++i) {
             const float4 u = A4[i];
             A[2 * i] = make_float2(u.x, u.y);
             A[2 * i + 1] = make_float2(u.z, u.w);
           }
         } else {
 #pragma unroll
-          for (int i = 0; i < KS_RW; ++i) A[i] = As[p * KS_AS + warp * KS_RW + i];
+          for (int i = 0; i < RL; ++i) A[i] = As[p * KS_AS + r0 + i];
         }
 #pragma unroll
-        for (int i = 0; i < KS_RW; ++i) {
-          tr[i] = fma(x.x, A[i].x, tr[i]);
-          tr[i] = fma(-x.y, A[i].y, tr[i]);
-          ti[i] = fma(x.x, A[i].y, ti[i]);
-          ti[i] = fma(x.y, A[i].x, ti[i]);
+        for (int i = 0; i < RL; ++i) {
+          t[0][i] = fma(A[i].x, x.x, t[0][i]);
+          t[1][i] = fma(A[i].y, x.y, t[1][i]);
+          t[2][i] = fma(A[i].x, x.y, t[2][i]);
+          t[3][i] = fma(A[i].y, x.x, t[3][i]);
         }
       }
 #pragma unroll
-      for (int i = 0; i < KS_RW; ++i) {
-        ksum<MIXED>(sr[i], cr[i], tr[i], K.plain);
-        ksum<MIXED>(si[i], ci[i], ti[i], K.plain);
-      }
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int i = 0; i < RL; ++i) ksum<MIXED>(s[a][i], c[a][i], t[a][i], K.plain);
     }
   }
-  if (act) {
-    const int nx = sbase + lane - K.nxm;
+  if (act && slot <= K.nxm) {
     double* o = K.rho_part + (size_t)blockIdx.y * 2 * K.nk;
 #pragma unroll
-    for (int i = 0; i < KS_RW; ++i) {
-      const int r = warp * KS_RW + i;
+    for (int i = 0; i < RL; ++i) {
+      const int r = r0 + i;
       if (r < nr) {
         const int4 R = K.rows[rbeg + r];
-        const int k = R.x + nx - K.kn[R.x].x;
-        if (k >= R.x && k < R.y) {
-          o[2 * k] = (double)sr[i] - (double)cr[i];
-          o[2 * k + 1] = (double)si[i] - (double)ci[i];
+        const double p1 = (double)s[0][i] - (double)c[0][i], p2 = (double)s[1][i] - (double)c[1][i];
+        const double p3 = (double)s[2][i] - (double)c[2][i], p4 = (double)s[3][i] - (double)c[3][i];
+        const int lo = K.kn[R.x].x;  // the row's first nx
+        const int kp = R.x + slot - lo;
+        if (kp >= R.x && kp < R.y) {
+          o[2 * kp] = p1 - p2;
+          o[2 * kp + 1] = p3 + p4;
+        }
+        const int km = R.x - slot - lo;
+        if (slot > 0 && km >= R.x && km < R.y) {
+          o[2 * km] = p1 + p2;
+          o[2 * km + 1] = p4 - p3;
         }
       }
     }
@@ -465,40 +480,56 @@ __global__ void __launch_bounds__(KS_FB) k_ks_force(KSpace K) {
   o[2] = (double)fz - (double)cz;
 }
 
-// Mixed precision, 4 QX = 4..32 slots: the thread keeps X(p, nx) for every slot in registers and
-// reads the dense slot table (W, kx W), W = G rho, of a chunk of rows from shared memory (one
-// broadcast 16-byte load per slot).  With S = sum_nx conj(X) W and Sx = sum_nx conj(X) kx W over
-// a row, that row adds Im(conj(Y Z) Sx) to F_x and ky, kz times Im(conj(Y Z) S) to F_y, F_z.
-// The rows are taken in order of their slot range (frow), so that the rows of a chunk share a
-// narrow window of slots; slots outside the window are skipped (a branch uniform over the block).
-template <int QX>
+// Mixed precision, nxm <= 15: the thread keeps X(p, n) for n = 0 .. nxm in registers and reads
+// the slot table of a chunk of rows from shared memory.  With S = sum_nx conj(X) W and
+// Sx = sum_nx conj(X) kx W over a row (W = G rho), that row adds Im(conj(Y Z) Sx) to F_x and
+// ky, kz times Im(conj(Y Z) S) to F_y, F_z.  X(p, -n) = conj X(p, n) and kx(-n) = -kx(n), so the
+// two signed slots +-n fold into one: with X(n) = c + id, W(n) = u + iv, W(-n) = u' + iv',
+//   S  gets c (u + u') + d (v - v') + i [c (v + v') - d (u - u')],
+//   Sx gets c (ku + ku') + d (kv - kv') + i [c (kv + kv') - d (ku - ku')],
+// where ku = kx(n) u, ku' = kx(-n) u' (the table's kx W columns): eight FMAs per |n| from two
+// broadcast 16-byte loads, where the signed slots took sixteen.  The block folds the signed slot
+// table (k_ks_rho_sum's (W, kx W) per signed slot) while staging it.  The rows are taken in order
+// of their slot range (frow), so that the rows of a chunk share a narrow window of slots; slots
+// outside the window are skipped (a branch uniform over the block).
+template <int QF>
 __global__ void __launch_bounds__(KS_FB) k_ks_force_dense(KSpace K) {
-  constexpr int NXP = 4 * QX;
+  constexpr int NF = 4 * QF;  // folded slots |n| = 0 .. NF - 1
   extern __shared__ __align__(16) unsigned char shraw[];
-  float4* Wd = reinterpret_cast<float4*>(shraw);          // [KS_FR][NXP]
-  int2* rc = reinterpret_cast<int2*>(Wd + KS_FR * NXP);   // [KS_FR] signed Y column, Z column
-  float2* ryz = reinterpret_cast<float2*>(rc + KS_FR);    // [KS_FR] ky, kz
+  float4* Wd = reinterpret_cast<float4*>(shraw);              // [KS_FR][NF][2]
+  int2* rc = reinterpret_cast<int2*>(Wd + KS_FR * NF * 2);    // [KS_FR] signed Y column, Z column
+  float2* ryz = reinterpret_cast<float2*>(rc + KS_FR);        // [KS_FR] ky, kz
   const int rbeg = blockIdx.y * KS_FR, nr = min(KS_FR, K.nrows - rbeg);
-  const int2 win = K.fwin[blockIdx.y];  // slots win.x .. win.y
-  const float4* wsrc = K.wdense + (size_t)rbeg * NXP;
-  for (int e = threadIdx.x; e < nr * NXP; e += KS_FB) Wd[e] = wsrc[e];
+  const int nxm = K.nxm, nsig = 4 * K.qx;
+  const int2 win = K.fwin[blockIdx.y];  // signed slots win.x .. win.y (slot j is nx = j - nxm)
+  // the folded window: |nx| from mlo to mhi
+  const int ax = abs(win.x - nxm), ay = abs(win.y - nxm);
+  const int mlo = (win.x <= nxm && nxm <= win.y) ? 0 : min(ax, ay), mhi = max(ax, ay);
+  const float4* wsrc = K.wdense + (size_t)rbeg * nsig;
+  for (int e = threadIdx.x; e < nr * NF; e += KS_FB) {
+    const int r = e / NF, m = e - r * NF;
+    float4 wp = make_float4(0.f, 0.f, 0.f, 0.f), wm = wp;
+    if (m <= nxm) {
+      wp = wsrc[r * nsig + nxm + m];
+      if (m > 0) wm = wsrc[r * nsig + nxm - m];
+    }
+    Wd[2 * e] = make_float4(wp.x + wm.x, wp.y - wm.y, wp.y + wm.y, wp.x - wm.x);
+    Wd[2 * e + 1] = make_float4(wp.z + wm.z, wp.w - wm.w, wp.w + wm.w, wp.z - wm.z);
+  }
   for (int r = threadIdx.x; r < nr; r += KS_FB) {
     const int4 R = K.rows[K.frow[rbeg + r]];
-    const int yc = K.nxm + 1 + abs(R.z);
-    rc[r] = make_int2(R.z < 0 ? -yc : yc, K.nxm + K.nym + 2 + R.w);
+    const int yc = nxm + 1 + abs(R.z);
+    rc[r] = make_int2(R.z < 0 ? -yc : yc, nxm + K.nym + 2 + R.w);
     ryz[r] = make_float2((float)K.kvec[3 * R.x + 1], (float)K.kvec[3 * R.x + 2]);
   }
   const int p = blockIdx.x * KS_FB + threadIdx.x;
   const int pc = min(p, K.nq - 1);
   const float2* T = K.tabf + pc;
-  float2 X[NXP];
+  float2 X[NF];
 #pragma unroll
-  for (int j = 0; j < NXP; ++j) {
+  for (int j = 0; j < NF; ++j) {
     X[j] = make_float2(0.f, 0.f);
-    if (j >= win.x && j <= win.y) {
-      X[j] = T[(size_t)abs(j - K.nxm) * K.nq];
-      if (j < K.nxm) X[j].y = -X[j].y;
-    }
+    if (j >= mlo && j <= mhi && j <= nxm) X[j] = T[(size_t)j * K.nq];
   }
   __syncthreads();
   if (p >= K.nq) return;
@@ -516,21 +547,19 @@ __global__ void __launch_bounds__(KS_FB) k_ks_force_dense(KSpace K) {
     if (R.x < 0) Y.y = -Y.y;
     float2 YZ;
     cmul(Y, Z, YZ);
-    const float4* w = Wd + r * NXP;
+    const float4* w = Wd + r * NF * 2;
     float s_re = 0.f, s_im = 0.f, x_re = 0.f, x_im = 0.f;
 #pragma unroll
-    for (int g = 0; g < QX; ++g) {  // groups of four slots; a group outside the window is skipped
-      if (4 * g + 3 < win.x || 4 * g > win.y) continue;
-      float4 v[4];
+    for (int g = 0; g < QF; ++g) {  // groups of four slots; a group outside the window is skipped
+      if (4 * g + 3 < mlo || 4 * g > mhi) continue;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) v[i] = w[4 * g + i];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {  // conj(X) W = (X.x W.x + X.y W.y) + i (X.x W.y - X.y W.x)
+      for (int i = 0; i < 4; ++i) {
         const float2 x = X[4 * g + i];
-        s_re = fmaf(x.x, v[i].x, fmaf(x.y, v[i].y, s_re));
-        s_im = fmaf(x.x, v[i].y, fmaf(-x.y, v[i].x, s_im));
-        x_re = fmaf(x.x, v[i].z, fmaf(x.y, v[i].w, x_re));
-        x_im = fmaf(x.x, v[i].w, fmaf(-x.y, v[i].z, x_im));
+        const float4 a = w[2 * (4 * g + i)], b = w[2 * (4 * g + i) + 1];
+        s_re = fmaf(x.x, a.x, fmaf(x.y, a.y, s_re));
+        s_im = fmaf(x.x, a.z, fmaf(-x.y, a.w, s_im));
+        x_re = fmaf(x.x, b.x, fmaf(x.y, b.y, x_re));
+        x_im = fmaf(x.x, b.z, fmaf(-x.y, b.w, x_im));
       }
     }
     const float srow = YZ.x * s_im - YZ.y * s_re;
@@ -582,19 +611,19 @@ size_t force_smem(const KSpace& K, bool mixed) {
   return (size_t)(2 * K.nxm + 1) * KS_FB * cx + (size_t)K.fchunk_k_max * (mixed ? sizeof(KD<true>) : sizeof(KD<false>)) +
          (size_t)K.fchunk_rows_max * (sizeof(int4) + cx);
 }
+// groups of four folded slots |nx| = 0 .. nxm of k_ks_force_dense
+int dense_qf(const KSpace& K) { return (K.nxm + 4) / 4; }
 size_t dense_smem(const KSpace& K) {
-  return (size_t)KS_FR * (4 * K.qx * sizeof(float4) + sizeof(int2) + sizeof(float2));
+  return (size_t)KS_FR * (4 * dense_qf(K) * 2 * sizeof(float4) + sizeof(int2) + sizeof(float2));
 }
 constexpr int KS_DENSE_QX_MAX = 8;  // the register-resident X of k_ks_force_dense: nxm <= 15
 
-template <int QX>
+template <int QF>
 void launch_dense(const KSpace& K, dim3 g, cudaStream_t st) {
-  k_ks_force_dense<QX><<<g, KS_FB, dense_smem(K), st>>>(K);
+  k_ks_force_dense<QF><<<g, KS_FB, dense_smem(K), st>>>(K);
 }
 typedef void (*dense_launcher)(const KSpace&, dim3, cudaStream_t);
-const dense_launcher kDense[KS_DENSE_QX_MAX + 1] = {nullptr,          launch_dense<1>, launch_dense<2>,
-                                                    launch_dense<3>, launch_dense<4>, launch_dense<5>,
-                                                    launch_dense<6>, launch_dense<7>, launch_dense<8>};
+const dense_launcher kDense[5] = {nullptr, launch_dense<1>, launch_dense<2>, launch_dense<3>, launch_dense<4>};
 bool use_dense(const KSpace& K, bool mixed) { return mixed && K.qx <= KS_DENSE_QX_MAX; }
 }  // namespace
 
@@ -612,7 +641,7 @@ int kspace_prepare(const KSpace& K, bool mixed) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_rho<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ks_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  return (int)e;  // dense_smem stays below 48 KB: 32 rows x 32 slots x 16 B + 512 B
+  return (int)e;  // dense_smem stays below 48 KB: 32 rows x 16 folded slots x 32 B + 512 B
 }
 
 void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaStream_t st, bool eflag, Acc acc,
@@ -622,7 +651,7 @@ void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaSt
   const int nt = K.nq * K.ncol;
   if (s.mixed) k_ks_tables<true><<<(nt + 255) / 256, 256, 0, st>>>(s, K);
   else k_ks_tables<false><<<(nt + 255) / 256, 256, 0, st>>>(s, K);
-  const dim3 g1((K.nrows + KS_RB - 1) / KS_RB, K.npchunks, (2 * K.nxm + 1 + 31) / 32);
+  const dim3 g1((K.nrows + KS_RB - 1) / KS_RB, K.npchunks, (K.nxm + KS_SL) / KS_SL);
   const size_t shm1 = rho_smem(K, s.mixed);
   if (s.mixed) k_ks_rho<true><<<g1, KS_RHO_T, shm1, st>>>(K);
   else k_ks_rho<false><<<g1, KS_RHO_T, shm1, st>>>(K);
@@ -632,7 +661,7 @@ void launch_kspace(const DevState& s, const SimConst& C, const KSpace& K, cudaSt
   else k_ks_rho_sum<false><<<gs, 256, 0, st>>>(K, 4. * pi, fac_alpha, acc, eflag);
   const dim3 g2((K.nq + KS_FB - 1) / KS_FB, K.nkchunks);
   if (use_dense(K, s.mixed)) {
-    kDense[K.qx](K, g2, st);
+    kDense[dense_qf(K)](K, g2, st);
   } else {
     const size_t shm2 = force_smem(K, s.mixed);
     if (s.mixed) k_ks_force<true><<<g2, KS_FB, shm2, st>>>(K);
