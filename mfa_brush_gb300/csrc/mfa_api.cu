@@ -871,8 +871,11 @@ int mfa_n_particles(const mfa_ctx* ctx, int64_t* n_total, int32_t* n_rep) {
 }
 
 // ---- per-routine drop-ins -------------------------------------------------------------------
+// A drop-in clears the accumulator slots it fills; from then on the energy, virial and head-force
+// readers take the per-routine accumulators (until the next mfa_step record).
 static int zero_call_slot(mfa_ctx* ctx, int slot, int n = 1) {
   CK(cudaMemsetAsync(ctx->acc_call + (size_t)slot * ctx->nrep, 0, sizeof(double) * ctx->nrep * n, ctx->st));
+  ctx->last_source = 2;
   return MFA_OK;
 }
 // the 9 virial slots of a group (each drop-in replaces its own group)
@@ -999,7 +1002,7 @@ int mfa_dipolar_correction(mfa_ctx* ctx, double* v) {
   if (!ctx) return MFA_ERR_ARG;
   if (!ctx->kspace) return fail(ctx, MFA_ERR_STATE, "dipolar_correction: not a charged system");
   int r;
-  if ((r = zero_call_slot(ctx, O_VDIP))) return r;
+  if ((r = zero_call_slot(ctx, O_VDIP)) || (r = zero_call_group(ctx, V_DIP))) return r;
   launch_dipolar(ctx->S, ctx->C, ctx->K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
   ctx->launches += 2;
   CK(cudaGetLastError());

@@ -291,9 +291,9 @@ def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod, model):
     the reference's k-set rule (8070 vectors), dipolar correction.  "counterions": the brush charge
     -4 per chain spread over its beads, 1280 +1 counterions, neutral solvent (13,760 charged
     particles; configs.charged_brush).  "uniform": -0.1 per brush bead neutralised by the whole
-    solvent (33,280 charged particles).  Prints the k-space energy and force errors of the FP64,
-    the mixed (Kahan-compensated FP32) and the plain FP32 sums against the FP64 oracle; the mixed
-    path must meet the 1e-5 force criterion."""
+    solvent (33,280 charged particles).  Prints the k-space energy, force and virial errors of the
+    FP64, the mixed (Kahan-compensated FP32) and the plain FP32 sums against the FP64 oracle; the
+    mixed path must meet the 1e-5 criterion on each."""
     if model == "counterions":
         p, (s, a_type, r0, v) = configs.charged_brush(gamma=1.0)
     else:
@@ -313,6 +313,7 @@ def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod, model):
     o.zero_force()
     uko = o.ewald_k()
     fko = o.state()[3]
+    wko = o.virial()["kspace"]
     rms = np.sqrt(np.mean(np.sum(fko ** 2, axis=1)))
     out = {}
     for name, precision, plain in (("fp64", "fp64", False), ("mixed", "mixed", False), ("plain", "mixed", True)):
@@ -320,13 +321,15 @@ def test_charged_brush_kspace_precision_at_full_size(gpu, oracle_mod, model):
         g.zero_force()
         uk = g.ewald_k()[0]
         fk = g.state()[3]
-        out[name] = (rel(uk, uko), np.linalg.norm(fk - fko, axis=1).max() / rms)
+        wk = g.virial()[0]["kspace"]
+        out[name] = (rel(uk, uko), np.linalg.norm(fk - fko, axis=1).max() / rms,
+                     np.abs(wk - wko).max() / np.abs(wko).max())
         g.close()
-    print("k-space vs FP64 oracle (%s, N=%d, rel energy error, max|dF|/F_rms): fp64 %.2e %.2e  "
-          "compensated FP32 %.2e %.2e  plain FP32 %.2e %.2e"
+    print("k-space vs FP64 oracle (%s, N=%d; rel energy error, max|dF|/F_rms, max|dW|/max|W| of the "
+          "k-space virial): fp64 %.2e %.2e %.2e  compensated FP32 %.2e %.2e %.2e  plain FP32 %.2e %.2e %.2e"
           % (model, s.n_mon_tot, *out["fp64"], *out["mixed"], *out["plain"]))
-    assert out["fp64"][0] < 1e-10 and out["fp64"][1] < 1e-9
-    assert out["mixed"][0] < 1e-5 and out["mixed"][1] < 1e-5
+    assert out["fp64"][0] < 1e-10 and out["fp64"][1] < 1e-9 and out["fp64"][2] < 1e-10
+    assert out["mixed"][0] < 1e-5 and out["mixed"][1] < 1e-5 and out["mixed"][2] < 1e-5
     assert out["plain"][0] < 1e-3 and out["plain"][1] < 1e-3  # reported; no 1e-5 promise
 
 
