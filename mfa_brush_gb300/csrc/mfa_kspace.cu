@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(KS_RHO_T, MIXED ? 3 : 1) k_ks_rho(KSpace K) {
       for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int i = 0; i < RL; ++i) t[a][i] = 0;
-#pragma unroll 2
+#pragma unroll 1
       for (int p = 0; p < nt; ++p) {
         const Cx x = Xs[p * KS_XS + (lane & (KS_SL - 1))];
         Cx A[RL];
