@@ -195,6 +195,11 @@ typedef struct mfa_options {
                                1: as many blocks as fit on the GPU at once, each taking blocks of
                                particles from a queue (an atomic ticket, no waiting) until none
                                is left.  The forces are the same bit for bit.                    */
+  int32_t separate_integrator; /* 0 (default): in the mixed-precision mfa_step without k-space,
+                               the steps without an energy record run their integration in the
+                               tail of the pair kernel (one launch per step instead of two);
+                               1: a separate integrator kernel on every step.  The trajectory is
+                               the same bit for bit.                                          */
 } mfa_options;
 
 typedef struct mfa_energies {

@@ -88,7 +88,8 @@ class Options(C.Structure):
     _fields_ = [("precision", i32), ("device", i32), ("skin", f64), ("nbr_capacity", i32),
                 ("energy_every", i32), ("use_graphs", i32), ("block_size", i32),
                 ("profile_from_step", i32), ("kspace_plain_sums", i32), ("observe", i32),
-                ("series_capacity", i32), ("list_cells", i32), ("pair_schedule", i32)]
+                ("series_capacity", i32), ("list_cells", i32), ("pair_schedule", i32),
+                ("separate_integrator", i32)]
 
 
 class Energies(C.Structure):

@@ -40,6 +40,7 @@ struct mfa_ctx {
   std::vector<double> v_ff_walls;  // LJ energy of the fixed wall beads among themselves (WALL 1)
   KSpace K;
   bool kspace = false;
+  bool fuse_integ = false;  // mfa_step runs the integration of its plain steps in the pair kernel
   unsigned* h_status = nullptr;  // pinned: [0] status bits, [1] largest list count seen
   cudaEvent_t ev_status = nullptr;  // recorded after each copy of the status words into h_status
   bool grow_pending = false;     // the list capacity is to be raised before the next step
@@ -170,7 +171,7 @@ __global__ void k_cond_rebuild(const int* flag, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, flag[0] ? 1u : 0u);
 }
 
-int capture_conditional_rebuild(mfa_ctx* ctx) {
+int capture_conditional_rebuild(mfa_ctx* ctx, const DevState& S) {
   cudaStream_t st = ctx->st;
   cudaStreamCaptureStatus cs;
   cudaGraph_t graph;
@@ -179,7 +180,7 @@ int capture_conditional_rebuild(mfa_ctx* ctx) {
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
-  k_cond_rebuild<<<1, 1, 0, st>>>(ctx->S.rebuild_flag, h);
+  k_cond_rebuild<<<1, 1, 0, st>>>(S.rebuild_flag, h);
   CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
   cudaGraphNodeParams cp = {};  // aggregate initialisation: all reserved fields zero
   cp.type = cudaGraphNodeTypeConditional;
@@ -190,7 +191,7 @@ int capture_conditional_rebuild(mfa_ctx* ctx) {
   CK(cudaGraphAddNode(&node, graph, deps, nullptr, nd, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(ctx->st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  launch_rebuild(ctx->S, ctx->st2, false);  // the flagged replicas (the flags stay set until its last kernel)
+  launch_rebuild(S, ctx->st2, false);  // the flagged replicas (the flags stay set until its last kernel)
   cudaGraph_t captured;
   CK(cudaStreamEndCapture(ctx->st2, &captured));
   CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
@@ -697,7 +698,12 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   for (auto d : dst) DA(*d, Nn);
   for (int k = 0; k < 9; ++k) DA(S.tmp[k], Nn);
   DA(S.tag, Nn); DA(S.info, Nn); DA(S.tmp_tag, Nn); DA(S.tmp_info, Nn); DA(S.slot_of_tag, Nn);
-  if (S.mixed) { DA(S.pfx, Nn); DA(S.vf, Nn); DA(S.f4, Nn); } else { DA(S.pd, Nn); DA(S.vd, Nn); }
+  if (S.mixed) {
+    DA(S.pfx, Nn); DA(S.vf, Nn); DA(S.f4, Nn);
+    DA(S.pfx_alt, Nn); DA(S.vf_alt, Nn);
+  } else {
+    DA(S.pd, Nn); DA(S.vd, Nn);
+  }
   DA(S.ref, Nn);
   DA(S.nn, Nn);
   DA(S.cell_of, Nn); DA(S.rank, Nn); DA(S.perm, Nn);
@@ -706,6 +712,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.cell_start, cell_off + 1);
   DA(S.scan_blk, 2 * 256);  // the cell-start scan's block sums and offsets
   DA(S.rebuild_flag, 1 + n_rep);
+  DA(S.steps_alt, 1);
+  S.sync_alt = 0;
   DA(S.pair_q, 2);
   DA(S.wl_rep, n_rep + 1);
   DA(S.wl_p, n_rep + 1);
@@ -772,6 +780,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaMemsetAsync(S.rep_rebuilds, 0, sizeof(long long) * n_rep, st));
   CK(cudaMemsetAsync(S.status, 0, 2 * sizeof(unsigned), st));
   CK(cudaMemsetAsync(S.steps_done, 0, sizeof(long long), st));
+  CK(cudaMemsetAsync(S.steps_alt, 0, sizeof(long long), st));
   CK(cudaMemsetAsync(S.rebuilds, 0, sizeof(long long), st));
   CK(cudaMemsetAsync(ctx->acc_step, 0, sizeof(double) * NOBS * n_rep, st));
   CK(cudaMemsetAsync(ctx->acc_call, 0, sizeof(double) * NOBS * n_rep, st));
@@ -802,6 +811,11 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
     int r = setup_kspace(ctx, a_type);
     if (r != MFA_OK) return r;
   }
+  if (ctx->opt.separate_integrator < 0 || ctx->opt.separate_integrator > 1)
+    return fail(ctx, MFA_ERR_ARG, "separate_integrator must be 0 or 1");
+  // the integration fused into the pair kernel: mixed precision, no k-space (its forces come after
+  // the pair kernel's), one block per tile
+  ctx->fuse_integ = S.mixed && !ctx->kspace && !ctx->opt.separate_integrator && !S.pair_persist;
   // ---- initial sort + list, then size the list from the observed maximum ------------------------
   rebuild(ctx, true);
   RET(post_status(ctx));
@@ -1103,19 +1117,43 @@ static int prepare_step(mfa_ctx* ctx) {
 
 // obs: the energy records also go into the observation averages (Rg^2 and momentum of the state
 // of the record's step, so those steps run the velocity and position halves as two kernels).
+// The context's state with the two view buffer sets (and step counters) exchanged.
+static DevState other_views(const DevState& S) {
+  DevState T = S;
+  std::swap(T.pfx, T.pfx_alt);
+  std::swap(T.vf, T.vf_alt);
+  std::swap(T.steps_done, T.steps_alt);
+  return T;
+}
+
+// n steps of the fused path (mfa_step).  With ctx->fuse_integ, a step without an energy record,
+// profile or observation, other than the last, runs its integration in the pair kernel's tail,
+// which writes the next step's views into the other buffer set: the sets alternate on each such
+// step.  The chunk starts in the set that makes it end in the context's own (ctx->S): the first
+// position update then copies the wall beads' views and the step counter across.
 static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs, bool capturing, int* err) {
-  const DevState& S = ctx->S;
   const SimConst& C = ctx->C;
   cudaStream_t st = ctx->st;
   Acc acc = acc_of(ctx->acc_step, ctx->nrep);
   const int mask = any_chains(ctx) ? bonded_mask(ctx) : 0;
   long long L = 0;
-  launch_integrate(S, C, st, 0, false, false, acc);
-  L += 1;
+  auto energies_at = [&](int k) { return ((phase + k) % ctx->opt.energy_every == 0) || k == n; };
+  auto fused_at = [&](int k) { return ctx->fuse_integ && k < n && !energies_at(k) && !prof; };
+  int n_fused = 0;
+  for (int k = 1; k <= n; ++k) n_fused += fused_at(k) ? 1 : 0;
+  const DevState sets[2] = {ctx->S, other_views(ctx->S)};
+  int cur = n_fused & 1;
+  {
+    DevState S0 = sets[cur];
+    S0.sync_alt = cur;
+    launch_integrate(S0, C, st, 0, false, false, acc);
+    L += 1;
+  }
   for (int k = 1; k <= n; ++k) {
-    const bool ef = ((phase + k) % ctx->opt.energy_every == 0) || k == n;
+    const DevState& S = sets[cur];
+    const bool ef = energies_at(k);
     if (capturing) {
-      int r = capture_conditional_rebuild(ctx);
+      int r = capture_conditional_rebuild(ctx, S);
       if (r != MFA_OK) {
         *err = r;
         return L;
@@ -1124,6 +1162,12 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs
     } else {
       launch_rebuild(S, st, false);
       L += kRebuildLaunches;
+    }
+    if (fused_at(k)) {  // forces and this step's integration in one kernel; the views move across
+      launch_pair(S, C, st, false, false, acc, ctx->opt.block_size, mask, true);
+      L += 1;
+      cur ^= 1;
+      continue;
     }
     // mixed: bonded terms inside the pair kernel; FP64: their own kernel
     launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
@@ -1618,24 +1662,40 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
     fam.push_back(f);
   };
   // the first position update belongs to the "positions" family; each step then runs
-  // rebuild, pair, bonded, kspace and the fused velocity+position kernel
+  // rebuild, pair, bonded, kspace and the fused velocity+position kernel, as mfa_step runs them:
+  // with ctx->fuse_integ the steps before the last (the energy step) integrate in the pair
+  // kernel's tail, whose time then counts as "pair"
+  const int n_fused = ctx->fuse_integ ? nsteps - 1 : 0;
+  const DevState sets[2] = {S, other_views(S)};
+  int cur = n_fused & 1;
   mark(-1);
-  launch_integrate(S, C, st, 0, false, false, acc);
+  {
+    DevState S0 = sets[cur];
+    S0.sync_alt = cur;
+    launch_integrate(S0, C, st, 0, false, false, acc);
+  }
   mark(7);
   for (int k = 1; k <= nsteps; ++k) {
     const bool ef = (k == nsteps);
+    const DevState& Sk = sets[cur];
     // the rebuild as the fused step runs it: the replicas whose skin test fired, if any
-    launch_rebuild(S, st, false);
+    launch_rebuild(Sk, st, false);
     mark(0);
-    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
+    if (ctx->fuse_integ && !ef) {
+      launch_pair(Sk, C, st, false, false, acc, ctx->opt.block_size, mask, true);
+      mark(1);
+      cur ^= 1;
+      continue;
+    }
+    launch_pair(Sk, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
     mark(1);
-    if (mask && !S.mixed) { launch_bonded(S, C, st, mask, ef, acc, true); mark(2); }
+    if (mask && !S.mixed) { launch_bonded(Sk, C, st, mask, ef, acc, true); mark(2); }
     if (ctx->kspace) {
-      launch_kspace(S, C, ctx->K, st, ef, acc, true);
-      launch_dipolar(S, C, ctx->K, st, ef, acc, true);
+      launch_kspace(Sk, C, ctx->K, st, ef, acc, true);
+      launch_dipolar(Sk, C, ctx->K, st, ef, acc, true);
       mark(4);
     }
-    launch_integrate(S, C, st, k < nsteps ? 2 : 1, true, ef, acc);
+    launch_integrate(Sk, C, st, k < nsteps ? 2 : 1, true, ef, acc);
     mark(3);
     if (ef) { launch_record(acc, ctx->rec, st); mark(6); }
   }

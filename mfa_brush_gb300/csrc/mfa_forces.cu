@@ -22,7 +22,7 @@
 // k_cforce : constant_force.f90:17-21 (Poiseuille body force m*g on every non-head bead).
 #include <type_traits>
 
-#include "mfa_state.cuh"
+#include "mfa_integ.cuh"
 
 namespace mfa {
 
@@ -363,9 +363,12 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
 }
 
 // kept pairs per batch (a thread screens its list until it has this many, then they are evaluated),
-// and list entries screened per group (their loads are all in flight at once)
+// and list entries screened per group (their loads are all in flight at once).  Measured on 256
+// brush replicas (4.66 M particles, skin 0.5): groups of 2 / 3 / 4 / 8 entries gave a pair kernel
+// of 0.574 / 0.582 / 0.583 / 0.648 ms with the evaluation loop not unrolled, batches of 12 / 16 /
+// 20 kept pairs the same within 0.1 %; unrolling the evaluation loop by 2 or 4 cost 4 % or 20 %.
 constexpr int PAIR_BATCH = 16;
-constexpr int PAIR_G = 4;
+constexpr int PAIR_G = 2;
 
 // Force factor fs of the pair (i, j) along d = r_i - r_j (LJ with the switch-on clamp, DPD with the
 // pair's Philox noise, real-space Coulomb), fluid_fluid.f90:97-261, dpd_forces.f90:45-115,
@@ -460,16 +463,23 @@ __device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimCon
 // Without FUSED the forces are added to (accumulate) or stored in the FP64 force arrays.
 // Virial (EFLAG): each visit of a pair adds half of F_ij (x) (r_i - r_j) (the other visit adds the
 // other half); a pair with a fixed wall bead, which has no list of its own, counts in full.
+//   INTEG   (FUSED, without EFLAG) the step's integration in the tail: each thread takes its
+//           particle's force and runs the integrator's update (int_mixed_particle, MODE 2) on it,
+//           writing the next step's views to the other view buffers (pfx_alt, vf_alt) while the
+//           neighbours still read pfx and vf; wall beads copy their views across, and the step
+//           counter of the other set is this one's plus one.  No force array is written.
 //   PERSIST (FUSED only) a grid of the blocks that fit on the GPU at once; each block takes tiles
 //           of blockDim.x particles from a queue (s.pair_q[0], one atomic ticket per tile, no
 //           waiting) and the last block to finish resets the queue for the next launch.  Compiled
 //           for 8 resident blocks per SM (64 registers): at 9 the tile loop spills.
-template <bool MIXED, bool EFLAG, bool FUSED = false, bool BONDED = false, bool UNI = false, bool PERSIST = false>
+template <bool MIXED, bool EFLAG, bool FUSED = false, bool BONDED = false, bool UNI = false, bool PERSIST = false,
+          bool INTEG = false>
 __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(DevState s, SimConst C, bool accumulate,
                                                                              Acc acc, int bmask = 0) {
   using real = real_t<MIXED>;
   static_assert(!FUSED || MIXED, "the fused form is the mixed-precision one");
   static_assert(!BONDED || FUSED, "bonded terms are fused only into the fused form");
+  static_assert(!INTEG || (FUSED && !EFLAG && !PERSIST), "the integration is fused into the plain fused form");
   __shared__ PairEntry<real> tab[NPAIR];
   // FUSED: the particle's FP64 total, in shared memory while the pair loop runs (registers are
   // scarce there; it is touched once per batch)
@@ -620,7 +630,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
         ++k;
         if (screen(j)) jl[m++] = j;
       }
-#pragma unroll 2
+#pragma unroll 1
       for (int t = 0; t < m; ++t) {
         const int j = jl[t];
         real dx, dy, dz;
@@ -672,7 +682,17 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
     }
   }
   if (inside) {
-    if constexpr (FUSED) {
+    if constexpr (INTEG) {
+      if (active) {
+        float ke, kin[6], fh[6];
+        int_mixed_particle<2, false>(s, C, i, w, d2f_fast(fxd), d2f_fast(fyd), d2f_fast(fzd), s.pfx_alt, s.vf_alt, ke,
+                                     kin, fh);
+      } else {  // a wall bead: its views as they are
+        s.pfx_alt[i] = s.pfx[i];
+        s.vf_alt[i] = s.vf[i];
+      }
+      if (i == 0) *s.steps_alt = *s.steps_done + 1;
+    } else if constexpr (FUSED) {
       s.f4[i] = make_float4(d2f_fast(fxd), d2f_fast(fyd), d2f_fast(fzd), 0.f);
     } else if (accumulate) {
       if (active) {
@@ -713,7 +733,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
 }
 
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag, Acc acc,
-                 int block, int bonded_mask) {
+                 int block, int bonded_mask, bool integ) {
   // 32, 64 or 128 threads per block (the kernel is compiled for at most 128); anything else
   // takes the built-in 128
   const int B = (block == 32 || block == 64) ? block : 128;
@@ -729,8 +749,15 @@ void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool acc
     // the persistent schedule for the steps without energies: [bonded][uni]
     const KernT kp[2][2] = {{k_pair<true, false, true, false, false, true>, k_pair<true, false, true, false, true, true>},
                             {k_pair<true, false, true, true, false, true>, k_pair<true, false, true, true, true, true>}};
+    // with the step's integration in the tail: [bonded][uni]
+    const KernT ki[2][2] = {{k_pair<true, false, true, false, false, false, true>,
+                             k_pair<true, false, true, false, true, false, true>},
+                            {k_pair<true, false, true, true, false, false, true>,
+                             k_pair<true, false, true, true, true, false, true>}};
     const int bi = bonded_mask ? 1 : 0, ui = uni ? 1 : 0;
-    if (s.pair_persist && !eflag) {
+    if (integ) {
+      ki[bi][ui]<<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
+    } else if (s.pair_persist && !eflag) {
       const KernT k = kp[bi][ui];
       int per_sm = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, B, 0);

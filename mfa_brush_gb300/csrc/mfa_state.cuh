@@ -22,6 +22,14 @@ struct DevState {
   // pair-kernel views
   int4* pfx;
   float4* vf;
+  // the other view buffers of the mixed path: a pair kernel with the step's integration fused in
+  // writes the next step's views there while its neighbours still read pfx and vf; the step
+  // counter has a copy per buffer set for the same reason
+  int4* pfx_alt;
+  float4* vf_alt;
+  long long* steps_alt;
+  int sync_alt;  // 1: the position update that starts a chunk also copies the wall beads' views and
+                 // the step counter from the other set into this one
   dbl4* pd;
   dbl4* vd;
   int4* ref;   // fixed-point position at the last rebuild
@@ -144,8 +152,10 @@ constexpr int NL_CAP_MAX = 420;
 // pair forces (fluid_fluid); accumulate = add into f, else overwrite; eflag = energies into acc;
 // bonded_mask != 0 in the fused mixed step (overwrite into f4) adds the bonded terms in the same
 // kernel (the caller then skips launch_bonded)
+// integ (the fused mixed step without energies, one block per tile): the step's integration in the
+// pair kernel's tail, views to the other buffer set (k_pair's INTEG)
 void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool accumulate, bool eflag,
-                 Acc acc, int block, int bonded_mask = 0);
+                 Acc acc, int block, int bonded_mask = 0, bool integ = false);
 // bonded terms: mask bit 1 FENE, 2 brush bending, 4 melt bending, 8 orientation
 void launch_bonded(const DevState& s, const SimConst& C, cudaStream_t st, int mask, bool eflag, Acc acc,
                    bool fused = false);

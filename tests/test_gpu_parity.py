@@ -423,6 +423,37 @@ def test_persistent_pair_schedule_does_not_change_the_trajectory(gpu):
             assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("setup", ["brush", "melt"])
+def test_fused_integration_does_not_change_the_trajectory(gpu, setup):
+    """The mixed mfa_step runs the integration of its plain steps in the pair kernel's tail, with
+    the views written to the other buffer set (options.separate_integrator 0, the default); with
+    a separate integrator kernel (1) the state is the same bit for bit: over calls of 7, 13 and 10
+    steps (odd and even numbers of fused steps, rebuilds included), then a drop-in pair force
+    evaluation on the views that the calls left."""
+    if setup == "brush":
+        p = configs.wca_params(gamma=5.0)
+        systems, a_type, r0, v = configs.concat(configs.replicas(4, seed=9))
+    else:
+        p, (systems, a_type, r0, v) = configs.melt_brush(L=14.0, D=24.0)
+    out = []
+    for sep in (False, True):
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", separate_integrator=sep)
+        states = []
+        for n in (7, 13, 10):
+            g.step(n)
+            states.append(g.state())
+        g.zero_force()
+        e = g.fluid_fluid()[0]
+        out.append((states, g.state()[3], e, g.step_index()))
+        g.close()
+    (s0, f0, e0, k0), (s1, f1, e1, k1) = out
+    assert k0 == k1
+    for a, b in zip(s0, s1):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+    assert np.array_equal(f0, f1) and np.array_equal(e0, e1)
+
+
 def test_measurement_aids(gpu):
     """mfa_fp32_fma_peak measures a plausible FP32 FMA throughput (a GB300 has 152 SMs x 128 lanes
     x 2 FLOP x ~2 GHz = ~80 TFLOP/s nominal); mfa_kspace_info gives the k-set and charge counts of
