@@ -37,6 +37,10 @@ CHUNK = 10
 # velocity in, float4 force out; fp64 -- double4 position and velocity in, three doubles out (the
 # neighbour list itself, 4 B per entry, is not counted)
 PAIR_BYTES = {"mixed": 16 + 16 + 16, "fp64": 32 + 32 + 24}
+# the mixed pair kernel with the step's integration in its tail: position and velocity views in
+# (16 + 16), info and tag (4 + 4), the FP64 position and velocity in and out (48 + 48), the
+# rebuild reference position (16), the next step's views out (16 + 16)
+PAIR_INTEG_BYTES = 16 + 16 + 4 + 4 + 48 + 48 + 16 + 16 + 16
 
 
 def profiled_traffic(precision, n_atoms, skin):
@@ -342,6 +346,8 @@ def main():
                     help="threads per block of the pair kernel (32, 64, 128); tuned with --skin auto")
     ap.add_argument("--list-cells", type=int, default=0,
                     help="list-build cells per list cut-off (1, 2, 3; 0 = the library's choice)")
+    ap.add_argument("--separate-integrator", action="store_true",
+                    help="a separate integrator kernel on every step (default: fused into the pair kernel)")
     ap.add_argument("--pair-schedule", type=int, default=0,
                     help="pair kernel schedule: 0 one block per tile, 1 persistent blocks over a tile queue")
     ap.add_argument("--skin", default="auto",
@@ -407,7 +413,8 @@ def main():
         args.pair_schedule = sch
     args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin,
-                    block_size=args.block, list_cells=args.list_cells, pair_schedule=args.pair_schedule)
+                    block_size=args.block, list_cells=args.list_cells, pair_schedule=args.pair_schedule,
+                    separate_integrator=args.separate_integrator)
 
     def barrier():
         if dist is not None:
@@ -451,7 +458,13 @@ def main():
     kt = g.kernel_times(args.kernel_steps)
     hbm, peak_kind = peaks()
     t_pair = kt["pair"][0] / 1000.0
-    achieved = PAIR_BYTES[args.precision] * n_atoms / t_pair / 1e9 if t_pair > 0 else 0.0
+    # kernel_times runs its steps as mfa_step does: with the integration fused, every step but the
+    # last (the energy step) runs the pair kernel with the integration in its tail
+    fused = args.precision == "mixed" and not args.separate_integrator and args.pair_schedule == 0
+    n_fused = args.kernel_steps - 1 if fused else 0
+    pair_bytes = (n_fused * PAIR_INTEG_BYTES + (args.kernel_steps - n_fused) * PAIR_BYTES[args.precision]) \
+        / args.kernel_steps
+    achieved = pair_bytes * n_atoms / t_pair / 1e9 if t_pair > 0 else 0.0
     traffic, traffic_skin = profiled_traffic(args.precision, n_atoms, args.skin)
 
     # end-to-end through the C ABI with pinned host buffers
@@ -470,6 +483,7 @@ def main():
                        "particles_total": n_all, "seed": args.seed,
                        "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
                        "pair_block": args.block, "list_cells": g.list_cells(), "pair_schedule": args.pair_schedule,
+                       "integration": "fused into the pair kernel" if fused else "separate kernel",
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
@@ -483,7 +497,9 @@ def main():
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,
-                         "kernel": "k_pair (%s)" % args.precision,
+                         "kernel": "k_pair (%s%s): %.0f B per particle per launch, averaged over the "
+                                   "%d timed launches" % (args.precision, ", integration fused" if fused else "",
+                                                          pair_bytes, args.kernel_steps),
                          "traffic_source": "ncu DRAM bytes per particle of one full launch at skin %s "
                                            "(profiles/k_pair_%s_brush_replicas.md), times N"
                                            % (traffic_skin, args.precision),
