@@ -243,7 +243,8 @@ def run_single(args):
         p, (s, a_type, r0, v) = configs.two_liquid_large()
     skin = 0.5 if args.skin == "auto" else float(args.skin)
     prof = {"profile_from_step": 0} if args.workload == "two-liquid" else {}
-    g = md.MdSystem(p, s, a_type, r0, v, precision=args.precision, skin=skin, **prof)
+    g = md.MdSystem(p, s, a_type, r0, v, precision=args.precision, skin=skin,
+                    separate_integrator=args.separate_integrator, **prof)
     done = 0
     while done < args.warmup:
         g.step(CHUNK)
@@ -279,11 +280,19 @@ def run_single(args):
         else:
             fam, flop, what = None, 0.0, ""
         if fam is None and kt.get("pair", (0, 0))[1]:
-            # as for the batched replicas: 48 B per particle against the measured copy bandwidth
+            # as for the batched replicas: the algorithmic bytes of the timed pair launches (with
+            # the integration in the tail on every kernel_times step but the last) against the
+            # measured copy bandwidth
             hbm, peak_kind = peaks()
-            achieved = PAIR_BYTES[args.precision] * n / (kt["pair"][0] / 1000.0) / 1e9
+            fused = args.precision == "mixed" and not args.separate_integrator
+            n_fused = args.kernel_steps - 1 if fused else 0
+            pb = (n_fused * PAIR_INTEG_BYTES + (args.kernel_steps - n_fused) * PAIR_BYTES[args.precision]) \
+                / args.kernel_steps
+            achieved = pb * n / (kt["pair"][0] / 1000.0) / 1e9
             roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                    "traffic": None, "kernel": "k_pair (%s)" % args.precision, "peak_kind": peak_kind}
+                    "traffic": None, "peak_kind": peak_kind,
+                    "kernel": "k_pair (%s%s): %.0f B per particle per launch, averaged over the %d timed launches"
+                              % (args.precision, ", integration fused" if fused else "", pb, args.kernel_steps)}
         elif fam and kt.get(fam, (0, 0))[1]:
             achieved = flop / (kt[fam][0] / 1000.0) / 1e12
             roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
