@@ -33,6 +33,10 @@ sys.path.insert(0, ROOT)
 METRIC = "atom-steps/s on 1 GB300: batched FP32-force vs plain FP64 (force rel err<=1e-5)"
 UNIT = "atom-steps/s"
 CHUNK = 10
+# steps per mfa_step call of the timed loop of the batched replicas: one graph of 100 steps, with
+# the energy record every 10 steps kept on the device (the fort.60/61 series ring); the e2e leg
+# keeps 10-step calls with a host round trip of the state after each
+STEP_CALL = 100
 # algorithmic bytes per particle of the pair kernel: mixed -- int4 fixed-point position and float4
 # velocity in, float4 force out; fp64 -- double4 position and velocity in, three doubles out (the
 # neighbour list itself, 4 B per entry, is not counted)
@@ -364,6 +368,10 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps = max(CHUNK, (args.steps // CHUNK) * CHUNK)
+    # the batched replicas run calls of STEP_CALL steps when the timed steps are a multiple of it,
+    # else calls of CHUNK; the warm-up is a whole number of calls (and captures the call's graph)
+    args.call = STEP_CALL if args.steps % STEP_CALL == 0 else CHUNK
+    args.warmup = -(-args.warmup // args.call) * args.call
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -404,8 +412,9 @@ def main():
         # are hotter and rebuild more often)
         best, rates = tune.tune_skin(p, reps, candidates=(0.3, 0.4, 0.5, 0.6, 0.7, 0.8), n_sample=len(reps),
                                      steps=100, warmup=args.warmup, precision=args.precision, device=local,
-                                     list_cells=args.list_cells)
-        kw = dict(n_sample=len(reps), steps=100, warmup=args.warmup, precision=args.precision, device=local)
+                                     chunk=100, list_cells=args.list_cells)
+        kw = dict(n_sample=len(reps), steps=100, warmup=args.warmup, precision=args.precision, device=local,
+                  chunk=100)
         lc, lrates = tune.tune_option(p, reps, best, "list_cells", (1, 2, 3), **kw)
         blk, brates = tune.tune_block(p, reps, best, list_cells=lc, **kw)
         sch, srates = tune.tune_option(p, reps, best, "pair_schedule", (0, 1), list_cells=lc, block_size=blk, **kw)
@@ -423,17 +432,17 @@ def main():
     args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin,
                     block_size=args.block, list_cells=args.list_cells, pair_schedule=args.pair_schedule,
-                    separate_integrator=args.separate_integrator)
+                    separate_integrator=args.separate_integrator, series_capacity=2 * STEP_CALL // CHUNK)
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    # warm-up (also captures the 10-step graph)
+    # warm-up (also captures the step graph)
     done = 0
     while done < args.warmup:
-        g.step(CHUNK)
-        done += CHUNK
+        g.step(args.call)
+        done += args.call
     g.synchronize()
     barrier()
     clk = ClockSampler(local)
@@ -443,8 +452,8 @@ def main():
     l0 = g.launch_count()
     g.synchronize()
     g.event_record(0)
-    for _ in range(args.steps // CHUNK):
-        g.step(CHUNK)
+    for _ in range(args.steps // args.call):
+        g.step(args.call)
     g.event_record(1)
     ms = g.event_elapsed(0, 1)
     g.synchronize()
@@ -490,7 +499,9 @@ def main():
             "config": {"workload": "256 uneven brush-channel replicas, WCA+FENE+DPD, batched",
                        "replicas": args.replicas * world, "particles_per_gpu": n_atoms,
                        "particles_total": n_all, "seed": args.seed,
-                       "precision": args.precision, "chunk_steps": CHUNK, "skin": args.skin,
+                       "precision": args.precision, "steps_per_call": args.call,
+                       "energy_record": "every %d steps on the device, kept in the energy-series ring" % CHUNK,
+                       "skin": args.skin,
                        "pair_block": args.block, "list_cells": g.list_cells(), "pair_schedule": args.pair_schedule,
                        "integration": "fused into the pair kernel" if fused else "separate kernel",
                        "skin_autotune": tuned,
