@@ -171,19 +171,21 @@ def config1_cpu(steps_all, steps_one):
             "kind": "port"}
 
 
-def plain_fp64(reps, p, skin, device, every=16, steps=100, warmup=20):
+def plain_fp64(reps, p, skin, device, every=16, steps=100, warmup=20, call=CHUNK):
     """The plain FP64 step on replicas run one at a time (every `every`-th replica of the set):
-    atom-steps/s over the sample, each replica timed with CUDA events on its own stream."""
+    atom-steps/s over the sample, each replica timed with CUDA events on its own stream, in
+    mfa_step calls of `call` steps."""
     from mfa_brush_gb300 import md
     tot_n, tot_t, picked = 0, 0.0, 0
+    warmup = max(call, warmup)
     for (s, a_type, r0, v) in reps[::every]:
         g = md.MdSystem(p, s, a_type, r0, v, precision="fp64", device=device, skin=skin)
-        for _ in range(warmup // CHUNK):
-            g.step(CHUNK)
+        for _ in range(warmup // call):
+            g.step(call)
         g.synchronize()
         g.event_record(0)
-        for _ in range(steps // CHUNK):
-            g.step(CHUNK)
+        for _ in range(steps // call):
+            g.step(call)
         g.event_record(1)
         tot_t += g.event_elapsed(0, 1) / 1000.0
         tot_n += s.n_part * steps
@@ -530,24 +532,25 @@ def main():
     if rank == 0 and not args.no_fp64:
         # the reference point of the batched mixed step: the same kind of replicas advanced one at
         # a time in plain FP64
-        fv, fk, fn = plain_fp64(reps, p, args.skin, local)
+        fv, fk, fn = plain_fp64(reps, p, args.skin, local, call=args.call)
         line["plain_fp64_one_at_a_time"] = {
             "value": fv, "unit": UNIT, "replicas": fk, "particles": int(fn), "steps": 100,
-            "sample": "every 16th replica of the set, each alone in its own FP64 context, 10-step graphs",
+            "sample": "every 16th replica of the set, each alone in its own FP64 context, %d-step graphs" % args.call,
             "speedup_of_value": value / world / fv}
         # the same batch in the plain FP64 mode (precision alone, batching held fixed)
         gd = md.MdSystem(p, systems, a_type, r0, v, precision="fp64", device=local, skin=args.skin,
                          list_cells=args.list_cells)
-        for _ in range(2):
-            gd.step(CHUNK)
+        nb = max(1, 100 // args.call)  # 100 steps in the timed loop's calls
+        for _ in range(max(1, 20 // args.call)):
+            gd.step(args.call)
         gd.synchronize()
         gd.event_record(0)
-        for _ in range(10):
-            gd.step(CHUNK)
+        for _ in range(nb):
+            gd.step(args.call)
         gd.event_record(1)
-        bv = n_atoms * 10 * CHUNK / (gd.event_elapsed(0, 1) / 1000.0)
+        bv = n_atoms * nb * args.call / (gd.event_elapsed(0, 1) / 1000.0)
         gd.close()
-        line["batched_fp64"] = {"value": bv, "unit": UNIT, "steps": 10 * CHUNK,
+        line["batched_fp64"] = {"value": bv, "unit": UNIT, "steps": nb * args.call, "steps_per_call": args.call,
                                 "speedup_of_value": value / world / bv}
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
