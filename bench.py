@@ -312,7 +312,7 @@ def run_single(args):
                        "chunk_steps": CHUNK, "skin": skin,
                        "l2_flush": ("inputs larger than L2" if n * 96 > 129e6
                                     else "none: the working set fits in L2")},
-            "gpu_launches": int(launches + 12 * rebuilds),
+            "gpu_launches": int(launches + 11 * rebuilds),
             "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "kernel_ms": {k: round(v_[0], 5) for k, v_ in kt.items() if v_[1]},
             "roofline": roof,
@@ -509,7 +509,7 @@ def main():
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",
                        "parallelism": "replicas" if world == 1 else "replicas x %d GPUs" % world},
-            "gpu_launches": int(launches + 12 * rebuilds),
+            "gpu_launches": int(launches + 11 * rebuilds),
             "rebuilds_per_100_steps": 100.0 * rebuilds / args.steps,
             "replica_rebuilds_per_100_steps": {
                 "mean": float(rep_rb.mean()), "min": float(rep_rb.min()), "max": float(rep_rb.max()),

@@ -159,13 +159,13 @@ __global__ void k_clear_overflow(unsigned* status) {
 }
 
 // rebuild of the flagged replicas (all of them when forced); counts and clears the flags
-constexpr int kRebuildLaunches = 12;
+constexpr int kRebuildLaunches = 11;
 void rebuild(mfa_ctx* ctx, bool force) {
   launch_rebuild(ctx->S, ctx->st, force);
   ctx->launches += kRebuildLaunches;
 }
 
-// Graph form of the skin check: the IF body (the twelve rebuild kernels) runs only on steps whose
+// Graph form of the skin check: the IF body (the eleven rebuild kernels) runs only on steps whose
 // position update raised the flag of some replica; other steps launch nothing.
 __global__ void k_cond_rebuild(const int* flag, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, flag[0] ? 1u : 0u);
@@ -708,7 +708,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.nn, Nn);
   DA(S.cell_of, Nn); DA(S.rank, Nn); DA(S.perm, Nn);
   S.ncell_tot = cell_off;
-  DA(S.cell_count, cell_off + 1);
+  DA(S.cell_count, cell_off + 1);  // zero between rebuilds: k_bin counts up, k_sort_cells zeroes
   DA(S.cell_start, cell_off + 1);
   DA(S.scan_blk, 2 * 256);  // the cell-start scan's block sums and offsets
   DA(S.rebuild_flag, 1 + n_rep);
@@ -770,6 +770,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   CK(cudaMemcpyAsync(S.tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(S.slot_of_tag, iota.data(), sizeof(int) * ctx->N, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(S.rebuild_flag, 0, sizeof(int) * (1 + n_rep), st));
+  CK(cudaMemsetAsync(S.cell_count, 0, sizeof(int) * (cell_off + 1), st));
   CK(cudaMemsetAsync(S.pair_q, 0, sizeof(int) * 2, st));
   {
     std::vector<int> cr(std::max(cell_off, 1));

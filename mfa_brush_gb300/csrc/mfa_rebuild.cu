@@ -149,16 +149,6 @@ __device__ __forceinline__ int wl_map_warp(const int* __restrict__ pre, const in
   const int wl_tot_ = s.pre[wl_cnt_];                                                              \
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < wl_tot_; g += gridDim.x * blockDim.x)
 
-// counts of the listed replicas' cells to zero; the other replicas keep the counts of their last
-// rebuild, which still describe their slots (the entry past the last cell stays zero)
-__global__ void k_zero_counts(DevState s) {
-  WL_FOR(wl_c, g) {
-    int r, c;
-    wl_map_warp(s.wl_c, s.wl_rep, wl_cnt_, g, r, c);
-    s.cell_count[s.reps[r].cell_off + c] = 0;
-  }
-}
-
 __global__ void k_bin(DevState s) {
   WL_FOR(wl_p, g) {
   int rr, loc;
@@ -335,6 +325,7 @@ __global__ void k_sort_cells(DevState s) {
   wl_map_warp(s.wl_c, s.wl_rep, wl_cnt_, g, r, lc);
   const int c = s.reps[r].cell_off + lc;
   int b = s.cell_start[c], n = s.cell_count[c];
+  s.cell_count[c] = 0;  // the last reader of the count: zero again for the next rebuild's k_bin
   for (int k = 1; k < n; ++k) {  // insertion sort by tag
     int p = s.perm[b + k];
     int t = s.tag[p];
@@ -615,7 +606,6 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   const int gN = std::min((s.N + B - 1) / B, s.nsm * 8);
   const int gC = std::min((s.ncell_tot + B - 1) / B, s.nsm * 8);
   k_worklist<<<1, WL_THREADS, 0, st>>>(s, force);
-  k_zero_counts<<<gC, B, 0, st>>>(s);
   k_bin<<<gN, B, 0, st>>>(s);
   k_wscan_sum<<<SCAN_BLOCKS, SCAN_T, 0, st>>>(s);
   k_wscan_blocks<<<1, SCAN_T, 0, st>>>(s);
