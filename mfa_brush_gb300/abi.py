@@ -70,7 +70,7 @@ class Params(C.Structure):
                 ("bend_form", i32), ("const_force", f64 * 3), ("charge", f64 * MAXT),
                 ("alpha_c", f64), ("sqrt_alpha", f64), ("inv_sqrt_pi", f64), ("n_kmax", i32),
                 ("rc_coul_2", f64), ("skin", f64), ("r_2_min_init", f64), ("r_2_min_time", f64),
-                ("compat", u32), ("hist_dim", i32)]
+                ("compat", u32), ("hist_dim", i32), ("va_wall", f64 * 2)]
 
     def table(self, name):
         """n_type x n_type numpy copy of a row-major MAXT x MAXT table."""

@@ -464,6 +464,8 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   C.charged = charged;
   C.wall = F.wall;
   C.dt = p->dt;
+  C.va_wall[0] = p->va_wall[0];
+  C.va_wall[1] = p->va_wall[1];
   C.half_dt = 0.5 * p->dt;
   C.half_dt2 = 0.5 * (p->dt * p->dt);
   for (int t = 0; t < MAXT; ++t) {

@@ -419,8 +419,14 @@ int mfa_derive_params(const mfa_inputs* in, mfa_params* p, mfa_system* s) {
   p->rc_coul_2 = (in->compat & MFA_COMPAT_COUL_IN_LJ) ? 0. : in->rc_coul * in->rc_coul;
   p->compat = in->compat;
   p->hist_dim = in->hist_dim > 0 ? in->hist_dim : 200;
-  if (!F.poiseuille && (in->va_spring_twall[0] != 0. || in->va_spring_twall[1] != 0.))
-    return MFA_ERR_UNSUPPORTED;  // moving-wall heads (Couette) are not built
+  if (in->va_spring_twall[0] != 0. || in->va_spring_twall[1] != 0. || in->va_spring_twall[2] != 0.) {
+    // init_params.f90:899-907: moving walls with the body force is an inconsistency the reference
+    // stops on; with explicit walls the wall sites would move too (verlet_positions.f90:214-221),
+    // which is not built
+    if (F.poiseuille || F.wall == 1) return MFA_ERR_UNSUPPORTED;
+    p->va_wall[0] = in->va_spring_twall[0];
+    p->va_wall[1] = in->va_spring_twall[1];
+  }
   s->boundary[0] = in->x_space * (double)in->n_cell_w_x;
   s->boundary[1] = in->y_space * (double)in->n_cell_w_y;
   s->boundary[2] = in->z_space_wall;

@@ -34,11 +34,16 @@ __device__ __forceinline__ void int_mixed_particle(const DevState& s, const SimC
       const float im = C.inv_mass_f[t];
       ax = Fx * im; ay = Fy * im; az = Fz * im;
       if (info_head(w)) {
+        const bool first = (s.tag[i] - R.p0) / R.n_mon < R.n_chain / 2;
         if (EFLAG) {  // f_on_heads before the heads are held (verlet_velocities.f90:18)
-          const int h = (s.tag[i] - R.p0) / R.n_mon < R.n_chain / 2 ? 0 : 3;
+          const int h = first ? 0 : 3;
           fh[h] = -Fx; fh[h + 1] = -Fy; fh[h + 2] = -Fz;
         }
-        vx = vy = vz = 0.;
+        // verlet_velocities.f90:111-124: the heads move with their wall (+-va_wall in x, y)
+        const double sg = first ? 1. : -1.;
+        vx = sg * C.va_wall[0];
+        vy = sg * C.va_wall[1];
+        vz = 0.;
         ax = ay = az = 0.f;
         Fx = Fy = Fz = 0.f;
       }

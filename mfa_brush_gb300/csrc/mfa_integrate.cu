@@ -4,9 +4,10 @@
 //   MODE 0  verlet_positions.f90:150-209: r += dt v + dt^2/2 a, x,y wrapped into [0,L),
 //           v += dt/2 a; then the pair-kernel views and the skin test (displacement since the
 //           last rebuild > skin/2 raises the rebuild flag; check_skin.f90:11-24).
-//   MODE 1  verlet_velocities.f90:25-153: a = F/m, v += dt/2 a, brush heads held fixed
-//           (v = a = F = 0, the POISEUILLE branch :113-120; without POISEUILLE the implicit-wall
-//           heads move with va_spring_twall, which must be 0 here), kinetic energy.
+//   MODE 1  verlet_velocities.f90:25-153: a = F/m, v += dt/2 a, brush heads driven: a = F = 0
+//           and v = (+-va_wall, 0) for the chains of the first / second half (:111-124, the two
+//           brushes sheared against each other; va_wall = 0 without shear and always with
+//           POISEUILLE, :113-120), kinetic energy.
 //   MODE 2  MODE 1 of step n followed by MODE 0 of step n+1 in one pass (the fused step): one
 //           read of r, v, F and one write of r, v and the views per particle per step.
 //   add_ext adds the 9-3 wall force (fluid_wall.f90:96-121) and the body force
@@ -73,11 +74,16 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       vy = vy + C.half_dt * ay;
       vz = vz + C.half_dt * az;
       if (info_head(w)) {
+        const bool first = (s.tag[i] - R.p0) / R.n_mon < R.n_chain / 2;
         if (EFLAG) {  // f_on_heads before the heads are held (verlet_velocities.f90:18)
-          const int h = (s.tag[i] - R.p0) / R.n_mon < R.n_chain / 2 ? 0 : 3;
+          const int h = first ? 0 : 3;
           fh[h] = -Fx; fh[h + 1] = -Fy; fh[h + 2] = -Fz;
         }
-        vx = vy = vz = 0.;
+        // verlet_velocities.f90:111-124: the heads move with their wall (+-va_wall in x, y)
+        const double sg = first ? 1. : -1.;
+        vx = sg * C.va_wall[0];
+        vy = sg * C.va_wall[1];
+        vz = 0.;
         ax = ay = az = 0.;
         if (MODE == 1) { s.fx[i] = 0.; s.fy[i] = 0.; s.fz[i] = 0.; }
       }

@@ -249,6 +249,13 @@ int orc_derive_params(const mfa_inputs* in, mfa_params* p, mfa_system* s) {
   p->rc_coul_2 = in->rc_coul * in->rc_coul;
   p->compat = in->compat;
   p->hist_dim = in->hist_dim > 0 ? in->hist_dim : 200;
+  /* heads sheared with the walls (verlet_velocities.f90:111-124); refused with the body force
+     (init_params.f90:899-907) and with explicit walls (their sites would move too) */
+  if (in->va_spring_twall[0] != 0. || in->va_spring_twall[1] != 0. || in->va_spring_twall[2] != 0.) {
+    if (f->poiseuille || f->wall == 1) return -2;
+    p->va_wall[0] = in->va_spring_twall[0];
+    p->va_wall[1] = in->va_spring_twall[1];
+  }
   p->r_2_min_init = 0.;
   p->r_2_min_time = 0.;
   /* box and counts */
@@ -1315,10 +1322,15 @@ void orc_verlet_velocities(orc_sys* o) {
       for (int d = 0; d < 3; ++d) o->v[3 * h + d] = o->force[3 * h + d] = o->a[3 * h + d] = 0.;
     }
   } else {
-    /* heads move with the walls (va_spring_twall = 0 for implicit walls without shear) */
+    /* verlet_velocities.f90:111-124: the heads of chains 1..n_chain/2 move at va_spring_twall(1:2),
+       the others at -va_spring_twall(1:2); no z velocity, force or acceleration */
     for (int c = 0; c < o->s.n_chain; ++c) {
       int h = c * o->s.n_mon;
-      for (int d = 0; d < 3; ++d) o->v[3 * h + d] = o->force[3 * h + d] = o->a[3 * h + d] = 0.;
+      const double sg = (c < o->s.n_chain / 2) ? 1. : -1.;
+      for (int d = 0; d < 3; ++d) o->force[3 * h + d] = o->a[3 * h + d] = 0.;
+      o->v[3 * h] = sg * o->p.va_wall[0];
+      o->v[3 * h + 1] = sg * o->p.va_wall[1];
+      o->v[3 * h + 2] = 0.;
     }
   }
   double t = 0.;

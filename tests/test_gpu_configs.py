@@ -588,3 +588,47 @@ def test_reference_defect_switches(gpu, oracle_mod, compat):
     assert np.abs(out[compat][1] - out[0][1]).max() > 1e-6 * np.abs(out[0][1]).max()
     if compat & 4:
         assert abs(out[compat][0] - out[0][0]) > 1e-6 * abs(out[0][0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sheared_brushes_moving_heads(gpu, oracle_mod, precision):
+    """Brush-brush shear (verlet_velocities.f90:111-124): the heads of chains 1..n_chain/2 move at
+    va_spring_twall(1:2), the others at minus it, with no z motion; DPD on.  Twelve md_main steps
+    through the drop-ins (FP64) or the fused step (mixed) against the oracle, positions,
+    velocities and the kinetic energy (which counts the heads' motion); the heads advance by
+    exactly +-va dt per step (modulo the box)."""
+    inp = configs.wca_inputs(gamma=5.0, kT=1.0, dt=0.005)
+    inp.va_spring_twall[0], inp.va_spring_twall[1], inp.va_spring_twall[2] = 0.4, -0.15, 0.0
+    p, _ = md.derive(inp)
+    assert tuple(p.va_wall) == (0.4, -0.15)
+    s, a_type, r0, v = configs.brush_channel(12.0, 10.0, 0.15, 12, seed=17)
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    n = 12
+    if precision == "fp64":
+        for _ in range(n):
+            eg = g.md_step()[0]
+    else:
+        g.step(n)
+        eg = g.energies()[0]
+    o.step(n, 1, 0)
+    r, vv, _, _ = g.state()
+    ro, vo, _, _ = o.state()
+    L = np.array(list(s.boundary))
+    d = r - ro
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < (1e-9 if precision == "fp64" else 1e-7)
+    tol = 1e-7 if precision == "fp64" else 1e-4
+    assert np.abs(vv - vo).max() < tol * max(1.0, np.sqrt(np.mean(vo ** 2)))
+    heads = np.arange(s.n_chain) * s.n_mon
+    sg = np.where(np.arange(s.n_chain) < s.n_chain // 2, 1.0, -1.0)
+    assert np.array_equal(vv[heads, 0], sg * 0.4) and np.array_equal(vv[heads, 1], sg * -0.15)
+    assert np.all(vv[heads, 2] == 0.0)
+    # the first position update used the start's head velocities (zero), the other n - 1 the wall's
+    dh = r[heads] - r0.reshape(-1, 3)[heads]
+    dh[:, :2] -= L[:2] * np.round(dh[:, :2] / L[:2])
+    want = np.stack([sg * 0.4, sg * -0.15, 0.0 * sg], axis=1) * (n - 1) * p.dt
+    assert np.abs(dh - want).max() < 1e-9
+    assert abs(eg["t_fluid"] - o.energies()["t_fluid"]) < (1e-9 if precision == "fp64" else 1e-5) * o.energies()["t_fluid"]
+    g.close()
+    o.close()

@@ -219,3 +219,31 @@ def test_ewald_virial_is_minus_the_strain_derivative(oracle_mod):
             assert abs(fd - W[g][a, b]) <= 1e-5 * max(1.0, np.abs(W[g]).max()), (g, a, b, fd, W[g][a, b])
     for g in ("pair", "kspace", "dipole"):
         assert np.abs(W[g] - W[g].T).max() <= 1e-9 * max(1.0, np.abs(W[g]).max())
+
+
+def test_sheared_heads_and_refusals(oracle_mod):
+    """The wall velocity of the brush-brush shear reaches the tables of both derivations; the
+    oracle moves the heads at +-va_wall; a moving wall is refused with the body force
+    (init_params.f90:899-907) and with explicit walls."""
+    import numpy as np
+    from mfa_brush_gb300 import abi, configs, md
+    inp = configs.wca_inputs(gamma=5.0, kT=1.0, dt=0.005)
+    inp.va_spring_twall[0], inp.va_spring_twall[1] = 0.25, 0.5
+    p, _ = md.derive(inp)
+    po, _ = oracle_mod.derive_params(inp)
+    assert tuple(p.va_wall) == tuple(po.va_wall) == (0.25, 0.5)
+    s, a_type, r0, v = configs.brush_channel(12.0, 10.0, 0.15, 10, seed=3)
+    o = oracle_mod.Oracle(po, s, a_type, r0, v)
+    o.step(5, 1, 0)
+    vv = o.state()[1]
+    heads = np.arange(s.n_chain) * s.n_mon
+    sg = np.where(np.arange(s.n_chain) < s.n_chain // 2, 1.0, -1.0)
+    assert np.array_equal(vv[heads, 0], 0.25 * sg) and np.array_equal(vv[heads, 1], 0.5 * sg)
+    o.close()
+    for flag in ("poiseuille", "wall1"):
+        bad = configs.wca_inputs(gamma=5.0, wall=1 if flag == "wall1" else 2)
+        bad.va_spring_twall[0] = 0.1
+        if flag == "poiseuille":
+            bad.flags.poiseuille = 1
+        with pytest.raises(abi.MfaError):
+            md.derive(bad)
