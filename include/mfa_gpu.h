@@ -262,6 +262,11 @@ typedef struct mfa_averages {
   double rg2_brush[3], rg2_melt[3], rg2_mean[3];  /* r_g2_mean(1..3,:) / count_obs (fort.42)    */
   double r_par_per2[2];     /* brush and melt (Rg_z^2 - (Rg_x^2 + Rg_y^2)/2) / Rg^2 (fort.43)     */
   double pressure[9];       /* press_tensor_mean / count_obs: the mean of mfa_virial.pressure   */
+  double f_heads[2][3];     /* the mean of mfa_observables.f_heads: minus the summed force on the
+                               heads of chains 1..n_chain/2 and of the others (the f_on_heads of
+                               obser_out.f90:160-176, whose x component over twice the wall area
+                               is the shear stress, and times D / va_spring_twall(1) the
+                               effective viscosity of the sheared brushes)                     */
 } mfa_averages;
 
 typedef struct mfa_ctx mfa_ctx;

@@ -115,7 +115,7 @@ class Averages(C.Structure):
                 [(k, f64) for k in ("v_total", "t_total", "e_total", "v_total2", "t_total2", "e_total2",
                                     "v_fluid", "t_fluid", "e_fluid", "v_fluid2", "t_fluid2", "e_fluid2")] +
                 [("momentum", f64 * 3), ("rg2_brush", f64 * 3), ("rg2_melt", f64 * 3), ("rg2_mean", f64 * 3),
-                 ("r_par_per2", f64 * 2), ("pressure", f64 * 9)])
+                 ("r_par_per2", f64 * 2), ("pressure", f64 * 9), ("f_heads", (f64 * 3) * 2)])
 
     def as_dict(self):
         import numpy as np

@@ -1392,6 +1392,7 @@ int mfa_get_averages(mfa_ctx* ctx, mfa_averages* out) {
     o.r_par_per2[0] = a[A_RPP] * ic;
     o.r_par_per2[1] = a[A_RPP + 1] * ic;
     for (int c = 0; c < 9; ++c) o.pressure[c] = a[A_P + c] * ic;
+    for (int c = 0; c < 6; ++c) o.f_heads[c / 3][c % 3] = a[A_FH + c] * ic;
   }
   return MFA_OK;
 }

@@ -392,6 +392,8 @@ __global__ void k_obs_accum(const double* __restrict__ rec, int nrep, const RepD
   if (sm > 0.) a[A_RPP + 1] += (o[5] - 0.5 * (o[3] + o[4])) / sm;  //  when there are no chains)
   // obser_out.f90:309: press_tensor_mean
   for (int c = 0; c < 9; ++c) a[A_P + c] += w.pressure[c];
+  // obser_out.f90:160-176: f_on_heads summed over the observations
+  for (int c = 0; c < 6; ++c) a[A_FH + c] += rec[(size_t)(O_FH + c) * nrep + r];
 }
 
 void launch_obs_accum(const DevState& s, const SimConst& C, cudaStream_t st, const double* rec, const double* obs,

@@ -63,7 +63,7 @@ __host__ __device__ inline void record_virial(const double* rec, int nrep, int r
 
 // Observation averages per replica (observation.f90:17-301): slots of the accumulator
 enum AvgSlot { A_COUNT = 0, A_VT, A_TT, A_ET, A_VT2, A_TT2, A_ET2, A_VF, A_TF, A_EF, A_VF2, A_TF2, A_EF2,
-               A_MOM = 13, A_RGB = 16, A_RGM = 19, A_RGA = 22, A_RPP = 25, A_P = 27, NAVG = 36 };
+               A_MOM = 13, A_RGB = 16, A_RGM = 19, A_RGA = 22, A_RPP = 25, A_P = 27, A_FH = 36, NAVG = 42 };
 
 
 }  // namespace mfa

@@ -57,11 +57,11 @@ def test_observation_averages_and_series(gpu, oracle_mod, precision):
                      "rg2_brush": rb, "rg2_melt": rm, "rg2_mean": 0.5 * (rb + rm),
                      "r_par_per2": np.array([(rb[2] - 0.5 * (rb[0] + rb[1])) / rb.sum(),
                                              (rm[2] - 0.5 * (rm[0] + rm[1])) / rm.sum()]),
-                     "pressure": P})
+                     "pressure": P, "f_heads": np.array(ob["f_heads"])})
     tol = TOL[precision]
     assert av["count"] == n_obs
     for key in ("v_total", "t_total", "e_total", "v_fluid", "e_fluid", "rg2_brush", "rg2_melt", "rg2_mean",
-                "r_par_per2", "pressure"):
+                "r_par_per2", "pressure", "f_heads"):
         near(av[key], np.mean([r[key] for r in rows], axis=0), tol, key)
     near(av["v_total2"], np.mean([r["v_total"] ** 2 for r in rows]), tol, "v_total2")
     # the momentum is a sum of cancelling terms: compare it on the scale of the particles' own
