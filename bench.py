@@ -361,6 +361,8 @@ def main():
                     help="threads per block of the pair kernel (32, 64, 128); tuned with --skin auto")
     ap.add_argument("--list-cells", type=int, default=0,
                     help="list-build cells per list cut-off (1, 2, 3; 0 = the library's choice)")
+    ap.add_argument("--list-cells-x", type=int, default=0,
+                    help="list-build cells per list cut-off along x alone (0 = as --list-cells)")
     ap.add_argument("--separate-integrator", action="store_true",
                     help="a separate integrator kernel on every step (default: fused into the pair kernel)")
     ap.add_argument("--pair-schedule", type=int, default=0,
@@ -434,7 +436,8 @@ def main():
     args.skin = float(args.skin)
     g = md.MdSystem(p, systems, a_type, r0, v, precision=args.precision, device=local, skin=args.skin,
                     block_size=args.block, list_cells=args.list_cells, pair_schedule=args.pair_schedule,
-                    separate_integrator=args.separate_integrator, series_capacity=2 * STEP_CALL // CHUNK)
+                    separate_integrator=args.separate_integrator, series_capacity=2 * STEP_CALL // CHUNK,
+                    list_cells_x=args.list_cells_x)
 
     def barrier():
         if dist is not None:
@@ -504,7 +507,8 @@ def main():
                        "precision": args.precision, "steps_per_call": args.call,
                        "energy_record": "every %d steps on the device, kept in the energy-series ring" % CHUNK,
                        "skin": args.skin,
-                       "pair_block": args.block, "list_cells": g.list_cells(), "pair_schedule": args.pair_schedule,
+                       "pair_block": args.block, "list_cells": g.list_cells(),
+                       "list_cells_x": g.options_in_use().list_cells_x, "pair_schedule": args.pair_schedule,
                        "integration": "fused into the pair kernel" if fused else "separate kernel",
                        "skin_autotune": tuned,
                        "l2_flush": "inputs larger than L2 (~1.5 GB working set)",

@@ -205,6 +205,10 @@ typedef struct mfa_options {
                                tail of the pair kernel (one launch per step instead of two);
                                1: a separate integrator kernel on every step.  The trajectory is
                                the same bit for bit.                                          */
+  int32_t list_cells_x;     /* list-build cells per list cut-off along x alone: 1, 2 or 3 when
+                               list_cells is 1 (finer cells in x trim the x-runs of the 3x3 rows
+                               closer to the cut-off sphere); 0 (default) = 2 when list_cells is
+                               1 and every box holds 5 such cells in x, else list_cells        */
 } mfa_options;
 
 typedef struct mfa_energies {

@@ -89,7 +89,7 @@ class Options(C.Structure):
                 ("energy_every", i32), ("use_graphs", i32), ("block_size", i32),
                 ("profile_from_step", i32), ("kspace_plain_sums", i32), ("observe", i32),
                 ("series_capacity", i32), ("list_cells", i32), ("pair_schedule", i32),
-                ("separate_integrator", i32)]
+                ("separate_integrator", i32), ("list_cells_x", i32)]
 
 
 class Energies(C.Structure):

@@ -591,6 +591,17 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       for (int d = 0; d < 2; ++d)
         while (nl_h < 3 && std::floor(ctx->sys[r].boundary[d] / (rl_max / nl_h)) < 2 * nl_h + 1) ++nl_h;
   }
+  // along x: as asked, else 2 with 3x3 rows in y, z when every box holds 5 such cells in x (the
+  // x-runs then follow the cut-off sphere more closely), else as in y, z
+  int nl_hx = ctx->opt.list_cells_x;
+  if (nl_hx == 0) {
+    nl_hx = nl_h;
+    bool fits = nl_h == 1;
+    for (int r = 0; r < n_rep; ++r) fits = fits && std::floor(ctx->sys[r].boundary[0] / (rl_max / 2)) >= 5;
+    if (fits) nl_hx = 2;
+  }
+  if (nl_hx < 1 || nl_hx > 3 || (nl_hx != nl_h && nl_h != 1))
+    return fail(ctx, MFA_ERR_ARG, "list_cells_x must be 0, or 1, 2 or 3 with list_cells 1");
   for (int r = 0; r < n_rep; ++r) {
     const mfa_system& s = ctx->sys[r];
     RepDesc& R = ctx->hreps[r];
@@ -604,9 +615,10 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
       R.ufx_f[d] = (float)R.ufx[d];
       // list cells of at least 1/h of the list cut-off: the (2h+1)^3 stencil covers every
       // neighbour, and 2h+1 cells in x and y keep each cell of a stencil row distinct
-      int nc = (int)std::floor(s.boundary[d] / (rl_max / nl_h));
+      const int h = (d == 0) ? nl_hx : nl_h;
+      int nc = (int)std::floor(s.boundary[d] / (rl_max / h));
       if (nc < 1) nc = 1;
-      if (d < 2 && nc < 2 * nl_h + 1)
+      if (d < 2 && nc < 2 * h + 1)
         return fail(ctx, MFA_ERR_UNSUPPORTED,
                     "box shorter than (2 + 1/list_cells)*(r_cut_max+skin) in x or y");
       R.nc[d] = nc;
@@ -751,6 +763,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   S.tabd = ctx->dtabd;
   S.rl2_uni = S.mixed ? C.rl2_uni_f : 0.f;
   S.nl_h = nl_h;
+  S.nl_hx = nl_hx;
   if (ctx->opt.pair_schedule < 0 || ctx->opt.pair_schedule > 1)
     return fail(ctx, MFA_ERR_ARG, "pair_schedule must be 0 or 1");
   S.pair_persist = ctx->opt.pair_schedule;
@@ -1224,6 +1237,7 @@ int mfa_get_options(mfa_ctx* ctx, mfa_options* out) {
   if (!ctx || !out) return MFA_ERR_ARG;
   *out = ctx->opt;
   out->list_cells = ctx->S.nl_h;
+  out->list_cells_x = ctx->S.nl_hx;
   return MFA_OK;
 }
 

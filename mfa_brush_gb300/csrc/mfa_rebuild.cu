@@ -416,7 +416,7 @@ __global__ void k_copyback(DevState s) {
 // coalesced; a particle with more neighbours writes the rest straight to the list)
 constexpr int NL_STAGE = 32;
 
-template <bool MIXED, bool UNI, int H>
+template <bool MIXED, bool UNI, int H, int HX = H>
 __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s) {
   const int nwl = *s.wl_n;
   const int nchunks = s.wl_k[nwl];
@@ -495,9 +495,9 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s) {
       d = fmaxf(d, 0.f) * l;
       return d * d;
     };
-    float gxp[H], gxm[H];  // squared gaps to the cells ix + k and ix - k, k = 1..H
+    float gxp[HX], gxm[HX];  // squared gaps to the cells ix + k and ix - k, k = 1..HX
 #pragma unroll
-    for (int k = 1; k <= H; ++k) {
+    for (int k = 1; k <= HX; ++k) {
       gxp[k - 1] = gap2(fl(ix + k) - px, lx);
       gxm[k - 1] = gap2(px - fl(ix - k + 1), lx);
     }
@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(NL_BLOCK, 8) k_nlist(DevState s) {
         if (rem2 <= 0.f) continue;  // the whole row is beyond the list cut-off
         int xa = ix, xb = ix;
 #pragma unroll
-        for (int k = 0; k < H; ++k) {
+        for (int k = 0; k < HX; ++k) {
           xa -= gxm[k] < rem2;
           xb += gxp[k] < rem2;
         }
@@ -619,7 +619,10 @@ void launch_rebuild(const DevState& s, cudaStream_t st, bool force) {
   const KernT kerns[3][3] = {{k_nlist<false, false, 1>, k_nlist<true, false, 1>, k_nlist<true, true, 1>},
                              {k_nlist<false, false, 2>, k_nlist<true, false, 2>, k_nlist<true, true, 2>},
                              {k_nlist<false, false, 3>, k_nlist<true, false, 3>, k_nlist<true, true, 3>}};
-  const KernT kern = kerns[s.nl_h - 1][var];
+  // cells finer along x alone (with 3x3 rows in y, z)
+  const KernT kx[2][3] = {{k_nlist<false, false, 1, 2>, k_nlist<true, false, 1, 2>, k_nlist<true, true, 1, 2>},
+                          {k_nlist<false, false, 1, 3>, k_nlist<true, false, 1, 3>, k_nlist<true, true, 1, 3>}};
+  const KernT kern = (s.nl_hx != s.nl_h) ? kx[s.nl_hx - 2][var] : kerns[s.nl_h - 1][var];
   const int gl = std::min((s.N + NL_BLOCK - 1) / NL_BLOCK, s.nsm * 8);
   kern<<<gl, NL_BLOCK, 0, st>>>(s);
   k_clear_flags<<<1, 256, 0, st>>>(s.rebuild_flag, s.nrep, s.rebuilds, s.rep_rebuilds);

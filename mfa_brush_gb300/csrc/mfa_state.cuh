@@ -43,6 +43,7 @@ struct DevState {
   // control words
   float rl2_uni;  // SimConst::rl2_uni_f (0: per-pair list cut-offs)
   int nl_h;       // list-build cells per list cut-off; the search covers (2 nl_h + 1)^3 cells
+  int nl_hx;      // the same along x alone (nl_h unless list_cells_x; only with nl_h 1)
   int pair_persist;  // mfa_options.pair_schedule
   int* pair_q;       // [2] the persistent pair kernel's queue: next tile, blocks finished
   int* rebuild_flag;          // [1 + nrep]: [0] some replica needs a rebuild, [1 + r] replica r does

@@ -69,7 +69,7 @@ def read_deck(deck_dir, conf="conf_old"):
 
 def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, device=0, nbr_capacity=0,
             profile_from_step=0, block_size=0, kspace_plain_sums=False, observe=False, series_capacity=0,
-            list_cells=0, pair_schedule=0, separate_integrator=False):
+            list_cells=0, pair_schedule=0, separate_integrator=False, list_cells_x=0):
     o = abi.Options()
     _lib().mfa_default_options(C.byref(o))
     o.precision = abi.PREC_MIXED if precision in ("mixed", abi.PREC_MIXED) else abi.PREC_FP64
@@ -86,6 +86,7 @@ def options(precision="mixed", skin=0.3, energy_every=10, use_graphs=True, devic
     o.list_cells = list_cells
     o.pair_schedule = pair_schedule
     o.separate_integrator = 1 if separate_integrator else 0
+    o.list_cells_x = list_cells_x
     return o
 
 

@@ -517,7 +517,9 @@ def test_state_round_trip_pinned_and_pageable(gpu):
 @pytest.mark.parametrize("setup", ["brush", "melt"])
 def test_list_cells_give_the_same_lists(gpu, precision, setup):
     """List-build cells of the whole, a half and a third of the list cut-off (list_cells 1, 2, 3)
-    walk 3^3, 5^3 and 7^3 cells; the lists hold the same pairs in another order.  Per replica the
+    walk 3^3, 5^3 and 7^3 cells, and cells of a half or a third of it along x alone (list_cells 1
+    with list_cells_x 2, 3) 5 x 3 x 3 and 7 x 3 x 3; the lists hold the same pairs in another
+    order.  Per replica the
     same interacting pairs and the same largest list count; pair forces equal up to the order of
     the sums (FP64 1e-12, mixed 1e-5 of F_rms); 20 steps of the fused step stay within 1e-6 sigma
     (brush replicas with one cut-off; melt in brush with per-type cut-offs)."""
@@ -529,9 +531,10 @@ def test_list_cells_give_the_same_lists(gpu, precision, setup):
         p, (s, a_type, r0, v) = configs.melt_brush(L=14.0, D=24.0)
         systems = [s]
     out = {}
-    for h in (1, 2, 3):
-        g = md.MdSystem(p, systems, a_type, r0, v, precision=precision, list_cells=h)
-        assert g.list_cells() == h
+    for h in (1, 2, 3, (1, 2), (1, 3)):
+        hyz, hx = h if isinstance(h, tuple) else (h, h)
+        g = md.MdSystem(p, systems, a_type, r0, v, precision=precision, list_cells=hyz, list_cells_x=hx)
+        assert g.list_cells() == hyz and g.options_in_use().list_cells_x == hx
         pairs = [set(map(tuple, np.sort(g.pair_list(k), axis=1).tolist())) for k in range(len(systems))]
         g.zero_force()
         g.fluid_fluid()
@@ -541,12 +544,13 @@ def test_list_cells_give_the_same_lists(gpu, precision, setup):
         out[h] = (pairs, f, mx, g.state()[0])
         g.close()
     g = md.MdSystem(p, systems, a_type, r0, v, precision=precision)
-    assert g.list_cells() == 1  # these boxes hold three cells of the list cut-off in x and y
+    # these boxes hold three cells of the list cut-off in x and y, and five of half of it in x
+    assert g.list_cells() == 1 and g.options_in_use().list_cells_x == 2
     g.close()
     pairs2, f2, mx2, r2 = out[2]
     frms = np.sqrt(np.mean(np.sum(f2 ** 2, axis=1)))
     tol = 1e-12 if precision == "fp64" else 1e-5
-    for h in (1, 3):
+    for h in (1, 3, (1, 2), (1, 3)):
         pairs, f, mx, r = out[h]
         assert pairs == pairs2 and mx == mx2
         assert np.abs(f - f2).max() <= tol * frms, (h, np.abs(f - f2).max() / frms)
