@@ -1154,7 +1154,9 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs
   const int mask = any_chains(ctx) ? bonded_mask(ctx) : 0;
   long long L = 0;
   auto energies_at = [&](int k) { return ((phase + k) % ctx->opt.energy_every == 0) || k == n; };
-  auto fused_at = [&](int k) { return ctx->fuse_integ && k < n && !energies_at(k) && !prof; };
+  // (an energy step fuses too, unless it also observes: the observation reads the state after its
+  // velocity update and before its position update)
+  auto fused_at = [&](int k) { return ctx->fuse_integ && k < n && !prof && !(obs && energies_at(k)); };
   int n_fused = 0;
   for (int k = 1; k <= n; ++k) n_fused += fused_at(k) ? 1 : 0;
   const DevState sets[2] = {ctx->S, other_views(ctx->S)};
@@ -1179,40 +1181,42 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs
       launch_rebuild(S, st, false);
       L += kRebuildLaunches;
     }
+    const bool split = prof || (obs && ef);
     if (fused_at(k)) {  // forces and this step's integration in one kernel; the views move across
-      launch_pair(S, C, st, false, false, acc, ctx->opt.block_size, mask, true);
+      launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, mask, true);
       L += 1;
       cur ^= 1;
-      continue;
-    }
-    // mixed: bonded terms inside the pair kernel; FP64: their own kernel
-    launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
-    L += 1;
-    if (mask && !S.mixed) { launch_bonded(S, C, st, mask, ef, acc, true); L += 1; }
-    if (ctx->kspace) {
-      launch_kspace(S, C, ctx->K, st, ef, acc, true);
-      launch_dipolar(S, C, ctx->K, st, ef, acc, true);
-      L += 7;
-    }
-    const bool split = prof || (obs && ef);
-    if (k < n && !split) {
-      launch_integrate(S, C, st, 2, true, ef, acc);
-      L += 1;
     } else {
-      launch_integrate(S, C, st, 1, true, ef, acc);
+      // mixed: bonded terms inside the pair kernel; FP64: their own kernel
+      launch_pair(S, C, st, false, ef, acc, ctx->opt.block_size, S.mixed ? mask : 0);
       L += 1;
-      if (prof) { launch_profiles(S, C, st, ctx->prof, C.hist_dim); L += 1; }
+      if (mask && !S.mixed) { launch_bonded(S, C, st, mask, ef, acc, true); L += 1; }
+      if (ctx->kspace) {
+        launch_kspace(S, C, ctx->K, st, ef, acc, true);
+        launch_dipolar(S, C, ctx->K, st, ef, acc, true);
+        L += 7;
+      }
+      if (k < n && !split) {
+        launch_integrate(S, C, st, 2, true, ef, acc);
+        L += 1;
+      } else {
+        launch_integrate(S, C, st, 1, true, ef, acc);
+        L += 1;
+        if (prof) { launch_profiles(S, C, st, ctx->prof, C.hist_dim); L += 1; }
+      }
     }
     if (ef) {
+      // the set that holds the step counter after this step's integration
+      const DevState& Sn = sets[cur];
       launch_record(acc, ctx->rec, st);
       L += 1;
       if (obs) {
-        launch_observe(S, C, st, ctx->obs);
-        launch_obs_accum(S, C, st, ctx->rec, ctx->obs, ctx->avg);
+        launch_observe(Sn, C, st, ctx->obs);
+        launch_obs_accum(Sn, C, st, ctx->rec, ctx->obs, ctx->avg);
         L += 2;
       }
       if (ctx->series) {
-        launch_series(S, st, ctx->rec, ctx->series, ctx->series_step, ctx->series_head, ctx->opt.series_capacity);
+        launch_series(Sn, st, ctx->rec, ctx->series, ctx->series_step, ctx->series_head, ctx->opt.series_capacity);
         L += 2;
       }
     }

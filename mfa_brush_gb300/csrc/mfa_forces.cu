@@ -463,7 +463,8 @@ __device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimCon
 // Without FUSED the forces are added to (accumulate) or stored in the FP64 force arrays.
 // Virial (EFLAG): each visit of a pair adds half of F_ij (x) (r_i - r_j) (the other visit adds the
 // other half); a pair with a fixed wall bead, which has no list of its own, counts in full.
-//   INTEG   (FUSED, without EFLAG) the step's integration in the tail: each thread takes its
+//   INTEG   (FUSED) the step's integration in the tail (with EFLAG also its kinetic energy and
+//           tensor and the head forces, into the same warp reduction): each thread takes its
 //           particle's force and runs the integrator's update (int_mixed_particle, MODE 2) on it,
 //           writing the next step's views to the other view buffers (pfx_alt, vf_alt) while the
 //           neighbours still read pfx and vf; wall beads copy their views across, and the step
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
   using real = real_t<MIXED>;
   static_assert(!FUSED || MIXED, "the fused form is the mixed-precision one");
   static_assert(!BONDED || FUSED, "bonded terms are fused only into the fused form");
-  static_assert(!INTEG || (FUSED && !EFLAG && !PERSIST), "the integration is fused into the plain fused form");
+  static_assert(!INTEG || (FUSED && !PERSIST), "the integration is fused into the fused form");
   __shared__ PairEntry<real> tab[NPAIR];
   // FUSED: the particle's FP64 total, in shared memory while the pair loop runs (registers are
   // scarce there; it is touched once per batch)
@@ -667,6 +668,8 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
   if (EFLAG && BONDED) bv.zero();
   bool hb = false;
   double fxd = 0., fyd = 0., fzd = 0.;
+  // INTEG with EFLAG: the integrator's kinetic energy, kinetic tensor and head forces
+  float ike = 0.f, ikin[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, ifh[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if constexpr (FUSED) {
     fxd = ftot[0][threadIdx.x];
     fyd = ftot[1][threadIdx.x];
@@ -684,9 +687,8 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
   if (inside) {
     if constexpr (INTEG) {
       if (active) {
-        float ke, kin[6], fh[6];
-        int_mixed_particle<2, false>(s, C, i, w, d2f_fast(fxd), d2f_fast(fyd), d2f_fast(fzd), s.pfx_alt, s.vf_alt, ke,
-                                     kin, fh);
+        int_mixed_particle<2, EFLAG>(s, C, i, w, d2f_fast(fxd), d2f_fast(fyd), d2f_fast(fzd), s.pfx_alt, s.vf_alt,
+                                     ike, ikin, ifh);
       } else {  // a wall bead: its views as they are
         s.pfx_alt[i] = s.pfx[i];
         s.vf_alt[i] = s.vf[i];
@@ -707,7 +709,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
     }
   }
   if (EFLAG) {  // one warp reduction for every energy and virial component of the kernel
-    constexpr int NB = BONDED ? 31 : 0, NW = FUSED ? 2 : 0, NV = 8 + NB + NW;
+    constexpr int NB = BONDED ? 31 : 0, NW = FUSED ? 2 : 0, NI = INTEG ? 13 : 0, NV = 8 + NB + NW + NI;
     int sl[NV];
     real v[NV];
     sl[0] = O_VFF; v[0] = e_lj;
@@ -718,8 +720,18 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
       bonded_slots(sl + 8, v + 8, eb, bv);
     }
     if constexpr (FUSED) {
-      sl[NV - 2] = O_VFW; v[NV - 2] = e_w;
-      sl[NV - 1] = O_VIR + 9 * V_WALL + 8; v[NV - 1] = w_wall;
+      sl[8 + NB] = O_VFW; v[8 + NB] = e_w;
+      sl[9 + NB] = O_VIR + 9 * V_WALL + 8; v[9 + NB] = w_wall;
+    }
+    if constexpr (INTEG) {  // the integrator's kinetic energy, kinetic tensor and head forces
+      constexpr int b = 8 + NB + NW;
+      const int idx[6] = {0, 4, 8, 1, 2, 5};
+      sl[b] = O_TFLUID; v[b] = ike;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        sl[b + 1 + c] = O_KIN + idx[c]; v[b + 1 + c] = ikin[c];
+        sl[b + 7 + c] = O_FH + c; v[b + 7 + c] = ifh[c];
+      }
     }
     obs_push<real, NV>(acc, sl, v, rep, active);
   }
@@ -749,14 +761,18 @@ void launch_pair(const DevState& s, const SimConst& C, cudaStream_t st, bool acc
     // the persistent schedule for the steps without energies: [bonded][uni]
     const KernT kp[2][2] = {{k_pair<true, false, true, false, false, true>, k_pair<true, false, true, false, true, true>},
                             {k_pair<true, false, true, true, false, true>, k_pair<true, false, true, true, true, true>}};
-    // with the step's integration in the tail: [bonded][uni]
-    const KernT ki[2][2] = {{k_pair<true, false, true, false, false, false, true>,
-                             k_pair<true, false, true, false, true, false, true>},
-                            {k_pair<true, false, true, true, false, false, true>,
-                             k_pair<true, false, true, true, true, false, true>}};
+    // with the step's integration in the tail: [eflag][bonded][uni]
+    const KernT ki[2][2][2] = {{{k_pair<true, false, true, false, false, false, true>,
+                                 k_pair<true, false, true, false, true, false, true>},
+                                {k_pair<true, false, true, true, false, false, true>,
+                                 k_pair<true, false, true, true, true, false, true>}},
+                               {{k_pair<true, true, true, false, false, false, true>,
+                                 k_pair<true, true, true, false, true, false, true>},
+                                {k_pair<true, true, true, true, false, false, true>,
+                                 k_pair<true, true, true, true, true, false, true>}}};
     const int bi = bonded_mask ? 1 : 0, ui = uni ? 1 : 0;
     if (integ) {
-      ki[bi][ui]<<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
+      ki[eflag ? 1 : 0][bi][ui]<<<g, B, 0, st>>>(s, C, false, acc, bonded_mask);
     } else if (s.pair_persist && !eflag) {
       const KernT k = kp[bi][ui];
       int per_sm = 0;

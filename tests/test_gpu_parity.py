@@ -425,11 +425,11 @@ def test_persistent_pair_schedule_does_not_change_the_trajectory(gpu):
 
 @pytest.mark.parametrize("setup", ["brush", "melt"])
 def test_fused_integration_does_not_change_the_trajectory(gpu, setup):
-    """The mixed mfa_step runs the integration of its plain steps in the pair kernel's tail, with
-    the views written to the other buffer set (options.separate_integrator 0, the default); with
-    a separate integrator kernel (1) the state is the same bit for bit: over calls of 7, 13 and 10
-    steps (odd and even numbers of fused steps, rebuilds included), then a drop-in pair force
-    evaluation on the views that the calls left."""
+    """The mixed mfa_step runs the integration of its steps in the pair kernel's tail, with the
+    views written to the other buffer set (options.separate_integrator 0, the default); with a
+    separate integrator kernel (1) the state is the same bit for bit: over calls of 7, 13 and 10
+    steps (odd and even numbers of fused steps, rebuilds and energy steps included), then a
+    drop-in pair force evaluation on the views that the calls left; the energy series agrees."""
     if setup == "brush":
         p = configs.wca_params(gamma=5.0)
         systems, a_type, r0, v = configs.concat(configs.replicas(4, seed=9))
@@ -437,21 +437,32 @@ def test_fused_integration_does_not_change_the_trajectory(gpu, setup):
         p, (systems, a_type, r0, v) = configs.melt_brush(L=14.0, D=24.0)
     out = []
     for sep in (False, True):
-        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", separate_integrator=sep)
-        states = []
+        g = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", separate_integrator=sep, energy_every=5,
+                        series_capacity=16)
+        states, series = [], []
         for n in (7, 13, 10):
             g.step(n)
             states.append(g.state())
+            series += g.energy_series()
         g.zero_force()
         e = g.fluid_fluid()[0]
-        out.append((states, g.state()[3], e, g.step_index()))
+        out.append((states, g.state()[3], e, g.step_index(), series))
         g.close()
-    (s0, f0, e0, k0), (s1, f1, e1, k1) = out
+    (s0, f0, e0, k0, r0_), (s1, f1, e1, k1, r1_) = out
     assert k0 == k1
     for a, b in zip(s0, s1):
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
     assert np.array_equal(f0, f1) and np.array_equal(e0, e1)
+    # the energy records (every 5th step and the last of each call; the fused energy steps push
+    # the kinetic energy and head forces from the pair kernel): same steps, same values up to the
+    # order of the FP64 atomic sums
+    assert len(r0_) == len(r1_) >= 6
+    for a, b in zip(r0_, r1_):
+        for ra, rb in zip(a, b):
+            assert ra["step"] == rb["step"]
+            for key in ("v_fluid_fluid", "v_intra_molec", "v_fluid_wall", "t_fluid", "e_total"):
+                assert abs(ra[key] - rb[key]) <= 1e-12 * max(abs(rb[key]), 1.0), (key, ra[key], rb[key])
 
 
 def test_measurement_aids(gpu):
