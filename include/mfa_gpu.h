@@ -367,8 +367,9 @@ int mfa_list_stats(mfa_ctx* ctx, int32_t* capacity, int32_t* max_count);
 /* The options the context runs with: those given to mfa_init / mfa_batch_init, with list_cells
    resolved to the value in use.                                                               */
 int mfa_get_options(mfa_ctx* ctx, mfa_options* out);
-/* Size of the reciprocal-space sum: k-vectors of the reference's k-set (ewald_k.f90:47-124) and
-   charged particles; both 0 for an uncharged context.                                         */
+/* Size of the reciprocal-space sum of replica 0: k-vectors of the reference's k-set
+   (ewald_k.f90:47-124) and charged particles; both 0 for an uncharged context.  Each replica of a
+   charged batch has its own k-set, built from its own box.                                    */
 int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged);
 /* Absolute step counter of replica 0 (s_time + steps done). */
 int mfa_get_step(mfa_ctx* ctx, int64_t* step);

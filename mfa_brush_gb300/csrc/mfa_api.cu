@@ -38,7 +38,7 @@ struct mfa_ctx {
   long long n_obs = 0;
   std::vector<double> v_coul_self, v_ww;
   std::vector<double> v_ff_walls;  // LJ energy of the fixed wall beads among themselves (WALL 1)
-  KSpace K;
+  std::vector<KSpace> Ks;  // k-space of each replica (its own box, k-set and charged particles)
   bool kspace = false;
   bool fuse_integ = false;  // mfa_step runs the integration of its plain steps in the pair kernel
   unsigned* h_status = nullptr;  // pinned: [0] status bits, [1] largest list count seen
@@ -224,9 +224,11 @@ void fill_virial(const mfa_ctx* ctx, const double* acc, int rep, mfa_virial* o) 
 }
 
 // ewald_k(0) (ewald_k.f90:37-124): the k-vectors in the reference's enumeration order, G(k),
-// and the list of charged particles (replica 0).
-int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
-  const mfa_system& s = ctx->sys[0];
+// and the list of charged particles, of replica rep (the particles p0 .. p0 + n_mon_tot - 1 of the
+// batch; a_type holds the whole batch).
+int setup_kspace(mfa_ctx* ctx, const int32_t* a_type, int rep) {
+  const mfa_system& s = ctx->sys[rep];
+  const int p0 = ctx->hreps[rep].p0;
   const mfa_params& p = ctx->P;
   const double pi = (double)3.1415926536f;  // mfa_common.f90:315
   const double* L = s.boundary;
@@ -254,7 +256,7 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
         const double kk = k0 * k0 + k1 * k1 + k2 * k2;
         kf.push_back((1. / kk) * std::exp(-kk * fac_alpha));
       }
-  KSpace& K = ctx->K;
+  KSpace& K = ctx->Ks[rep];
   std::memset(&K, 0, sizeof K);
   K.nk = (int)kn.size();
   K.nxm = nx;
@@ -266,14 +268,14 @@ int setup_kspace(mfa_ctx* ctx, const int32_t* a_type) {
   K.cz = dk[2] / (2. * M_PI);
   K.inv_V = (1. / L[0]) * (1. / L[1]) / (L[2] * (1. + z_slab));
   K.lz_half = L[2] / 2.;
-  K.rep = 0;
+  K.rep = rep;
   K.plain = ctx->opt.kspace_plain_sums ? 1 : 0;
   std::vector<int> qt;
   std::vector<double> qv;
   for (int t = 0; t < s.n_mon_tot; ++t)
-    if (p.charge[a_type[t] - 1] != 0.) {
-      qt.push_back(t);
-      qv.push_back(p.charge[a_type[t] - 1]);
+    if (p.charge[a_type[p0 + t] - 1] != 0.) {
+      qt.push_back(p0 + t);  // the batch's tag
+      qv.push_back(p.charge[a_type[p0 + t] - 1]);
     }
   K.nq = (int)qt.size();
   std::vector<float> qvf(qv.begin(), qv.end());
@@ -438,7 +440,6 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   if (p->compat & MFA_COMPAT_EWALD_I_ONLY)
     return fail(ctx, MFA_ERR_UNSUPPORTED, "Coulomb force on i only depends on the reference's loop order");
   const bool charged = F.system == 2 || F.system == 3;
-  if (charged && n_rep != 1) return fail(ctx, MFA_ERR_UNSUPPORTED, "k-space Ewald is built for one replica");
   ctx->nrep = n_rep;
   ctx->sys.assign(sysv, sysv + n_rep);
   long long N = 0;
@@ -824,8 +825,11 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   }
   // ---- k-space --------------------------------------------------------------------------------
   if (charged && p->n_kmax > 0) {
-    int r = setup_kspace(ctx, a_type);
-    if (r != MFA_OK) return r;
+    ctx->Ks.assign(n_rep, KSpace{});
+    for (int rep = 0; rep < n_rep; ++rep) {
+      int r = setup_kspace(ctx, a_type, rep);
+      if (r != MFA_OK) return r;
+    }
   }
   if (ctx->opt.separate_integrator < 0 || ctx->opt.separate_integrator > 1)
     return fail(ctx, MFA_ERR_ARG, "separate_integrator must be 0 or 1");
@@ -1022,8 +1026,8 @@ int mfa_ewald_k(mfa_ctx* ctx, int32_t mode, double* v) {
   if (!ctx->kspace) return fail(ctx, MFA_ERR_STATE, "ewald_k: not a charged system");
   int r;
   if ((r = zero_call_slot(ctx, O_VCOULK)) || (r = zero_call_group(ctx, V_KSPACE))) return r;
-  launch_kspace(ctx->S, ctx->C, ctx->K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
-  ctx->launches += 4;
+  for (const KSpace& K : ctx->Ks) launch_kspace(ctx->S, ctx->C, K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 4 * (long long)ctx->Ks.size();
   CK(cudaGetLastError());
   return read_call_slot(ctx, O_VCOULK, v, 0.);
 }
@@ -1033,8 +1037,8 @@ int mfa_dipolar_correction(mfa_ctx* ctx, double* v) {
   if (!ctx->kspace) return fail(ctx, MFA_ERR_STATE, "dipolar_correction: not a charged system");
   int r;
   if ((r = zero_call_slot(ctx, O_VDIP)) || (r = zero_call_group(ctx, V_DIP))) return r;
-  launch_dipolar(ctx->S, ctx->C, ctx->K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
-  ctx->launches += 2;
+  for (const KSpace& K : ctx->Ks) launch_dipolar(ctx->S, ctx->C, K, ctx->st, true, acc_of(ctx->acc_call, ctx->nrep));
+  ctx->launches += 2 * (long long)ctx->Ks.size();
   CK(cudaGetLastError());
   return read_call_slot(ctx, O_VDIP, v, 0.);
 }
@@ -1192,9 +1196,11 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs
       L += 1;
       if (mask && !S.mixed) { launch_bonded(S, C, st, mask, ef, acc, true); L += 1; }
       if (ctx->kspace) {
-        launch_kspace(S, C, ctx->K, st, ef, acc, true);
-        launch_dipolar(S, C, ctx->K, st, ef, acc, true);
-        L += 7;
+        for (const KSpace& K : ctx->Ks) {
+          launch_kspace(S, C, K, st, ef, acc, true);
+          launch_dipolar(S, C, K, st, ef, acc, true);
+          L += 7;
+        }
       }
       if (k < n && !split) {
         launch_integrate(S, C, st, 2, true, ef, acc);
@@ -1247,8 +1253,8 @@ int mfa_get_options(mfa_ctx* ctx, mfa_options* out) {
 
 int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged) {
   if (!ctx) return MFA_ERR_ARG;
-  if (n_k) *n_k = ctx->kspace ? ctx->K.nk : 0;
-  if (n_charged) *n_charged = ctx->kspace ? ctx->K.nq : 0;
+  if (n_k) *n_k = ctx->kspace ? ctx->Ks[0].nk : 0;
+  if (n_charged) *n_charged = ctx->kspace ? ctx->Ks[0].nq : 0;
   return MFA_OK;
 }
 
@@ -1713,8 +1719,10 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
     mark(1);
     if (mask && !S.mixed) { launch_bonded(Sk, C, st, mask, ef, acc, true); mark(2); }
     if (ctx->kspace) {
-      launch_kspace(Sk, C, ctx->K, st, ef, acc, true);
-      launch_dipolar(Sk, C, ctx->K, st, ef, acc, true);
+      for (const KSpace& K : ctx->Ks) {
+        launch_kspace(Sk, C, K, st, ef, acc, true);
+        launch_dipolar(Sk, C, K, st, ef, acc, true);
+      }
       mark(4);
     }
     launch_integrate(Sk, C, st, k < nsteps ? 2 : 1, true, ef, acc);

@@ -342,6 +342,70 @@ def test_ewald_contexts_with_different_tables_coexist(gpu, oracle_mod):
     g17.close()
 
 
+def charged_batch():
+    """Three charged brush channels of different boxes, grafting densities and chain lengths (each
+    replica gets its own k-set from its own box)."""
+    p, _, _, _, _ = charged_system()
+    return p, [configs.brush_channel(10.0, 10.0, 0.08, 10, rho=0.5, seed=21),
+               configs.brush_channel(12.0, 9.0, 0.1, 8, rho=0.5, seed=22),
+               configs.brush_channel(11.0, 11.0, 0.05, 12, rho=0.5, seed=23)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ewald_batch_matches_oracle_per_replica(gpu, oracle_mod, precision):
+    """A batch of three charged replicas: the k-space energy, forces and slab dipole correction of
+    each replica against its own oracle (ewald_k.f90 and dipolar_correction.f90 per system)."""
+    p, reps = charged_batch()
+    systems, a_type, r0, v = configs.concat(reps)
+    g = md.MdSystem(p, systems, a_type, r0, v, precision=precision)
+    g.zero_force(); uk = g.ewald_k(); fk = g.state()[3]
+    g.zero_force(); ud = g.dipolar_correction(); fd = g.state()[3]
+    off = 0
+    nks = []
+    for k, (s, at, rr, vv) in enumerate(reps):
+        o = oracle_mod.Oracle(p, s, at, rr, vv)
+        o.ewald_init()
+        nks.append(len(o.kvecs()))
+        o.zero_force(); uko = o.ewald_k(); fko = o.state()[3]
+        o.zero_force(); udo = o.dipolar_correction(); fdo = o.state()[3]
+        n = s.n_part
+        assert rel(uk[k], uko) < (1e-10 if precision == "fp64" else 1e-5)
+        assert_force_parity(fk[off:off + n], fko, precision)
+        assert rel(ud[k], udo) < 1e-10
+        assert np.abs(fd[off:off + n] - fdo).max() < 1e-10 * max(1.0, np.abs(fdo).max())
+        off += n
+    assert len(set(nks)) >= 2  # the replicas' boxes give different k-sets
+    assert g.kspace_info()[0] == nks[0]  # mfa_kspace_info reports the first replica
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_charged_batch_equals_single(gpu, precision):
+    """A charged replica inside a batch gets a bit-identical trajectory to the same replica run
+    alone: its k-space sums cover its own charges in the same order.  Its energies agree to
+    round-off (1e-12 FP64, 1e-7 mixed, whose kernels add a warp's terms in FP32 before the FP64
+    totals): a batch's warps straddle the replicas' boundaries, which regroups the terms."""
+    p, reps = charged_batch()
+    systems, a_type, r0, v = configs.concat(reps)
+    gb = md.MdSystem(p, systems, a_type, r0, v, precision=precision, nbr_capacity=160)
+    gb.step(30)
+    rb, vb, _, _ = gb.state()
+    eb = gb.energies()
+    off = 0
+    for k, (s, at, rr, vv) in enumerate(reps):
+        g1 = md.MdSystem(p, s, at, rr, vv, precision=precision, nbr_capacity=160)
+        g1.step(30)
+        r1, v1, _, _ = g1.state()
+        n = s.n_part
+        assert np.array_equal(r1, rb[off:off + n])
+        assert np.array_equal(v1, vb[off:off + n])
+        e1 = g1.energies()[0]
+        for key in ("v_coul", "v_total", "e_total"):
+            assert rel(e1[key], eb[k][key]) < (1e-12 if precision == "fp64" else 1e-7), key
+        g1.close()
+        off += n
+    gb.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_charged_run_deterministic(gpu, precision):
     """A charged system (slab Ewald + dipolar correction) run twice gives bit-identical states and
