@@ -34,13 +34,16 @@ _EDGE_W = 1e-3
 Z_LO = 0.9  # first/last lattice layer: the repulsive 9-3 wall force there is ~100 eps/sigma
 
 
-def _lattice(L, D, n_sites_min, z_lo=Z_LO):
+def _lattice(L, D, n_sites_min, z_lo=Z_LO, a_max=1.0):
     """Lattice dims (nx, nz) and spacings covering [0,L)^2 x [z_lo, D-z_lo] with at least
-    n_sites_min sites strictly between the two anchor layers (z index 0 and nz-1)."""
-    a = (L * L * max(D - 2 * z_lo, 0.5) / max(n_sites_min, 1)) ** (1.0 / 3.0)
+    n_sites_min sites strictly between the two anchor layers (z index 0 and nz-1).  Both spacings
+    are at most a_max: a walk's face-diagonal step (taken when the axis steps are blocked) is then
+    a bond of at most sqrt(2) a_max, short of the FENE limit of 1.5 (at 1.49, spacing 1.05, the
+    bond force is ~4000 and the first steps can tear the chain at dt = 0.005)."""
+    a = min(a_max, (L * L * max(D - 2 * z_lo, 0.5) / max(n_sites_min, 1)) ** (1.0 / 3.0))
     for _ in range(400):
-        nx = max(3, int(L / a))
-        nz = max(3, int((D - 2 * z_lo) / a) + 1)
+        nx = max(3, int(np.ceil(L / a)))
+        nz = max(3, int(np.ceil((D - 2 * z_lo) / a)) + 1)
         if nx * nx * (nz - 2) >= n_sites_min:
             break
         a *= 0.99
@@ -50,12 +53,14 @@ def _lattice(L, D, n_sites_min, z_lo=Z_LO):
 
 
 def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=None, kT=1.0,
-                  solvent_type=3, melt_type=3, max_fill=0.97, z_lo=Z_LO, wall_spacing=0.0, wall_type=4):
+                  solvent_type=3, melt_type=3, max_fill=0.97, z_lo=Z_LO, wall_spacing=0.0, wall_type=4,
+                  a_max=1.0):
     """One replica: returns (abi.System, a_type[n], r0[n,3], v[n,3]).  Types are the reference's:
     1 head, 2 brush bead, 3 melt/solvent.  wall_spacing > 0 appends explicit wall beads (type
     wall_type, at rest) on a square lattice of that spacing at z = 0 and z = D, after the mobile
     particles as in the reference (init_system.f90:172-187; gen_wall.f90 uses two beads per
-    lattice cell, this generator one)."""
+    lattice cell, this generator one).  a_max caps the lattice spacing (see _lattice); a
+    chain-free replica may raise it."""
     rng = np.random.default_rng(seed)
     n_chain = 2 * int(round(sigma_g * L * L))
     n_brush = n_chain * n_mon
@@ -64,7 +69,7 @@ def brush_channel(L, D, sigma_g, n_mon, rho=0.8, seed=0, n_mon_d=1, n_chain_d=No
         n_chain_d = max(0, (n_total - n_brush) // n_mon_d)
     n_melt = n_chain_d * n_mon_d
     n = n_brush + n_melt
-    nx, nz, ax, az = _lattice(L, D, int(np.ceil((n - n_chain) / max_fill)), z_lo)
+    nx, nz, ax, az = _lattice(L, D, int(np.ceil((n - n_chain) / max_fill)), z_lo, a_max)
     occ = np.zeros((nx, nx, nz), bool)
     # the first and last layer hold the brush heads only; no other bead may enter them
     occ[:, :, 0] = True
@@ -342,8 +347,9 @@ def charged_brush(gamma=5.0, seed=41):
     is spread over the 39 non-head beads of each chain (q = -4/39).  The same number of +1
     counterions (1280) are the fourth species (PARTICLE_4, single beads, WCA with everything),
     drawn at random among the free beads and stored after the neutral solvent, as the reference
-    orders its molecules.  The lattice is filled to 75 % (a fuller lattice at this seed starts
-    with a contact that the FP64 reference algorithm does not survive).
+    orders its molecules.  The lattice is filled to 75 % (at 97 %, on the wider lattice spacing
+    that preceded the 1 sigma cap, this seed started with a contact that the FP64 reference
+    algorithm did not survive).
     Returns (mfa_params, (System, a_type, r0, v))."""
     s, a_type, r0, v = brush_channel(40.0, 30.0, 0.1, 40, rho=0.7, seed=seed, max_fill=0.75)
     n_brush = s.n_mon * s.n_chain

@@ -126,35 +126,47 @@ struct RepDesc {
 };
 
 // ---------------------------------------------------------------------------------------------
-// Philox4x32-10 (Salmon et al., SC'11) keyed on the replica seed; counter (step, tag_lo, tag_hi).
+// Pair noise: Philox2x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter (min tag, max tag), key
+// pair_key(seed, step).  A pair needs two 32-bit words (two uniforms for one Box-Muller normal),
+// which is exactly one 2x32 block: half the multiplies of a 4x32 block, whose other two words
+// would go unused.
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
-                                              uint32_t k0, uint32_t k1) {
-  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+__device__ __forceinline__ void philox2x32_10(uint32_t& c0, uint32_t& c1, uint32_t k) {
+  const uint32_t M = 0xD256D193u, W = 0x9E3779B9u;
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
-    if (r > 0) { k0 += W0; k1 += W1; }
-    uint32_t hi0 = __umulhi(M0, c0), lo0 = M0 * c0;
-    uint32_t hi1 = __umulhi(M1, c2), lo1 = M1 * c2;
-    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    if (r > 0) k += W;
+    const uint32_t hi = __umulhi(M, c0), lo = M * c0;
+    c0 = hi ^ k ^ c1;
+    c1 = lo;
   }
 }
 
+// The step's key of a replica: the low 32 bits of the step XOR a 32-bit digest of the 64-bit
+// seed (the MurmurHash3 64-bit finalizer, low half).  For one replica the keys of two steps less
+// than 2^24 apart differ, and no step's round keys (key + r W, r < 10) are another step's shifted
+// by whole rounds: adding r W changes the top byte, which the step does not reach.
+__host__ __device__ __forceinline__ uint32_t pair_key(unsigned long long seed, long long step) {
+  unsigned long long h = seed;
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdULL;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ULL;
+  h ^= h >> 33;
+  return (uint32_t)h ^ (uint32_t)(unsigned long long)step;
+}
+
 // Two 23-bit uniforms of the unordered pair (ta, tb): u1 in (0,1), u2 in [0,1), exact in FP32.
-__device__ __forceinline__ void pair_uniform_bits(unsigned long long seed, long long step, int ta, int tb,
-                                                  uint32_t& b1, uint32_t& b2) {
-  uint32_t lo = (uint32_t)min(ta, tb), hi = (uint32_t)max(ta, tb);
-  uint32_t c0 = (uint32_t)(unsigned long long)step, c1 = (uint32_t)((unsigned long long)step >> 32);
-  uint32_t c2 = lo, c3 = hi;
-  philox4x32_10(c0, c1, c2, c3, (uint32_t)seed, (uint32_t)(seed >> 32));
+__device__ __forceinline__ void pair_uniform_bits(uint32_t key, int ta, int tb, uint32_t& b1, uint32_t& b2) {
+  uint32_t c0 = (uint32_t)min(ta, tb), c1 = (uint32_t)max(ta, tb);
+  philox2x32_10(c0, c1, key);
   b1 = c0 >> 9;
   b2 = c1 >> 9;
 }
 
-__device__ __forceinline__ float pair_gauss_f(unsigned long long seed, long long step, int ta, int tb) {
+__device__ __forceinline__ float pair_gauss_f(uint32_t key, int ta, int tb) {
   uint32_t b1, b2;
-  pair_uniform_bits(seed, step, ta, tb, b1, b2);
+  pair_uniform_bits(key, ta, tb, b1, b2);
   // b1, b2 < 2^23: 2^23 + b is exact in FP32, so the subtraction converts without an I2F
   const float f1 = __uint_as_float(0x4B000000u | b1) - 8388608.0f;
   const float f2 = __uint_as_float(0x4B000000u | b2) - 8388608.0f;
@@ -167,9 +179,9 @@ __device__ __forceinline__ float pair_gauss_f(unsigned long long seed, long long
   return sqrtf(-2.0f * logf(u1)) * c;
 }
 
-__device__ __forceinline__ double pair_gauss_d(unsigned long long seed, long long step, int ta, int tb) {
+__device__ __forceinline__ double pair_gauss_d(uint32_t key, int ta, int tb) {
   uint32_t b1, b2;
-  pair_uniform_bits(seed, step, ta, tb, b1, b2);
+  pair_uniform_bits(key, ta, tb, b1, b2);
   double u1 = ((double)b1 + 0.5) * (1.0 / 8388608.0);
   double u2 = (double)b2 * (1.0 / 8388608.0);
   return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);

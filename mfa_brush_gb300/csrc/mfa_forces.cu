@@ -378,7 +378,7 @@ __device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimCon
                                                  const PairEntry<real_t<MIXED>>& e, real_t<MIXED> dx,
                                                  real_t<MIXED> dy, real_t<MIXED> dz, int wj, int j,
                                                  real_t<MIXED> vix, real_t<MIXED> viy, real_t<MIXED> viz, int tag_i,
-                                                 int p0, unsigned long long seed, long long step, real_t<MIXED> r2min,
+                                                 int p0, uint32_t nkey, real_t<MIXED> r2min,
                                                  real_t<MIXED> half, real_t<MIXED>& e_lj, real_t<MIXED>& e_c) {
   using real = real_t<MIXED>;
   (void)wj;
@@ -429,8 +429,8 @@ __device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimCon
       wd = wr * wr;
     }
     real g;
-    if constexpr (MIXED) g = pair_gauss_f(seed, step, tag_i, tag_j);
-    else g = pair_gauss_d(seed, step, tag_i, tag_j);
+    if constexpr (MIXED) g = pair_gauss_f(nkey, tag_i, tag_j);
+    else g = pair_gauss_d(nkey, tag_i, tag_j);
     const real rdot = ((vix - vjx) * dx + (viy - vjy) * dy + (viz - vjz) * dz) * ir;
     fs += (sig * wr * g - gam * wd * rdot) * ir;
   }
@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
       tag_i = (int)__double_as_longlong(v4.w) - p0;
     }
     const double L0 = R.L[0], L1 = R.L[1], iL0 = R.invL[0], iL1 = R.invL[1];
-    const unsigned long long seed = R.seed;
+    const uint32_t nkey = pair_key(R.seed, step);  // the replica's noise key of this step
     const int* __restrict__ nb = s.nbr + i;
     auto delta = [&](int j, real& dx, real& dy, real& dz) -> int {
       if constexpr (MIXED) {
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
         const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
         // half of each mobile pair (both ends sum it); a fixed wall bead has no list of its own
         const real half = info_mobile(wj) ? (real)0.5 : (real)1;
-        const real fs = pair_fs<MIXED, EFLAG>(s, C, e, dx, dy, dz, wj, j, vix, viy, viz, tag_i, p0, seed, step,
+        const real fs = pair_fs<MIXED, EFLAG>(s, C, e, dx, dy, dz, wj, j, vix, viy, viz, tag_i, p0, nkey,
                                               r2min, half, e_lj, e_c);
         if constexpr (MIXED) {  // unmerged products and sums: alike with and without energies
           fx = __fadd_rn(fx, __fmul_rn(fs, dx));

@@ -11,7 +11,7 @@
  * Deliberate differences from the Fortran, each behind a switch or documented:
  *   - DPD noise: the reference draws g ~ N(0,1) from a serial or wall-clock-seeded ziggurat
  *     (dpd_forces.f90:29-33), which cannot be reproduced.  Here g is a Box-Muller normal from a
- *     Philox4x32-10 stream keyed on (replica seed, step, min(tag), max(tag)), the same stream the
+ *     Philox2x32-10 stream keyed on (replica seed, step, min(tag), max(tag)), the same stream the
  *     CUDA product uses, so DPD-on parity is deterministic against this oracle.
  *   - Cell index clamping: get_cell (cell_list.f90:186-213) indexes out of range for a particle
  *     exactly on the upper box face or outside the channel; here the per-axis index is clamped.
@@ -51,36 +51,47 @@ static inline double ipow(double x, int n) {
 }
 
 /* ------------------------------------------------------------------------------------------
- * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and a Box-Muller normal.
+ * Philox2x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and a Box-Muller normal.
  * ---------------------------------------------------------------------------------------- */
-static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
-  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+static void philox2x32_10(uint32_t c[2], uint32_t k) {
+  const uint32_t M = 0xD256D193u, W = 0x9E3779B9u;
   for (int r = 0; r < 10; ++r) {
-    if (r > 0) { k0 += W0; k1 += W1; }
-    uint64_t p0 = (uint64_t)M0 * c[0];
-    uint64_t p1 = (uint64_t)M1 * c[2];
-    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
-    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    if (r > 0) k += W;
+    uint64_t p = (uint64_t)M * c[0];
+    uint32_t hi = (uint32_t)(p >> 32), lo = (uint32_t)p;
+    c[0] = hi ^ k ^ c[1];
+    c[1] = lo;
   }
 }
 
-/* Unit normal for the unordered pair (ta, tb) at `step`.  u1 in (0,1) and u2 in [0,1) are
- * exact multiples of 2^-23 so FP32 and FP64 consumers see the same uniforms. */
+/* Key of (replica seed, step): the low 32 bits of the step XOR the low half of the MurmurHash3
+ * 64-bit finalizer of the seed. */
+uint32_t orc_pair_key(uint64_t seed, int64_t step) {
+  uint64_t h = seed;
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdULL;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ULL;
+  h ^= h >> 33;
+  return (uint32_t)h ^ (uint32_t)(uint64_t)step;
+}
+
+/* Unit normal for the unordered pair (ta, tb) at `step`: counter (min tag, max tag), key
+ * orc_pair_key(seed, step).  u1 in (0,1) and u2 in [0,1) are exact multiples of 2^-23 so FP32
+ * and FP64 consumers see the same uniforms. */
 double orc_pair_gauss(uint64_t seed, int64_t step, int32_t ta, int32_t tb) {
-  uint32_t lo = (uint32_t)(ta < tb ? ta : tb), hi = (uint32_t)(ta < tb ? tb : ta);
-  uint32_t c[4] = {(uint32_t)(uint64_t)step, (uint32_t)((uint64_t)step >> 32), lo, hi};
-  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  uint32_t c[2] = {(uint32_t)(ta < tb ? ta : tb), (uint32_t)(ta < tb ? tb : ta)};
+  philox2x32_10(c, orc_pair_key(seed, step));
   double u1 = ((double)(c[0] >> 9) + 0.5) * (1.0 / 8388608.0);
   double u2 = (double)(c[1] >> 9) * (1.0 / 8388608.0);
   return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
 }
 
-void orc_philox(uint64_t seed, int64_t step, uint32_t a, uint32_t b, uint32_t* out4) {
-  uint32_t c[4] = {(uint32_t)(uint64_t)step, (uint32_t)((uint64_t)step >> 32), a, b};
-  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-  memcpy(out4, c, 16);
+/* The raw block: counter (c0, c1), key k. */
+void orc_philox2x32(uint32_t c0, uint32_t c1, uint32_t k, uint32_t* out2) {
+  uint32_t c[2] = {c0, c1};
+  philox2x32_10(c, k);
+  memcpy(out2, c, 8);
 }
 
 /* ------------------------------------------------------------------------------------------

@@ -71,7 +71,8 @@ def lib():
             "orc_get_energies": (None, [vp, dp]),
             "orc_observe": (None, [vp, dp]),
             "orc_pair_gauss": (C.c_double, [C.c_uint64, C.c_int64, C.c_int32, C.c_int32]),
-            "orc_philox": (None, [C.c_uint64, C.c_int64, C.c_uint32, C.c_uint32, P(C.c_uint32)]),
+            "orc_philox2x32": (None, [C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_uint32)]),
+            "orc_pair_key": (C.c_uint32, [C.c_uint64, C.c_int64]),
             "orc_track_force_scale": (None, [vp, C.c_int]),
             "orc_get_force_scale": (None, [vp, dp]),
             "orc_get_virial": (None, [vp, dp]),

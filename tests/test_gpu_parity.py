@@ -200,11 +200,12 @@ def test_batched_replicas_equal_single(gpu, precision):
     """A replica inside a batch gets a bit-identical trajectory to the same replica run alone,
     rebuilds included: each replica is rebuilt when its own particles have moved half the skin
     (check_skin.f90 decides per system), so its sort order and lists do not depend on the others.
-    The cold replica (velocities scaled by 0.1) is rebuilt less often than the others."""
+    The cold replica (solvent on a lattice of spacing > 2^(1/6), so no potential energy to
+    release, velocities scaled by 0.1) is rebuilt less often than the others."""
     p = configs.wca_params(gamma=5.0)
     reps = [configs.brush_channel(15.0, 12.0, 0.2, 20, seed=11),
             configs.brush_channel(18.0, 15.0, 0.1, 35, seed=12),
-            configs.brush_channel(16.0, 10.0, 0.05, 50, seed=13)]
+            configs.brush_channel(16.0, 10.0, 0.0, 10, rho=0.35, a_max=1.25, seed=13)]
     s2, a2, r2, v2 = reps[2]
     reps[2] = (s2, a2, r2, v2 * 0.1)
     systems, a_type, r0, v = configs.concat(reps)

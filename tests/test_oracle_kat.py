@@ -66,18 +66,60 @@ def test_binning_boxes(try_deck):
 
 
 def test_philox_known_answers(oracle_mod):
-    """Philox4x32-10 known-answer vectors published with Random123 (Salmon et al. 2011)."""
+    """Philox2x32-10 known-answer vectors published with Random123 (Salmon et al. 2011):
+    counter (c0, c1), key k."""
     import ctypes as C
     L = oracle_mod.lib()
-    out = (C.c_uint32 * 4)()
-    # counter (c0,c1,c2,c3) = (step_lo, step_hi, a, b); key = (seed_lo, seed_hi)
-    L.orc_philox(0, 0, 0, 0, out)
-    assert list(out) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
-    L.orc_philox(0xFFFFFFFFFFFFFFFF, -1, 0xFFFFFFFF, 0xFFFFFFFF, out)
-    assert list(out) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
-    step = ((0x85A308D3 << 32) | 0x243F6A88) - (1 << 64)  # as a signed 64-bit counter
-    L.orc_philox(0x299F31D0A4093822, step, 0x13198A2E, 0x03707344, out)
-    assert list(out) == [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+    out = (C.c_uint32 * 2)()
+    L.orc_philox2x32(0, 0, 0, out)
+    assert list(out) == [0xFF1DAE59, 0x6CD10DF2]
+    L.orc_philox2x32(0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, out)
+    assert list(out) == [0x2C3F628B, 0xAB4FD7AD]
+
+
+def _philox2x32_np(c0, c1, k):
+    """Vectorised Philox2x32-10 (the published round function), for large-sample checks."""
+    M, W, m32 = np.uint64(0xD256D193), np.uint64(0x9E3779B9), np.uint64(0xFFFFFFFF)
+    c0, c1, k = c0.astype(np.uint64), c1.astype(np.uint64), np.uint64(k)
+    for r in range(10):
+        if r:
+            k = (k + W) & m32
+        p = M * c0
+        c0, c1 = (p >> np.uint64(32)) ^ k ^ c1, p & m32
+    return c0, c1
+
+
+def test_pair_noise_large_sample(oracle_mod):
+    """The pair noise over 10^6 draws for three counter patterns (neighbouring tags, a stride, a
+    block) and two keys: mean and variance of g within 5 standard errors, every used bit of both
+    words set half the time; the vectorised restatement equals orc_pair_gauss draw for draw."""
+    L = oracle_mod.lib()
+    n = 1_000_000
+    i = np.arange(n, dtype=np.uint64)
+    for seed, step in ((2024, 7), (0x9E3779B97F4A7C15, 123456)):
+        k = L.orc_pair_key(seed, step)
+        for a, b in ((i, i + 1), (i, i + 7), (i % 1000, i // 1000 + 1000)):
+            c0, c1 = _philox2x32_np(a, b, k)
+            u1 = ((c0 >> np.uint64(9)).astype(np.float64) + 0.5) / 8388608.0
+            u2 = (c1 >> np.uint64(9)).astype(np.float64) / 8388608.0
+            g = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+            for t in (0, 17, n - 1):
+                assert g[t] == oracle_mod.pair_gauss(seed, step, int(a[t]), int(b[t]))
+            assert abs(g.mean()) < 5.0 / np.sqrt(n)
+            assert abs(g.var() - 1.0) < 5.0 * np.sqrt(2.0 / n)
+            for w in (c0, c1):
+                f = np.array([((w >> np.uint64(j)) & np.uint64(1)).mean() for j in range(9, 32)])
+                assert np.abs(f - 0.5).max() < 5.0 * 0.5 / np.sqrt(n)
+
+
+def test_pair_key_distinct_over_steps(oracle_mod):
+    """A replica's noise keys of distinct steps differ (the step enters by XOR), and replicas with
+    consecutive seeds get unrelated keys (the seed is hashed)."""
+    L = oracle_mod.lib()
+    ks = [L.orc_pair_key(12345, t) for t in range(5000)]
+    assert len(set(ks)) == 5000
+    k0 = [L.orc_pair_key(s, 0) for s in range(64)]
+    assert len(set(k >> 24 for k in k0)) > 32
 
 
 def test_pair_gauss_is_symmetric_and_normal(oracle_mod):
