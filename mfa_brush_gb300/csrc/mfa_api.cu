@@ -467,6 +467,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   C.dt = p->dt;
   C.va_wall[0] = p->va_wall[0];
   C.va_wall[1] = p->va_wall[1];
+  C.move_walls = F.wall == 1 && (p->va_wall[0] != 0. || p->va_wall[1] != 0.);
   C.half_dt = 0.5 * p->dt;
   C.half_dt2 = 0.5 * (p->dt * p->dt);
   for (int t = 0; t < MAXT; ++t) {

@@ -87,6 +87,7 @@ struct SimConst {
   double coul_rc2;                // own Coulomb cut-off^2 (0: inside LJ range)
   double skin_half2;              // (skin/2)^2
   double va_wall[2];              // head velocity of chains 1..n_chain/2 (the others: -va_wall)
+  int move_walls;                 // WALL 1 with va_wall != 0: the wall beads' sites move too
   int hist_dim;
   // FP32 copies for the mixed-precision integrator
   float dt_f, skin_half2_f, a_w_f;

@@ -689,6 +689,10 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
       if (active) {
         int_mixed_particle<2, EFLAG>(s, C, i, w, d2f_fast(fxd), d2f_fast(fyd), d2f_fast(fzd), s.pfx_alt, s.vf_alt,
                                      ike, ikin, ifh);
+      } else if (C.move_walls) {  // a wall bead on a moving wall: its next site
+        double x, y, z;
+        s.pfx_alt[i] = move_wall_bead(s, C, i, w, x, y, z);
+        s.vf_alt[i] = s.vf[i];
       } else {  // a wall bead: its views as they are
         s.pfx_alt[i] = s.pfx[i];
         s.vf_alt[i] = s.vf[i];

@@ -421,9 +421,9 @@ int mfa_derive_params(const mfa_inputs* in, mfa_params* p, mfa_system* s) {
   p->hist_dim = in->hist_dim > 0 ? in->hist_dim : 200;
   if (in->va_spring_twall[0] != 0. || in->va_spring_twall[1] != 0. || in->va_spring_twall[2] != 0.) {
     // init_params.f90:899-907: moving walls with the body force is an inconsistency the reference
-    // stops on; with explicit walls the wall sites would move too (verlet_positions.f90:214-221),
-    // which is not built
-    if (F.poiseuille || F.wall == 1) return MFA_ERR_UNSUPPORTED;
+    // stops on.  With explicit walls the wall sites move too (verlet_positions.f90:214-221), in
+    // x and y; a z velocity would move them into the channel, which is not built.
+    if (F.poiseuille || (F.wall == 1 && in->va_spring_twall[2] != 0.)) return MFA_ERR_UNSUPPORTED;
     p->va_wall[0] = in->va_spring_twall[0];
     p->va_wall[1] = in->va_spring_twall[1];
   }

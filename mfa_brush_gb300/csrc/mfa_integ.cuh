@@ -19,6 +19,43 @@ __device__ __forceinline__ double wrap_bits(double x, double L, long long Lbits)
 // The update of one mobile particle i (info word w) in the mixed path, after its force (Fx, Fy, Fz)
 // for MODE >= 1; the views go to (pfx_out, vf_out).  Shared by k_int_mixed and by the pair kernel
 // that fuses MODE 2 into its tail, so both give the same bits.
+// verlet_positions.f90:214-247 (WALL 1 with a wall velocity): the sites of the first half of a
+// replica's wall beads move by +va_spring_twall dt per step and the other half by
+// -va_spring_twall dt, wrapped into [0, L) in x and y, and the beads sit on their sites.  Their
+// velocity stays 0 (the reference assigns the wall beads none).  Writes the FP64 position
+// (x, y, z out), returns the fixed-point view (w in .w) and raises the replica's rebuild flag
+// when the bead has moved half the skin since the last rebuild (the test rounded as the mobile
+// particles' test of the mixed path rounds it).  Shared by every position update, so all paths
+// move a wall bead by the same bits.
+__device__ __forceinline__ int4 move_wall_bead(const DevState& s, const SimConst& C, int i, int w, double& x,
+                                               double& y, double& z) {
+  const int rep = info_rep(w);
+  const RepDesc& R = s.reps[rep];
+  const bool first = s.tag[i] - R.p0 - R.n_mon_tot < (R.n_part - R.n_mon_tot) / 2;
+  // rounded as written (no contraction into an FMA): the oracle's additions, bit for bit
+  const double ddx = __dmul_rn(C.va_wall[0], C.dt), ddy = __dmul_rn(C.va_wall[1], C.dt);
+  x = s.rx[i];
+  y = s.ry[i];
+  z = s.rz[i];
+  x = first ? __dadd_rn(x, ddx) : __dsub_rn(x, ddx);
+  y = first ? __dadd_rn(y, ddy) : __dsub_rn(y, ddy);
+  if (x > R.L[0]) x -= R.L[0]; else if (x < 0.) x += R.L[0];
+  if (y > R.L[1]) y -= R.L[1]; else if (y < 0.) y += R.L[1];
+  s.rx[i] = x;
+  s.ry[i] = y;
+  int4 q;
+  q.x = to_fx_periodic(x, R.sfx[0]);
+  q.y = to_fx_periodic(y, R.sfx[1]);
+  q.z = to_fx_z(z, R.sfx[2]);
+  q.w = w;
+  const int4 q0 = s.ref[i];
+  const float dx = i2f_fast(fx_diff(q.x, q0.x)) * R.ufx_f[0];
+  const float dy = i2f_fast(fx_diff(q.y, q0.y)) * R.ufx_f[1];
+  const float dz = i2f_fast(fx_diff(q.z, q0.z)) * R.ufx_f[2];
+  if (__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))) > C.skin_half2_f) flag_rebuild(s, rep);
+  return q;
+}
+
 template <int MODE, bool EFLAG>
 __device__ __forceinline__ void int_mixed_particle(const DevState& s, const SimConst& C, int i, int w, float Fx,
                                                    float Fy, float Fz, int4* __restrict__ pfx_out,

@@ -118,6 +118,10 @@ __global__ void __launch_bounds__(256) k_integrate(DevState s, SimConst C, Acc a
       if (dx * dx + dy * dy + dz * dz > C.skin_half2_f) flag_rebuild(s, rep);
       if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(s.status, ST_NAN);
     }
+  } else if ((MODE == 0 || MODE == 2) && inside && C.move_walls) {  // a wall bead on a moving wall
+    double x, y, z;
+    int4 q = move_wall_bead(s, C, i, w, x, y, z);
+    store_views(s, i, s.reps[rep], x, y, z, 0., 0., 0., w, s.tag[i], q);
   }
   if (MODE >= 1 && i == 0) *s.steps_done += 1;
   if (EFLAG && MODE >= 1) {
@@ -169,6 +173,10 @@ __global__ void __launch_bounds__(256) k_int_mixed(DevState s, SimConst C, Acc a
       }
     }
     int_mixed_particle<MODE, EFLAG>(s, C, i, w, Fx, Fy, Fz, s.pfx, s.vf, ke, kin, fh);
+  } else if ((MODE == 0 || MODE == 2) && inside && C.move_walls) {  // a wall bead on a moving wall
+    double x, y, z;
+    s.pfx[i] = move_wall_bead(s, C, i, w, x, y, z);
+    if (MODE == 0 && s.sync_alt) s.vf[i] = s.vf_alt[i];
   } else if (MODE == 0 && inside && s.sync_alt) {
     s.pfx[i] = s.pfx_alt[i];  // a chunk that starts in the other view buffers: the wall beads' views
     s.vf[i] = s.vf_alt[i];

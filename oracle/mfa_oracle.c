@@ -261,9 +261,9 @@ int orc_derive_params(const mfa_inputs* in, mfa_params* p, mfa_system* s) {
   p->compat = in->compat;
   p->hist_dim = in->hist_dim > 0 ? in->hist_dim : 200;
   /* heads sheared with the walls (verlet_velocities.f90:111-124); refused with the body force
-     (init_params.f90:899-907) and with explicit walls (their sites would move too) */
+     (init_params.f90:899-907) and, with explicit walls (whose sites move too), for a z velocity */
   if (in->va_spring_twall[0] != 0. || in->va_spring_twall[1] != 0. || in->va_spring_twall[2] != 0.) {
-    if (f->poiseuille || f->wall == 1) return -2;
+    if (f->poiseuille || (f->wall == 1 && in->va_spring_twall[2] != 0.)) return -2;
     p->va_wall[0] = in->va_spring_twall[0];
     p->va_wall[1] = in->va_spring_twall[1];
   }
@@ -1310,6 +1310,25 @@ void orc_verlet_positions(orc_sys* o) {
     }
     update_part_cell(o, i, old_cell);
     for (int d = 0; d < 3; ++d) v[d] = v[d] + 0.5 * dt * a[d];
+  }
+  /* verlet_positions.f90:214-247 (WALL 1 with a wall velocity): the sites of wall beads
+     1..n_wall/2 move by +va_spring_twall dt, the others by -va_spring_twall dt, wrapped into
+     [0, L) in x and y, and the beads sit on their sites (their velocity stays 0).  Their cells
+     follow them here (the reference's linked cells hold the mobile particles only). */
+  if (o->p.flags.wall == 1 && (o->p.va_wall[0] != 0. || o->p.va_wall[1] != 0.)) {
+    const int n_wall = o->n - o->nm;
+    for (int k = 0; k < n_wall; ++k) {
+      const int i = o->nm + 1 + k;
+      double* r = &o->r0[3 * (i - 1)];
+      const int old_cell = get_cell(o, r);
+      for (int d = 0; d < 2; ++d) {
+        const double dd = o->p.va_wall[d] * dt;
+        r[d] = (k < n_wall / 2) ? r[d] + dd : r[d] - dd;
+        if (r[d] > L[d]) r[d] = r[d] - L[d];
+        else if (r[d] < 0.) r[d] = r[d] + L[d];
+      }
+      update_part_cell(o, i, old_cell);
+    }
   }
 }
 

@@ -632,3 +632,41 @@ def test_sheared_brushes_moving_heads(gpu, oracle_mod, precision):
     assert abs(eg["t_fluid"] - o.energies()["t_fluid"]) < (1e-9 if precision == "fp64" else 1e-5) * o.energies()["t_fluid"]
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_moving_explicit_walls(gpu, oracle_mod, precision):
+    """Couette with explicit walls (WALL 1, verlet_positions.f90:214-247): the sites of wall beads
+    1..n_wall/2 move by +va dt per step, the others by -va dt, and the heads move at +-va
+    (verlet_velocities.f90:111-124).  At va = 1 the walls pass half the skin within the run, so
+    the lists must be rebuilt for them.  60 md_main steps through the drop-ins (FP64) or the
+    fused step (mixed) against the oracle: the wall beads' positions bit for bit, the mobile
+    particles' within the usual tolerances."""
+    inp = configs.wca_inputs(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    inp.va_spring_twall[0], inp.va_spring_twall[1] = 1.0, -0.5
+    p, _ = md.derive(inp)
+    s, a_type, r0, v = configs.explicit_wall_channel(seed=8)
+    g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
+    o = oracle_mod.Oracle(p, s, a_type, r0, v)
+    n = 60
+    assert n * p.dt * 1.0 > 0.5 * g.options_in_use().skin
+    if precision == "fp64":
+        for _ in range(n):
+            g.md_step()
+    else:
+        g.step(n)
+    o.step(n, 1, 0)
+    r, vv, _, _ = g.state()
+    ro, vo, _, _ = o.state()
+    nm = s.n_mon_tot
+    assert np.array_equal(r[nm:], ro[nm:])
+    assert np.all(vv[nm:] == 0.0)
+    L = np.array(list(s.boundary))
+    d = r[:nm] - ro[:nm]
+    d[:, :2] -= L[:2] * np.round(d[:, :2] / L[:2])
+    assert np.abs(d).max() < (1e-8 if precision == "fp64" else 1e-5)
+    tol = 1e-6 if precision == "fp64" else 1e-3
+    assert np.abs(vv[:nm] - vo[:nm]).max() < tol * max(1.0, np.sqrt(np.mean(vo[:nm] ** 2)))
+    assert g.replica_rebuild_counts()[0] >= 1
+    g.close()
+    o.close()

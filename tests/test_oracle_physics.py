@@ -224,7 +224,7 @@ def test_ewald_virial_is_minus_the_strain_derivative(oracle_mod):
 def test_sheared_heads_and_refusals(oracle_mod):
     """The wall velocity of the brush-brush shear reaches the tables of both derivations; the
     oracle moves the heads at +-va_wall; a moving wall is refused with the body force
-    (init_params.f90:899-907) and with explicit walls."""
+    (init_params.f90:899-907) and, with explicit walls, for a z velocity."""
     import numpy as np
     from mfa_brush_gb300 import abi, configs, md
     inp = configs.wca_inputs(gamma=5.0, kT=1.0, dt=0.005)
@@ -240,10 +240,45 @@ def test_sheared_heads_and_refusals(oracle_mod):
     sg = np.where(np.arange(s.n_chain) < s.n_chain // 2, 1.0, -1.0)
     assert np.array_equal(vv[heads, 0], 0.25 * sg) and np.array_equal(vv[heads, 1], 0.5 * sg)
     o.close()
-    for flag in ("poiseuille", "wall1"):
-        bad = configs.wca_inputs(gamma=5.0, wall=1 if flag == "wall1" else 2)
+    for flag in ("poiseuille", "wall1_z"):
+        bad = configs.wca_inputs(gamma=5.0, wall=1 if flag == "wall1_z" else 2)
         bad.va_spring_twall[0] = 0.1
         if flag == "poiseuille":
             bad.flags.poiseuille = 1
+        else:
+            bad.va_spring_twall[2] = 0.1
         with pytest.raises(abi.MfaError):
             md.derive(bad)
+
+
+def test_moving_explicit_walls_oracle(oracle_mod):
+    """WALL 1 with a wall velocity (verlet_positions.f90:214-247): after n steps the oracle's
+    wall beads 1..n_wall/2 sit at x0 + n va dt and the others at x0 - n va dt (wrapped), z
+    unchanged; the heads move at +-va_wall."""
+    import numpy as np
+    from mfa_brush_gb300 import configs, md
+    inp = configs.wca_inputs(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    inp.va_spring_twall[0], inp.va_spring_twall[1] = 0.5, -0.25
+    p, _ = md.derive(inp)
+    po, _ = oracle_mod.derive_params(inp)
+    assert tuple(po.va_wall) == (0.5, -0.25)
+    s, a_type, r0, v = configs.explicit_wall_channel(seed=3)
+    o = oracle_mod.Oracle(po, s, a_type, r0, v)
+    n = 7
+    o.step(n, 1, 0)
+    r, vv = o.state()[:2]
+    o.close()
+    nm, nw = s.n_mon_tot, s.n_part - s.n_mon_tot
+    L = np.array(list(s.boundary))
+    sg = np.where(np.arange(nw) < nw // 2, 1.0, -1.0)
+    for d, va in ((0, 0.5), (1, -0.25)):
+        x = r0[nm:, d].copy()
+        for _ in range(n):  # the same additions and wraps as the position update
+            x = np.where(sg > 0, x + va * po.dt, x - va * po.dt)
+            x = np.where(x > L[d], x - L[d], np.where(x < 0.0, x + L[d], x))
+        assert np.array_equal(r[nm:, d], x)
+    assert np.array_equal(r[nm:, 2], r0[nm:, 2])
+    assert np.all(vv[nm:] == 0.0)
+    heads = np.arange(s.n_chain) * s.n_mon
+    hs = np.where(np.arange(s.n_chain) < s.n_chain // 2, 1.0, -1.0)
+    assert np.array_equal(vv[heads, 0], 0.5 * hs) and np.array_equal(vv[heads, 1], -0.25 * hs)
