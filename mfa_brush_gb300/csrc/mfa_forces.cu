@@ -365,9 +365,11 @@ __global__ void __launch_bounds__(128) k_bonded(DevState s, SimConst C, int mask
 // kept pairs per batch (a thread screens its list until it has this many, then they are evaluated),
 // and list entries screened per group (their loads are all in flight at once).  Measured on 256
 // brush replicas (4.66 M particles, skin 0.5): groups of 2 / 3 / 4 / 8 entries gave a pair kernel
-// of 0.574 / 0.582 / 0.583 / 0.648 ms with the evaluation loop not unrolled, batches of 12 / 16 /
-// 20 kept pairs the same within 0.1 %; unrolling the evaluation loop by 2 or 4 cost 4 % or 20 %.
-constexpr int PAIR_BATCH = 16;
+// of 0.574 / 0.582 / 0.583 / 0.648 ms with the evaluation loop not unrolled; unrolling it by 2 or
+// 4 cost 4 % or 20 %.  With the batch in shared memory, the kernel with the integration in its
+// tail took 0.598 / 0.586 / 0.586 / 0.588 / 0.597 / 0.607 ms at batches of 8 / 10 / 12 / 16 /
+// 24 / 32 (groups of 2; 12 with groups of 4: 0.585).
+constexpr int PAIR_BATCH = 12;
 constexpr int PAIR_G = 2;
 
 // Force factor fs of the pair (i, j) along d = r_i - r_j (LJ with the switch-on clamp, DPD with the
@@ -584,7 +586,11 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
     // pair, i.e. on almost every list entry.
     constexpr int BATCH = PAIR_BATCH;
     constexpr int G = PAIR_G;  // list entries screened per group: their loads are all in flight at once
-    int jl[BATCH];
+    // the batch's kept entries in shared memory, a column per thread (conflict-free): a
+    // dynamically indexed local array lives in local memory, whose loads missed L1 behind the
+    // gathers
+    __shared__ int jls[BATCH * 128];
+    int* const jl = jls + threadIdx.x;
     int k = 0;
     // screening against the largest cut-off of the type pair; MIXED uses the coarse conversion
     // (512 fixed-point units of resolution, inside the 2e-4 margin of screen2)
@@ -621,7 +627,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
         for (int u = 0; u < G; ++u) hg[u] = screen(jg[u]);
 #pragma unroll
         for (int u = 0; u < G; ++u)
-          if (hg[u]) jl[m++] = jg[u];
+          if (hg[u]) jl[128 * m++] = jg[u];
         k += G;
 #pragma unroll
         for (int u = 0; u < G; ++u) jg[u] = jn[u];
@@ -629,11 +635,11 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
       while (k < n && m < BATCH) {
         const int j = __ldg(nb + (size_t)k * s.Np);
         ++k;
-        if (screen(j)) jl[m++] = j;
+        if (screen(j)) jl[128 * m++] = j;
       }
 #pragma unroll 1
       for (int t = 0; t < m; ++t) {
-        const int j = jl[t];
+        const int j = jl[128 * t];
         real dx, dy, dz;
         const int wj = delta(j, dx, dy, dz);
         const PairEntry<real>& e = tab[ti * MAXT + info_type(wj)];
