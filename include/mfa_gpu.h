@@ -155,8 +155,10 @@ typedef struct mfa_params {
   int32_t hist_dim;
   double va_wall[2];        /* x, y velocity of the heads of chains 1..n_chain/2, the other heads
                                moving at -va_wall (verlet_velocities.f90:111-124: the two brushes
-                               sheared against each other); mfa_inputs.va_spring_twall(1:2).  0
-                               without shear; the reference stops on a non-zero value with
+                               sheared against each other); with explicit walls (WALL 1) also the
+                               sites of wall beads 1..n_wall/2 (the others at -va_wall,
+                               verlet_positions.f90:214-247); mfa_inputs.va_spring_twall(1:2).
+                               0 without shear; the reference stops on a non-zero value with
                                POISEUILLE (init_params.f90:899-907)                             */
 } mfa_params;
 
