@@ -319,6 +319,15 @@ __global__ void k_place(DevState s) {
   }
 }
 
+// compare-exchange of (tag, slot) pairs by tag
+__device__ __forceinline__ void cmpx(int (&t)[8], int (&p)[8], int i, int j) {
+  if (t[j] < t[i]) {
+    const int u = t[i], q = p[i];
+    t[i] = t[j]; p[i] = p[j];
+    t[j] = u; p[j] = q;
+  }
+}
+
 __global__ void k_sort_cells(DevState s) {
   WL_FOR(wl_c, g) {
   int r, lc;
@@ -326,6 +335,29 @@ __global__ void k_sort_cells(DevState s) {
   const int c = s.reps[r].cell_off + lc;
   int b = s.cell_start[c], n = s.cell_count[c];
   s.cell_count[c] = 0;  // the last reader of the count: zero again for the next rebuild's k_bin
+  if (n <= 1) continue;
+  if (n <= 8) {
+    // a cell of up to 8: all its slots and tags loaded at once (two dependent loads, not a chain
+    // per element), sorted in registers by a fixed network (Batcher's odd-even merge for 8, its
+    // 4-input form for up to 4) with the unused places padded by the largest tag
+    int p[8], t[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) p[k] = k < n ? s.perm[b + k] : 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t[k] = k < n ? s.tag[p[k]] : 0x7fffffff;
+    cmpx(t, p, 0, 1); cmpx(t, p, 2, 3); cmpx(t, p, 0, 2); cmpx(t, p, 1, 3); cmpx(t, p, 1, 2);
+    if (n > 4) {
+      cmpx(t, p, 4, 5); cmpx(t, p, 6, 7); cmpx(t, p, 4, 6); cmpx(t, p, 5, 7); cmpx(t, p, 5, 6);
+      // merge of the two sorted halves
+      cmpx(t, p, 0, 4); cmpx(t, p, 1, 5); cmpx(t, p, 2, 6); cmpx(t, p, 3, 7);
+      cmpx(t, p, 2, 4); cmpx(t, p, 3, 5);
+      cmpx(t, p, 1, 2); cmpx(t, p, 3, 4); cmpx(t, p, 5, 6);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k < n) s.perm[b + k] = p[k];
+    continue;
+  }
   for (int k = 1; k < n; ++k) {  // insertion sort by tag
     int p = s.perm[b + k];
     int t = s.tag[p];
