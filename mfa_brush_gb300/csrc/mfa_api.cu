@@ -730,6 +730,7 @@ int mfa_batch_init(const mfa_params* p, int32_t n_rep, const mfa_system* sysv, c
   DA(S.rebuild_flag, 1 + n_rep);
   DA(S.steps_alt, 1);
   S.sync_alt = 0;
+  S.permute_accel = 1;
   DA(S.pair_q, 2);
   DA(S.wl_rep, n_rep + 1);
   DA(S.wl_p, n_rep + 1);
@@ -1175,15 +1176,17 @@ static long long issue_steps(mfa_ctx* ctx, int n, int phase, bool prof, bool obs
   for (int k = 1; k <= n; ++k) {
     const DevState& S = sets[cur];
     const bool ef = energies_at(k);
+    DevState Sr = S;  // the step's rebuild leaves the (dead) accelerations of mobile particles behind
+    Sr.permute_accel = 0;
     if (capturing) {
-      int r = capture_conditional_rebuild(ctx, S);
+      int r = capture_conditional_rebuild(ctx, Sr);
       if (r != MFA_OK) {
         *err = r;
         return L;
       }
       L += 1;  // the rebuild body's launches are not counted: they run only when triggered
     } else {
-      launch_rebuild(S, st, false);
+      launch_rebuild(Sr, st, false);
       L += kRebuildLaunches;
     }
     const bool split = prof || (obs && ef);
@@ -1708,7 +1711,9 @@ int mfa_kernel_times(mfa_ctx* ctx, int32_t nsteps, float* mean_ms, int32_t* laun
     const bool ef = (k == nsteps);
     const DevState& Sk = sets[cur];
     // the rebuild as the fused step runs it: the replicas whose skin test fired, if any
-    launch_rebuild(Sk, st, false);
+    DevState Sr = Sk;
+    Sr.permute_accel = 0;
+    launch_rebuild(Sr, st, false);
     mark(0);
     if (ctx->fuse_integ && !ef) {
       launch_pair(Sk, C, st, false, false, acc, ctx->opt.block_size, mask, true);

@@ -383,11 +383,14 @@ __global__ void k_permute(DevState s) {
   s.tmp[3][i] = s.vx[o];
   s.tmp[4][i] = s.vy[o];
   s.tmp[5][i] = s.vz[o];
-  s.tmp[6][i] = s.ax[o];
-  s.tmp[7][i] = s.ay[o];
-  s.tmp[8][i] = s.az[o];
+  const int wo = s.info[o];
+  if (s.permute_accel || !info_mobile(wo)) {
+    s.tmp[6][i] = s.ax[o];
+    s.tmp[7][i] = s.ay[o];
+    s.tmp[8][i] = s.az[o];
+  }
   s.tmp_tag[i] = s.tag[o];
-  s.tmp_info[i] = s.info[o];
+  s.tmp_info[i] = wo;
   }
 }
 
@@ -418,8 +421,10 @@ __global__ void k_copyback(DevState s) {
   double vx = s.tmp[3][i], vy = s.tmp[4][i], vz = s.tmp[5][i];
   s.rx[i] = x; s.ry[i] = y; s.rz[i] = z;
   s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
-  s.ax[i] = s.tmp[6][i]; s.ay[i] = s.tmp[7][i]; s.az[i] = s.tmp[8][i];
   int t = s.tmp_tag[i], w = s.tmp_info[i];
+  if (s.permute_accel || !info_mobile(w)) {
+    s.ax[i] = s.tmp[6][i]; s.ay[i] = s.tmp[7][i]; s.az[i] = s.tmp[8][i];
+  }
   s.tag[i] = t;
   s.info[i] = w;
   s.slot_of_tag[t] = i;

@@ -30,6 +30,10 @@ struct DevState {
   long long* steps_alt;
   int sync_alt;  // 1: the position update that starts a chunk also copies the wall beads' views and
                  // the step counter from the other set into this one
+  int permute_accel;  // 1: a rebuild carries the mobile particles' FP64 accelerations into the new
+                      // order.  0 for the rebuilds inside mfa_step: there the accelerations are
+                      // dead from the call's first position update to its last velocity update,
+                      // which rewrites them (the wall beads' are carried either way)
   dbl4* pd;
   dbl4* vd;
   int4* ref;   // fixed-point position at the last rebuild
