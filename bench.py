@@ -47,16 +47,18 @@ PAIR_BYTES = {"mixed": 16 + 16 + 16, "fp64": 32 + 32 + 24}
 PAIR_INTEG_BYTES = 16 + 16 + 4 + 4 + 48 + 48 + 16 + 16 + 16
 
 
-def profiled_traffic(precision, n_atoms, skin):
+def profiled_traffic(precision, n_atoms, skin, separate=False):
     """DRAM bytes of one pair-kernel launch, scaled to n_atoms from the committed ncu summary
     (profiles/k_pair_<precision>_brush_replicas.md): the `traffic_bytes_per_particle_skin_S:`
-    line of the profiled skin nearest to `skin`, else `traffic_bytes_per_particle:`.
+    line of the profiled skin nearest to `skin` (`traffic_separate_bytes_per_particle_skin_S:` for
+    the kernel without the integration), else `traffic_bytes_per_particle:`.
     Returns (bytes, the skin of the profile or None)."""
     per_skin, default = {}, None
+    key = "traffic_separate_bytes_per_particle_skin_" if separate else "traffic_bytes_per_particle_skin_"
     try:
         with open(os.path.join(ROOT, "profiles", "k_pair_%s_brush_replicas.md" % precision)) as f:
             for ln in f:
-                if ln.startswith("traffic_bytes_per_particle_skin_"):
+                if ln.startswith(key):
                     k, val = ln.split(":")
                     per_skin[float(k.rsplit("_", 1)[1])] = float(val)
                 elif ln.startswith("traffic_bytes_per_particle:"):
@@ -488,7 +490,8 @@ def main():
     pair_bytes = (n_fused * PAIR_INTEG_BYTES + (args.kernel_steps - n_fused) * PAIR_BYTES[args.precision]) \
         / args.kernel_steps
     achieved = pair_bytes * n_atoms / t_pair / 1e9 if t_pair > 0 else 0.0
-    traffic, traffic_skin = profiled_traffic(args.precision, n_atoms, args.skin)
+    traffic, traffic_skin = profiled_traffic(args.precision, n_atoms, args.skin,
+                                             separate=args.precision == "mixed" and not fused)
 
     # end-to-end through the C ABI with pinned host buffers
     e2e = None
