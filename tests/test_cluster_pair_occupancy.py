@@ -20,7 +20,6 @@ near one per pair, the count that made evaluating each pair once slower than the
 import os
 
 import numpy as np
-import pytest
 from scipy.spatial import cKDTree
 
 from mfa_brush_gb300 import configs
@@ -113,5 +112,19 @@ def test_cluster_pairs_in_a_melt(oracle_mod):
     for M in (4, 8):
         st = cluster_pair_stats(r, L, M, 2.0 * RC_WCA)
         print("melt", {k: round(v, 3) if isinstance(v, float) else v for k, v in st.items()})
+        assert st["occupancy"] < 0.25
+        assert st["list_entries_per_pair"] < 2.5
+
+
+def test_cluster_pairs_in_two_liquids(oracle_mod):
+    """A 20 x 20 x 16 two-liquid channel (brushes, liquids A and B layered, 5,120 particles); every
+    pair counted at the liquids' 2 x 2^(1/6) cut-off (an upper bound, as for the melt)."""
+    from mfa_brush_gb300 import md
+    p, _ = md.derive(configs.two_liquid_inputs(f_x=0.01))
+    sysm = configs.two_liquid_channel(L=20.0, D=16.0, seed=5)
+    r, L = _relaxed(oracle_mod, p, sysm)
+    for M in (4, 8):
+        st = cluster_pair_stats(r, L, M, 2.0 * RC_WCA)
+        print("two liquids", {k: round(v, 3) if isinstance(v, float) else v for k, v in st.items()})
         assert st["occupancy"] < 0.25
         assert st["list_entries_per_pair"] < 2.5
