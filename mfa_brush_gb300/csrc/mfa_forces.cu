@@ -79,8 +79,9 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
 // One angle term of bending.f90:47-109 with r_prev = r_c - r_{c-1}, r_next = r_{c+1} - r_c.
-// fa acts on c-1, fc on c+1 (c gets -fa-fc).  MIXED computes the angle as atan2(|p x n|, p.n),
-// which keeps FP32 accurate for the nearly straight chains that stiff brushes produce.
+// fa acts on c-1, fc on c+1 (c gets -fa-fc).  MIXED takes the angle's sine and cosine from
+// |p x n| and p.n (the harmonic form its angle as atan2(|p x n|, p.n)), which keeps FP32
+// accurate for the nearly straight chains that stiff brushes produce.
 template <bool MIXED>
 __device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, const SimConst& C, real_t<MIXED> kb,
                           real_t<MIXED> aeq, real_t<MIXED>* fa, real_t<MIXED>* fc, real_t<MIXED>& e) {
@@ -126,24 +127,35 @@ __device__ void bend_term(const real_t<MIXED>* rp, const real_t<MIXED>* rn, cons
 #pragma unroll
     for (int j = 0; j < 3; ++j) dp[j] *= sc;
   }
-  real alpha;
+  real fm;
   if constexpr (MIXED) {
     real cx = rp[1] * rn[2] - rp[2] * rn[1];
     real cy = rp[2] * rn[0] - rp[0] * rn[2];
     real cz = rp[0] * rn[1] - rp[1] * rn[0];
-    alpha = atan2f(sqrtf(cx * cx + cy * cy + cz * cz), dot);
+    const real cr = sqrtf(cx * cx + cy * cy + cz * cz);
+    if (C.bend_form == 1) {
+      // the cosine form needs sin(alpha) and cos(alpha) only: |p x n| / (|p| |n|) and
+      // p.n / (|p| |n|), with no angle and no library sine (the force then takes the same
+      // operations whether or not the energy is formed)
+      const real inv = (real)1 / (srp * srn);
+      fm = kb * (cr * inv);
+      e = kb * ((real)1 - dot * inv);
+    } else {
+      const real da = atan2f(cr, dot) - aeq;
+      fm = kb * da;
+      e = (real)0.5 * fm * da;
+    }
   } else {
     real ca = dot / sqrt(rp2 * rn2);
-    alpha = (ca >= 1.0) ? aeq : acos(ca);  // bending.f90:93-98 guard: delta_alpha = 0
-  }
-  real fm;
-  if (C.bend_form == 1) {
-    fm = kb * sin(alpha);
-    e = kb * ((real)1 - cos(alpha));
-  } else {
-    real da = alpha - aeq;
-    fm = kb * da;
-    e = (real)0.5 * fm * da;
+    const real alpha = (ca >= 1.0) ? aeq : acos(ca);  // bending.f90:93-98 guard: delta_alpha = 0
+    if (C.bend_form == 1) {
+      fm = kb * sin(alpha);
+      e = kb * ((real)1 - cos(alpha));
+    } else {
+      real da = alpha - aeq;
+      fm = kb * da;
+      e = (real)0.5 * fm * da;
+    }
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
