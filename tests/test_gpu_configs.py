@@ -634,23 +634,25 @@ def test_sheared_brushes_moving_heads(gpu, oracle_mod, precision):
     o.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fused", "mixed"])
 def test_moving_explicit_walls(gpu, oracle_mod, precision):
     """Couette with explicit walls (WALL 1, verlet_positions.f90:214-247): the sites of wall beads
     1..n_wall/2 move by +va dt per step, the others by -va dt, and the heads move at +-va
     (verlet_velocities.f90:111-124).  At va = 1 the walls pass half the skin within the run, so
     the lists must be rebuilt for them.  60 md_main steps through the drop-ins (FP64) or the
-    fused step (mixed) against the oracle: the wall beads' positions bit for bit, the mobile
-    particles' within the usual tolerances."""
+    fused step (mixed, and FP64 through its fused integrator) against the oracle: the wall beads'
+    positions bit for bit, the mobile particles' within the usual tolerances."""
     inp = configs.wca_inputs(gamma=5.0, wall=1, dpd_cut_off=1.0)
     inp.va_spring_twall[0], inp.va_spring_twall[1] = 1.0, -0.5
     p, _ = md.derive(inp)
     s, a_type, r0, v = configs.explicit_wall_channel(seed=8)
+    fused = precision == "fp64_fused"
+    precision = "fp64" if fused else precision
     g = md.MdSystem(p, s, a_type, r0, v, precision=precision)
     o = oracle_mod.Oracle(p, s, a_type, r0, v)
     n = 60
     assert n * p.dt * 1.0 > 0.5 * g.options_in_use().skin
-    if precision == "fp64":
+    if precision == "fp64" and not fused:
         for _ in range(n):
             g.md_step()
     else:
