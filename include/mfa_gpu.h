@@ -373,6 +373,8 @@ int mfa_get_options(mfa_ctx* ctx, mfa_options* out);
    (ewald_k.f90:47-124) and charged particles; both 0 for an uncharged context.  Each replica of a
    charged batch has its own k-set, built from its own box.                                    */
 int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged);
+/* The same for replica rep of a batch (0 <= rep < n_rep; MFA_ERR_ARG otherwise). */
+int mfa_kspace_info_replica(mfa_ctx* ctx, int32_t rep, int32_t* n_k, int32_t* n_charged);
 /* Absolute step counter of replica 0 (s_time + steps done). */
 int mfa_get_step(mfa_ctx* ctx, int64_t* step);
 

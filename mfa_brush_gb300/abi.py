@@ -196,6 +196,7 @@ SIGNATURES = {
     "mfa_list_stats": (i32, [vp, ip, ip]),
     "mfa_get_options": (i32, [vp, P(Options)]),
     "mfa_kspace_info": (i32, [vp, ip, ip]),
+    "mfa_kspace_info_replica": (i32, [vp, i32, ip, ip]),
     "mfa_reset_profiles": (i32, [vp]),
     "mfa_cell_list": (i32, [vp, i32, i32, ip, ip, i32, ip]),
     "mfa_cell_neigh_list": (i32, [ip, i32, ip]),

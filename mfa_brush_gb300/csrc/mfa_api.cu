@@ -1255,6 +1255,14 @@ int mfa_get_options(mfa_ctx* ctx, mfa_options* out) {
   return MFA_OK;
 }
 
+int mfa_kspace_info_replica(mfa_ctx* ctx, int32_t rep, int32_t* n_k, int32_t* n_charged) {
+  if (!ctx) return MFA_ERR_ARG;
+  if (rep < 0 || rep >= ctx->nrep) return fail(ctx, MFA_ERR_ARG, "kspace_info_replica: no such replica");
+  if (n_k) *n_k = ctx->kspace ? ctx->Ks[rep].nk : 0;
+  if (n_charged) *n_charged = ctx->kspace ? ctx->Ks[rep].nq : 0;
+  return MFA_OK;
+}
+
 int mfa_kspace_info(mfa_ctx* ctx, int32_t* n_k, int32_t* n_charged) {
   if (!ctx) return MFA_ERR_ARG;
   if (n_k) *n_k = ctx->kspace ? ctx->Ks[0].nk : 0;

@@ -263,10 +263,14 @@ class MdSystem:
         self._ck(self.lib.mfa_list_stats(self.ctx, C.byref(cap), C.byref(mx)))
         return cap.value, mx.value
 
-    def kspace_info(self):
-        """(k-vectors, charged particles) of the reciprocal-space sum; (0, 0) when uncharged."""
+    def kspace_info(self, rep=None):
+        """(k-vectors, charged particles) of the reciprocal-space sum of replica `rep` (replica 0
+        when None); (0, 0) when uncharged."""
         nk, nq = abi.i32(0), abi.i32(0)
-        self._ck(self.lib.mfa_kspace_info(self.ctx, C.byref(nk), C.byref(nq)))
+        if rep is None:
+            self._ck(self.lib.mfa_kspace_info(self.ctx, C.byref(nk), C.byref(nq)))
+        else:
+            self._ck(self.lib.mfa_kspace_info_replica(self.ctx, rep, C.byref(nk), C.byref(nq)))
         return nk.value, nq.value
 
     def averages(self):

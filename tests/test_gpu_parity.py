@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import assert_force_parity, rel_force_err
-from mfa_brush_gb300 import configs, md
+from mfa_brush_gb300 import abi, configs, md
 
 pytestmark = pytest.mark.gpu
 
@@ -377,6 +377,9 @@ def test_ewald_batch_matches_oracle_per_replica(gpu, oracle_mod, precision):
         off += n
     assert len(set(nks)) >= 2  # the replicas' boxes give different k-sets
     assert g.kspace_info()[0] == nks[0]  # mfa_kspace_info reports the first replica
+    assert [g.kspace_info(k)[0] for k in range(3)] == nks
+    with pytest.raises(abi.MfaError):
+        g.kspace_info(3)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
