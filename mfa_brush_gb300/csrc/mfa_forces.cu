@@ -546,6 +546,12 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
     ftot[2][threadIdx.x] = ez;
   }
   __syncthreads();
+  // Shared memory of the batch of kept list entries (a column per thread) and, in the energy
+  // variant with bonded terms, of the bonded virial partials after it: the batch is dead once
+  // the pair loop ends, and a barrier separates the two uses, so the variant keeps room for L1.
+  constexpr int JL_WORDS = PAIR_BATCH * 128;
+  constexpr int BV_WORDS = (EFLAG && BONDED) ? 128 * (int)(sizeof(BondVir<real_t<MIXED>>) / 4) : 0;
+  __shared__ __align__(16) int pair_pool[JL_WORDS > BV_WORDS ? JL_WORDS : BV_WORDS];
   real fx = 0, fy = 0, fz = 0;        // the current batch (FUSED), else the whole sum
   real e_lj = 0, e_c = 0;
   real wv[6] = {0, 0, 0, 0, 0, 0};   // EFLAG: pair virial, xx yy zz xy xz yz
@@ -601,8 +607,7 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
     // the batch's kept entries in shared memory, a column per thread (conflict-free): a
     // dynamically indexed local array lives in local memory, whose loads missed L1 behind the
     // gathers
-    __shared__ int jls[BATCH * 128];
-    int* const jl = jls + threadIdx.x;
+    int* const jl = pair_pool + threadIdx.x;
     int k = 0;
     // screening against the largest cut-off of the type pair; MIXED uses the coarse conversion
     // (512 fixed-point units of resolution, inside the 2e-4 margin of screen2)
@@ -681,9 +686,12 @@ __global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(Dev
   real eb[4] = {0, 0, 0, 0};
   // the bonded virial partials of the thread (EFLAG): in shared memory, where the bonded terms'
   // registers are scarce (27 words per thread: a stride prime to the 32 banks)
-  __shared__ BondVir<real> bvs[(EFLAG && BONDED) ? 128 : 1];
-  BondVir<real>& bv = bvs[(EFLAG && BONDED) ? threadIdx.x : 0];
-  if (EFLAG && BONDED) bv.zero();
+  __shared__ BondVir<real> bv_unused[1];  // the reference the other variants pass and never use
+  BondVir<real>& bv = (EFLAG && BONDED) ? reinterpret_cast<BondVir<real>*>(pair_pool)[threadIdx.x] : bv_unused[0];
+  if (EFLAG && BONDED) {
+    __syncthreads();  // every thread of the block is past its pair loop: the batch area is free
+    bv.zero();
+  }
   bool hb = false;
   double fxd = 0., fyd = 0., fzd = 0.;
   // INTEG with EFLAG: the integrator's kinetic energy, kinetic tensor and head forces
