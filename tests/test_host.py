@@ -157,6 +157,28 @@ def test_replica_workload_shapes():
     assert np.all(2 * sg * N <= 0.7 * 0.8 * D)
 
 
+def test_generated_bonds_stay_clear_of_the_fene_limit():
+    """The lattice spacing is capped at 1 sigma, so a chain's face-diagonal step is a bond of at
+    most sqrt(2) sigma (the FENE limit is 1.5 sigma; at 1.49 the start's bond force is ~4000) and
+    no two beads start closer than ~0.94 sigma: 16 replicas of the bench set and the melt."""
+    from scipy.spatial import cKDTree
+    from mfa_brush_gb300 import configs
+    reps = configs.replicas(256, 2024, indices=list(range(0, 256, 16)))
+    melt = configs.melt_brush(L=20.0, D=40.0)[1]
+    for s, a_type, r0, v in reps + [melt]:
+        L = np.array(list(s.boundary))
+        for st, nc, nm in ((0, s.n_chain, s.n_mon), (s.n_chain * s.n_mon, s.n_chain_d, s.n_mon_d)):
+            if nc == 0 or nm < 2:
+                continue
+            idx = st + np.arange(nc * nm).reshape(nc, nm)
+            d = r0[idx[:, 1:]] - r0[idx[:, :-1]]
+            d[..., :2] -= L[:2] * np.round(d[..., :2] / L[:2])
+            assert np.sqrt((d ** 2).sum(-1)).max() <= np.sqrt(2.0) + 1e-9
+        x = np.column_stack([r0[:, 0] % L[0], r0[:, 1] % L[1], r0[:, 2]])
+        dd, _ = cKDTree(x, boxsize=[L[0], L[1], 1e9]).query(x, k=2)
+        assert dd[:, 1].min() > 0.9
+
+
 def test_small_channel_is_well_formed():
     from mfa_brush_gb300 import configs
     s, a_type, r0, v = configs.small_channel()
