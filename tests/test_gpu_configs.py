@@ -701,3 +701,28 @@ def test_sheared_batch_equals_single(gpu):
         sg = np.where(np.arange(s.n_chain) < s.n_chain // 2, 1.0, -1.0)
         assert np.array_equal(v1[heads, 0], 0.3 * sg)
         off += n
+
+
+def test_moving_walls_batch_equals_single(gpu):
+    """Moving explicit walls in a batch: each replica's wall beads 1..n_wall/2 of its own count
+    move at +va, so two replicas of different sizes run batched give the same trajectories, bit
+    for bit, as each run alone (mixed, 40 fused steps, the walls passing half the skin)."""
+    inp = configs.wca_inputs(gamma=5.0, wall=1, dpd_cut_off=1.0)
+    inp.va_spring_twall[0], inp.va_spring_twall[1] = 1.0, 0.5
+    p, _ = md.derive(inp)
+    reps = [configs.explicit_wall_channel(seed=41, L=12.0, D=10.0),
+            configs.explicit_wall_channel(seed=42, L=14.0, D=12.0)]
+    systems, a_type, r0, v = configs.concat(reps)
+    gb = md.MdSystem(p, systems, a_type, r0, v, precision="mixed", nbr_capacity=160)
+    gb.step(40)
+    rb, vb, _, _ = gb.state()
+    gb.close()
+    off = 0
+    for s, at, rr, vv in reps:
+        g1 = md.MdSystem(p, s, at, rr, vv, precision="mixed", nbr_capacity=160)
+        g1.step(40)
+        r1, v1, _, _ = g1.state()
+        g1.close()
+        n = s.n_part
+        assert np.array_equal(r1, rb[off:off + n]) and np.array_equal(v1, vb[off:off + n])
+        off += n
