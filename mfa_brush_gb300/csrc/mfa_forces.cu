@@ -489,7 +489,11 @@ __device__ __forceinline__ real_t<MIXED> pair_fs(const DevState& s, const SimCon
 //           for 8 resident blocks per SM (64 registers): at 9 the tile loop spills.
 template <bool MIXED, bool EFLAG, bool FUSED = false, bool BONDED = false, bool UNI = false, bool PERSIST = false,
           bool INTEG = false>
-__global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : 9) : 4) k_pair(DevState s, SimConst C, bool accumulate,
+// Resident blocks per SM: 10 for the kernel with the integration in its tail (48 registers and a
+// 52-byte spill; 0.558 against 0.584 ms per step at 9 blocks, 56 registers; 11 or 12 blocks leave
+// 40 registers and spill 124 bytes: 0.579 ms), 9 for the other fused forms, 8 for the persistent
+// schedule (its tile loop spills at 9).
+__global__ void __launch_bounds__(128, MIXED ? (PERSIST ? 8 : ((INTEG && !EFLAG) ? 10 : 9)) : 4) k_pair(DevState s, SimConst C, bool accumulate,
                                                                              Acc acc, int bmask = 0) {
   using real = real_t<MIXED>;
   static_assert(!FUSED || MIXED, "the fused form is the mixed-precision one");
